@@ -1,0 +1,152 @@
+/*
+ * mc_dagprop_gb300.h -- C ABI of the GB300 Monte Carlo DAG-propagation engine.
+ *
+ * Plain C types only: pointers, sizes and opaque handles.  Every entry point
+ * returns an int status (MCD_OK = 0); on failure mcd_last_error() gives the
+ * message for the calling thread.  Nothing throws across this boundary.
+ *
+ * Each entry point replaces one piece of the reference's pybind11-bound C++
+ * (paths inside the reference project, src/mc_dagprop/monte_carlo/_core.cpp):
+ *
+ *   mcd_generator_*           GenericDelayGenerator            _core.cpp:146-159, 519-542
+ *   mcd_dag_create            Simulator::Simulator (DAG compile) _core.cpp:193-307
+ *   mcd_dag_node_count        Simulator::node_count            _core.cpp:309
+ *   mcd_dag_activity_count    Simulator::activity_count        _core.cpp:310
+ *   mcd_run_many_host         Simulator::run_many / run        _core.cpp:312-361
+ *   mcd_run_device            the same, device buffers, sample-minor layout
+ *   mcd_propagate_*           the propagation loop alone       _core.cpp:331-350
+ *   mcd_stats_*               per-event statistics (no reference counterpart;
+ *                             the reference's users stack run_many results in numpy)
+ *
+ * Layouts.  "Sample-major" (host entry points) is the reference's SimResult
+ * layout: one contiguous row per sample, realized[s*E + e], durations[s*L + l],
+ * cause_event[s*E + e].  "Sample-minor" (device entry points) is the GPU layout:
+ * one row per event / link with samples contiguous, realized[e*ld + s],
+ * durations[l*ld + s], cause_event[e*ld + s], ld >= n_samples.
+ *
+ * Random numbers.  Each sample s is identified by a 64-bit seed; delays are drawn
+ * from Philox4x32-10 keyed by that seed with the link index in the counter, so a
+ * sample's delays do not depend on which batch, chunk or position it runs in.
+ * Sampled delays therefore match the reference in distribution, not draw for
+ * draw; given the same durations, propagation reproduces the reference bit for bit.
+ */
+#ifndef MC_DAGPROP_GB300_H
+#define MC_DAGPROP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCD_ABI_VERSION 1
+
+/* Status codes. */
+#define MCD_OK 0
+#define MCD_ERR_INVALID 1  /* bad argument: maps to ValueError / TypeError           */
+#define MCD_ERR_RUNTIME 2  /* the reference's RuntimeError cases (cycle, reserved
+                              type -1, negative max_delay, table length mismatch)   */
+#define MCD_ERR_CUDA 3     /* CUDA runtime failure                                   */
+#define MCD_ERR_NOMEM 4    /* device or host allocation failed                       */
+#define MCD_ERR_DEVICE 5   /* a kernel reported an error (see message)              */
+
+typedef struct mcd_generator mcd_generator; /* GenericDelayGenerator */
+typedef struct mcd_dag mcd_dag;             /* compiled, device-resident Simulator */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *mcd_last_error(void);
+int mcd_abi_version(void);
+
+/* ---- GenericDelayGenerator (_core.cpp:146-159, bindings 519-542) ----
+ * A later add_* for the same activity_type replaces the earlier one.
+ * activity_type -1 is accepted here and rejected by mcd_dag_create, as in the
+ * reference (_core.cpp:196-198).  Empirical tables with values/weights of
+ * different lengths fail with MCD_ERR_RUNTIME (_core.cpp:119-120, 134-135). */
+int mcd_generator_create(mcd_generator **out);
+void mcd_generator_destroy(mcd_generator *gen);
+int mcd_generator_set_seed(mcd_generator *gen, int64_t seed); /* stored; unused by runs, as in the reference */
+int mcd_generator_add_constant(mcd_generator *gen, int32_t activity_type, double factor);
+int mcd_generator_add_exponential(mcd_generator *gen, int32_t activity_type, double lambda_, double max_scale);
+int mcd_generator_add_gamma(mcd_generator *gen, int32_t activity_type, double shape, double scale,
+                            double max_scale);
+int mcd_generator_add_empirical_absolute(mcd_generator *gen, int32_t activity_type, const double *values,
+                                         int64_t n_values, const double *weights, int64_t n_weights);
+int mcd_generator_add_empirical_relative(mcd_generator *gen, int32_t activity_type, const double *factors,
+                                         int64_t n_factors, const double *weights, int64_t n_weights);
+
+/* ---- DagContext, flattened (_core.cpp:52-62) ----
+ * events:          earliest[n_events] (EventTimestamp.latest/actual are not read by the path)
+ * activity map:    act_idx / act_duration / act_type [n_activities] (the (src,dst) key is not read)
+ * precedence_list: target[n_targets], pred_offsets[n_targets+1],
+ *                  pred_src / pred_act [pred_offsets[n_targets]] in list order */
+typedef struct mcd_dag_desc {
+    int32_t n_events;
+    const double *earliest;
+    int32_t n_activities;
+    const int32_t *act_idx;
+    const double *act_duration;
+    const int32_t *act_type;
+    int32_t n_targets;
+    const int32_t *target;
+    const int64_t *pred_offsets;
+    const int32_t *pred_src;
+    const int32_t *pred_act;
+    double max_delay;
+} mcd_dag_desc;
+
+/* Compiled-DAG facts, for tests and tuning. */
+typedef struct mcd_dag_info {
+    int32_t n_events, n_links, n_levels, n_warps;
+    int64_t n_preds;
+    int32_t window_slots;      /* live event rows a sample tile keeps on chip */
+    int32_t window_in_smem;    /* 1: window in shared memory, 0: re-read from global */
+    int32_t n_orphan_links;    /* links sampled but not referenced by precedence_list */
+    int32_t device;
+    int64_t device_bytes;      /* resident compiled-DAG bytes */
+} mcd_dag_info;
+
+/* Simulator::Simulator: validates, compiles to level-ordered CSR and uploads to
+ * the current CUDA device.  The generator is copied; both inputs may be freed
+ * afterwards.  Each handle owns one CUDA stream; a handle is not reentrant,
+ * separate handles run concurrently. */
+int mcd_dag_create(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag **out);
+void mcd_dag_destroy(mcd_dag *dag);
+int32_t mcd_dag_node_count(const mcd_dag *dag);
+int32_t mcd_dag_activity_count(const mcd_dag *dag);
+int mcd_dag_get_info(const mcd_dag *dag, mcd_dag_info *info);
+/* The handle's stream (a cudaStream_t), for callers that order their own work on it. */
+void *mcd_dag_stream(const mcd_dag *dag);
+
+/* ---- Host buffers, sample-major (reference SimResult layout) ----
+ * run_many over n seeds: realized[n*E], durations[n*L], cause_event[n*E];
+ * any output may be NULL.  Copies to and from the device happen inside; the call
+ * returns when the outputs are in host memory.  Pinned host memory
+ * (mcd_host_alloc) makes the copies run at full link speed. */
+int mcd_run_many_host(mcd_dag *dag, const int64_t *seeds, int64_t n, double *realized, double *durations,
+                      int32_t *cause_event);
+/* Propagation alone, given durations[n*L] (for example the reference's own
+ * SimResult.durations); bit-exact with the reference's loop. */
+int mcd_propagate_host(mcd_dag *dag, const double *durations, int64_t n, double *realized,
+                       int32_t *cause_event);
+
+/* ---- Device buffers, sample-minor, asynchronous on `stream` (NULL = the handle's stream) ----
+ * seeds[n] on the device; outputs realized[E*ld], durations[L*ld], cause_event[E*ld]
+ * (any may be NULL).  Kernel errors are latched on the handle and reported by
+ * mcd_dag_check(). */
+int mcd_run_device(mcd_dag *dag, const int64_t *seeds, int64_t n, double *realized, double *durations,
+                   int32_t *cause_event, int64_t ld, void *stream);
+/* Propagation alone from device durations[L*ld_in] (sample-minor). */
+int mcd_propagate_device(mcd_dag *dag, const double *durations, int64_t ld_in, int64_t n, double *realized,
+                         int32_t *cause_event, int64_t ld, void *stream);
+/* Synchronises the handle's stream and reports a latched kernel error, if any. */
+int mcd_dag_check(mcd_dag *dag);
+
+/* ---- Pinned host memory ---- */
+int mcd_host_alloc(size_t bytes, void **out);
+void mcd_host_free(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MC_DAGPROP_GB300_H */

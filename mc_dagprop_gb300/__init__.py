@@ -1,0 +1,39 @@
+"""GB300-native Monte Carlo DAG propagation, a drop-in for ``mc_dagprop``'s
+Monte Carlo path (``MonteCarloPropagator.run`` / ``run_many``).
+
+The compiled extension (``_core`` over ``_lib/libmcdagprop_gb300.so``) is
+required; there is no CPU fallback.  Build it with ``python -c "import
+__graft_entry__ as g; g.build()"`` or ``python mc_dagprop_gb300/_build.py``.
+"""
+from __future__ import annotations
+
+__version__ = "0.9.0+gb300"
+
+try:
+    from .monte_carlo import (
+        Activity,
+        DagContext,
+        Event,
+        EventTimestamp,
+        GenericDelayGenerator,
+        MonteCarloPropagator,
+        SimResult,
+        Simulator,
+    )
+except ImportError as exc:  # the compiled module is missing: fail loudly
+    raise ImportError(
+        "mc_dagprop_gb300 requires its compiled extension 'mc_dagprop_gb300._core' "
+        "(CUDA, sm_103a). Build it with `python mc_dagprop_gb300/_build.py`."
+    ) from exc
+
+__all__ = [
+    "GenericDelayGenerator",
+    "DagContext",
+    "SimResult",
+    "Event",
+    "Activity",
+    "Simulator",
+    "MonteCarloPropagator",
+    "EventTimestamp",
+    "__version__",
+]

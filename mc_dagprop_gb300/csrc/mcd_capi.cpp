@@ -1,0 +1,469 @@
+// mcd_capi.cpp -- the extern "C" entry points of include/mc_dagprop_gb300.h.
+//
+// Owns the compiled, device-resident DAG (one allocation), the handle's two CUDA
+// streams and a workspace for the host-buffer entry points, which run in
+// chunks: copy seeds in, run the fused kernel into sample-minor rows, transpose
+// to the reference's sample-major SimResult layout, copy out -- two chunks in
+// flight on alternating streams so copies overlap compute.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "mcd_host.hpp"
+
+namespace mcd {
+cudaError_t launch_propagate(const KArgs &a, bool given, bool win_smem, cudaStream_t st);
+cudaError_t launch_transpose_f64(const double *in, int64_t ld_in, double *out, int64_t ld_out, int64_t rows,
+                                 int64_t cols, cudaStream_t st);
+cudaError_t launch_transpose_i32(const int32_t *in, int64_t ld_in, int32_t *out, int64_t ld_out, int64_t rows,
+                                 int64_t cols, cudaStream_t st);
+}  // namespace mcd
+
+using namespace mcd;
+
+struct mcd_dag {
+    int device = 0;
+    cudaStream_t stream[2] = {nullptr, nullptr};
+    HostDag h;
+    char *dmem = nullptr;
+    size_t dbytes = 0;
+    EvRec *d_ev = nullptr;
+    PredRec *d_pred = nullptr;
+    LinkRec *d_aux = nullptr;
+    DistParam *d_dist = nullptr;
+    AliasEntry *d_alias = nullptr;
+    int32_t *d_wk = nullptr;
+    int32_t *d_err = nullptr;
+    char *ws = nullptr;  // workspace
+    size_t ws_bytes = 0;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+void cuda_check(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) {
+        if (e == cudaErrorMemoryAllocation)
+            throw McdError(MCD_ERR_NOMEM, std::string(what) + ": " + cudaGetErrorString(e));
+        throw McdError(MCD_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+template <typename F>
+int guarded(F &&f) {
+    try {
+        f();
+        g_last_error.clear();
+        return MCD_OK;
+    } catch (const McdError &e) {
+        return fail(e.code, e.what());
+    } catch (const std::bad_alloc &) {
+        return fail(MCD_ERR_NOMEM, "host allocation failed");
+    } catch (const std::exception &e) {
+        return fail(MCD_ERR_RUNTIME, e.what());
+    }
+}
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+void ensure_ws(mcd_dag *g, size_t bytes) {
+    if (bytes <= g->ws_bytes) return;
+    cuda_check(cudaStreamSynchronize(g->stream[0]), "stream sync");
+    cuda_check(cudaStreamSynchronize(g->stream[1]), "stream sync");
+    if (g->ws) cudaFree(g->ws);
+    g->ws = nullptr;
+    g->ws_bytes = 0;
+    cuda_check(cudaMalloc(&g->ws, bytes), "workspace allocation");
+    g->ws_bytes = bytes;
+}
+
+KArgs base_args(const mcd_dag *g) {
+    KArgs a{};
+    a.ev = g->d_ev;
+    a.pred = g->d_pred;
+    a.aux = g->d_aux;
+    a.dist = g->d_dist;
+    a.alias = g->d_alias;
+    a.wk_off = g->d_wk;
+    a.n_levels = g->h.n_levels;
+    a.n_warps = g->h.n_warps;
+    a.n_aux = (int32_t)g->h.aux.size();
+    a.window_slots = g->h.window_slots;
+    a.err = g->d_err;
+    return a;
+}
+
+void check_device_error(mcd_dag *g) {
+    cuda_check(cudaStreamSynchronize(g->stream[0]), "stream sync");
+    cuda_check(cudaStreamSynchronize(g->stream[1]), "stream sync");
+    int32_t flags = 0;
+    cuda_check(cudaMemcpy(&flags, g->d_err, sizeof(flags), cudaMemcpyDeviceToHost), "error flag read");
+    if (flags) {
+        cuda_check(cudaMemset(g->d_err, 0, sizeof(int32_t)), "error flag reset");
+        if (flags & ERR_GAMMA_REJECTION)
+            throw McdError(MCD_ERR_DEVICE,
+                           "gamma sampler: truncation at max_scale rejected 8192 consecutive draws; "
+                           "max_scale is too small for this shape/scale");
+        throw McdError(MCD_ERR_DEVICE, "kernel reported error flags " + std::to_string(flags));
+    }
+}
+
+// Samples per chunk for the host-buffer entry points: two chunk buffer sets
+// (sample-minor rows + sample-major rows) within ~2 GiB, a multiple of 32.
+int64_t host_chunk(const mcd_dag *g, int64_t n) {
+    const double per_sample = 2.0 * (12.0 * g->h.E + 8.0 * g->h.L) + 8.0;
+    int64_t c = (int64_t)((double)(1ll << 30) / std::max(per_sample, 1.0));
+    c = std::max<int64_t>(32, c / 32 * 32);
+    const int64_t n32 = (n + 31) / 32 * 32;
+    return std::min(c, std::max<int64_t>(32, n32));
+}
+
+struct ChunkBufs {
+    int64_t *seeds;
+    double *real_minor, *dur_minor;
+    int32_t *cause_minor;
+    double *real_major, *dur_major;
+    int32_t *cause_major;
+};
+
+// Carves two chunk buffer sets of C samples out of the workspace.
+void carve(mcd_dag *g, int64_t C, ChunkBufs cb[2]) {
+    const size_t E = (size_t)g->h.E, L = (size_t)g->h.L;
+    const size_t sz_seed = align_up((size_t)C * 8, 256), sz_re = align_up(E * (size_t)C * 8, 256),
+                 sz_du = align_up(L * (size_t)C * 8, 256), sz_ca = align_up(E * (size_t)C * 4, 256);
+    const size_t per = sz_seed + 2 * (sz_re + sz_du + sz_ca);
+    ensure_ws(g, 2 * per);
+    for (int k = 0; k < 2; ++k) {
+        char *p = g->ws + k * per;
+        cb[k].seeds = (int64_t *)p;
+        p += sz_seed;
+        cb[k].real_minor = (double *)p;
+        p += sz_re;
+        cb[k].dur_minor = (double *)p;
+        p += sz_du;
+        cb[k].cause_minor = (int32_t *)p;
+        p += sz_ca;
+        cb[k].real_major = (double *)p;
+        p += sz_re;
+        cb[k].dur_major = (double *)p;
+        p += sz_du;
+        cb[k].cause_major = (int32_t *)p;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *mcd_last_error(void) { return g_last_error.c_str(); }
+int mcd_abi_version(void) { return MCD_ABI_VERSION; }
+
+int mcd_generator_create(mcd_generator **out) {
+    return guarded([&] {
+        if (!out) throw McdError(MCD_ERR_INVALID, "null output pointer");
+        *out = new mcd_generator();
+    });
+}
+
+void mcd_generator_destroy(mcd_generator *g) { delete g; }
+
+int mcd_generator_set_seed(mcd_generator *g, int64_t seed) {
+    return guarded([&] {
+        if (!g) throw McdError(MCD_ERR_INVALID, "null generator");
+        g->seed = seed;
+    });
+}
+
+static int add_dist(mcd_generator *g, int32_t type, int32_t kind, double p0, double p1, double p2) {
+    return guarded([&] {
+        if (!g) throw McdError(MCD_ERR_INVALID, "null generator");
+        g->dists.push_back(DistSpec{type, kind, p0, p1, p2, {}, {}});
+    });
+}
+
+int mcd_generator_add_constant(mcd_generator *g, int32_t t, double factor) {
+    return add_dist(g, t, MCD_KIND_CONSTANT, factor, 0.0, 0.0);
+}
+int mcd_generator_add_exponential(mcd_generator *g, int32_t t, double lambda_, double max_scale) {
+    return add_dist(g, t, MCD_KIND_EXPONENTIAL, lambda_, max_scale, 0.0);
+}
+int mcd_generator_add_gamma(mcd_generator *g, int32_t t, double shape, double scale, double max_scale) {
+    return add_dist(g, t, MCD_KIND_GAMMA, shape, scale, max_scale);
+}
+
+static int add_table(mcd_generator *g, int32_t t, int32_t kind, const double *v, int64_t nv, const double *w,
+                     int64_t nw, const char *what) {
+    return guarded([&] {
+        if (!g) throw McdError(MCD_ERR_INVALID, "null generator");
+        if (nv != nw)  // _core.cpp:119-120, 134-135
+            throw McdError(MCD_ERR_RUNTIME, std::string(what) + " and weights must have same length");
+        if (nv < 0 || (nv > 0 && (!v || !w))) throw McdError(MCD_ERR_INVALID, "bad table arguments");
+        DistSpec s{t, kind, 0.0, 0.0, 0.0, std::vector<double>(v, v + nv), std::vector<double>(w, w + nw)};
+        g->dists.push_back(std::move(s));
+    });
+}
+
+int mcd_generator_add_empirical_absolute(mcd_generator *g, int32_t t, const double *values, int64_t nv,
+                                         const double *weights, int64_t nw) {
+    return add_table(g, t, MCD_KIND_EMP_ABS, values, nv, weights, nw, "EmpiricalAbsoluteDist: values");
+}
+int mcd_generator_add_empirical_relative(mcd_generator *g, int32_t t, const double *factors, int64_t nf,
+                                         const double *weights, int64_t nw) {
+    return add_table(g, t, MCD_KIND_EMP_REL, factors, nf, weights, nw, "EmpiricalRelativeDist: factors");
+}
+
+int mcd_dag_create(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag **out) {
+    mcd_dag *g = nullptr;
+    int rc = guarded([&] {
+        if (!desc || !gen || !out) throw McdError(MCD_ERR_INVALID, "null argument");
+        *out = nullptr;
+        g = new mcd_dag();
+        compile_dag(*desc, *gen, g->h);
+        cuda_check(cudaGetDevice(&g->device), "cudaGetDevice");
+        for (int k = 0; k < 2; ++k)
+            cuda_check(cudaStreamCreateWithFlags(&g->stream[k], cudaStreamNonBlocking), "stream create");
+        const HostDag &h = g->h;
+        const size_t s_ev = align_up(h.ev.size() * sizeof(EvRec), 256),
+                     s_pred = align_up(h.pred.size() * sizeof(PredRec), 256),
+                     s_aux = align_up(h.aux.size() * sizeof(LinkRec), 256),
+                     s_dist = align_up(h.dist.size() * sizeof(DistParam), 256),
+                     s_alias = align_up(h.alias.size() * sizeof(AliasEntry), 256),
+                     s_wk = align_up(h.wk_off.size() * sizeof(int32_t), 256), s_err = 256;
+        g->dbytes = s_ev + s_pred + s_aux + s_dist + s_alias + s_wk + s_err;
+        cuda_check(cudaMalloc(&g->dmem, g->dbytes), "compiled DAG allocation");
+        char *p = g->dmem;
+        auto place = [&](auto *&dst, const auto &vec, size_t sz) {
+            dst = reinterpret_cast<std::remove_reference_t<decltype(dst)>>(p);
+            if (!vec.empty())
+                cuda_check(cudaMemcpy(p, vec.data(), vec.size() * sizeof(vec[0]), cudaMemcpyHostToDevice),
+                           "compiled DAG upload");
+            p += sz;
+        };
+        place(g->d_ev, h.ev, s_ev);
+        place(g->d_pred, h.pred, s_pred);
+        place(g->d_aux, h.aux, s_aux);
+        place(g->d_dist, h.dist, s_dist);
+        place(g->d_alias, h.alias, s_alias);
+        place(g->d_wk, h.wk_off, s_wk);
+        g->d_err = reinterpret_cast<int32_t *>(p);
+        cuda_check(cudaMemset(g->d_err, 0, sizeof(int32_t)), "error flag init");
+        *out = g;
+    });
+    if (rc != MCD_OK && g) {
+        std::string keep = g_last_error;
+        mcd_dag_destroy(g);
+        g_last_error = keep;
+    }
+    return rc;
+}
+
+void mcd_dag_destroy(mcd_dag *g) {
+    if (!g) return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(g->device);
+    for (int k = 0; k < 2; ++k)
+        if (g->stream[k]) {
+            cudaStreamSynchronize(g->stream[k]);
+            cudaStreamDestroy(g->stream[k]);
+        }
+    if (g->ws) cudaFree(g->ws);
+    if (g->dmem) cudaFree(g->dmem);
+    cudaSetDevice(prev);
+    delete g;
+}
+
+int32_t mcd_dag_node_count(const mcd_dag *g) { return g ? g->h.E : -1; }
+int32_t mcd_dag_activity_count(const mcd_dag *g) { return g ? g->h.L : -1; }
+void *mcd_dag_stream(const mcd_dag *g) { return g ? (void *)g->stream[0] : nullptr; }
+
+int mcd_dag_get_info(const mcd_dag *g, mcd_dag_info *info) {
+    return guarded([&] {
+        if (!g || !info) throw McdError(MCD_ERR_INVALID, "null argument");
+        info->n_events = g->h.E;
+        info->n_links = g->h.L;
+        info->n_levels = g->h.n_levels;
+        info->n_warps = g->h.n_warps;
+        info->n_preds = (int64_t)g->h.pred.size();
+        info->window_slots = g->h.window_slots;
+        info->window_in_smem = g->h.win_smem ? 1 : 0;
+        info->n_orphan_links = g->h.n_orphan;
+        info->device = g->device;
+        info->device_bytes = (int64_t)g->dbytes;
+    });
+}
+
+int mcd_dag_check(mcd_dag *g) {
+    return guarded([&] {
+        if (!g) throw McdError(MCD_ERR_INVALID, "null handle");
+        cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
+        check_device_error(g);
+    });
+}
+
+int mcd_run_device(mcd_dag *g, const int64_t *seeds, int64_t n, double *realized, double *durations,
+                   int32_t *cause, int64_t ld, void *stream) {
+    return guarded([&] {
+        if (!g) throw McdError(MCD_ERR_INVALID, "null handle");
+        if (n < 0 || ld < n) throw McdError(MCD_ERR_INVALID, "need 0 <= n <= ld");
+        if (n > 0 && !seeds) throw McdError(MCD_ERR_INVALID, "null seeds");
+        cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
+        cudaStream_t st = stream ? (cudaStream_t)stream : g->stream[0];
+        KArgs a = base_args(g);
+        a.seeds = seeds;
+        a.n = n;
+        a.ld = ld;
+        a.realized = realized;
+        a.durations = durations;
+        a.cause = cause;
+        if (!g->h.win_smem && !realized) {
+            ensure_ws(g, (size_t)g->h.E * (size_t)ld * 8);
+            a.scratch = (double *)g->ws;
+        }
+        cuda_check(launch_propagate(a, false, g->h.win_smem, st), "propagate launch");
+    });
+}
+
+int mcd_propagate_device(mcd_dag *g, const double *dur, int64_t ld_in, int64_t n, double *realized,
+                         int32_t *cause, int64_t ld, void *stream) {
+    return guarded([&] {
+        if (!g) throw McdError(MCD_ERR_INVALID, "null handle");
+        if (n < 0 || ld < n || ld_in < n) throw McdError(MCD_ERR_INVALID, "need 0 <= n <= ld, ld_in");
+        if (n > 0 && g->h.L > 0 && !dur) throw McdError(MCD_ERR_INVALID, "null durations");
+        cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
+        cudaStream_t st = stream ? (cudaStream_t)stream : g->stream[0];
+        KArgs a = base_args(g);
+        a.n = n;
+        a.ld = ld;
+        a.realized = realized;
+        a.cause = cause;
+        a.dur_in = dur;
+        a.ld_in = ld_in;
+        if (!g->h.win_smem && !realized) {
+            ensure_ws(g, (size_t)g->h.E * (size_t)ld * 8);
+            a.scratch = (double *)g->ws;
+        }
+        cuda_check(launch_propagate(a, true, g->h.win_smem, st), "propagate launch");
+    });
+}
+
+int mcd_run_many_host(mcd_dag *g, const int64_t *seeds, int64_t n, double *realized, double *durations,
+                      int32_t *cause) {
+    return guarded([&] {
+        if (!g) throw McdError(MCD_ERR_INVALID, "null handle");
+        if (n < 0) throw McdError(MCD_ERR_INVALID, "negative sample count");
+        if (n == 0) return;
+        if (!seeds) throw McdError(MCD_ERR_INVALID, "null seeds");
+        cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
+        const int64_t E = g->h.E, L = g->h.L;
+        const int64_t C = host_chunk(g, n);
+        ChunkBufs cb[2];
+        carve(g, C, cb);
+        int64_t idx = 0;
+        for (int64_t off = 0; off < n; off += C, ++idx) {
+            const int k = (int)(idx & 1);
+            cudaStream_t st = g->stream[k];
+            const int64_t m = std::min(C, n - off);
+            cuda_check(cudaMemcpyAsync(cb[k].seeds, seeds + off, (size_t)m * 8, cudaMemcpyHostToDevice, st),
+                       "seed upload");
+            KArgs a = base_args(g);
+            a.seeds = cb[k].seeds;
+            a.n = m;
+            a.ld = C;
+            a.realized = cb[k].real_minor;  // always: also the spill rows of a global window
+            a.durations = durations ? cb[k].dur_minor : nullptr;
+            a.cause = cause ? cb[k].cause_minor : nullptr;
+            cuda_check(launch_propagate(a, false, g->h.win_smem, st), "propagate launch");
+            if (realized) {
+                cuda_check(launch_transpose_f64(cb[k].real_minor, C, cb[k].real_major, E, E, m, st), "transpose");
+                cuda_check(cudaMemcpyAsync(realized + off * E, cb[k].real_major, (size_t)(m * E) * 8,
+                                           cudaMemcpyDeviceToHost, st),
+                           "realized download");
+            }
+            if (durations) {
+                cuda_check(launch_transpose_f64(cb[k].dur_minor, C, cb[k].dur_major, L, L, m, st), "transpose");
+                cuda_check(cudaMemcpyAsync(durations + off * L, cb[k].dur_major, (size_t)(m * L) * 8,
+                                           cudaMemcpyDeviceToHost, st),
+                           "durations download");
+            }
+            if (cause) {
+                cuda_check(launch_transpose_i32(cb[k].cause_minor, C, cb[k].cause_major, E, E, m, st),
+                           "transpose");
+                cuda_check(cudaMemcpyAsync(cause + off * E, cb[k].cause_major, (size_t)(m * E) * 4,
+                                           cudaMemcpyDeviceToHost, st),
+                           "cause download");
+            }
+        }
+        check_device_error(g);
+    });
+}
+
+int mcd_propagate_host(mcd_dag *g, const double *durations, int64_t n, double *realized, int32_t *cause) {
+    return guarded([&] {
+        if (!g) throw McdError(MCD_ERR_INVALID, "null handle");
+        if (n < 0) throw McdError(MCD_ERR_INVALID, "negative sample count");
+        if (n == 0) return;
+        if (!durations && g->h.L > 0) throw McdError(MCD_ERR_INVALID, "null durations");
+        cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
+        const int64_t E = g->h.E, L = g->h.L;
+        const int64_t C = host_chunk(g, n);
+        ChunkBufs cb[2];
+        carve(g, C, cb);
+        int64_t idx = 0;
+        for (int64_t off = 0; off < n; off += C, ++idx) {
+            const int k = (int)(idx & 1);
+            cudaStream_t st = g->stream[k];
+            const int64_t m = std::min(C, n - off);
+            if (L > 0) {
+                cuda_check(cudaMemcpyAsync(cb[k].dur_major, durations + off * L, (size_t)(m * L) * 8,
+                                           cudaMemcpyHostToDevice, st),
+                           "durations upload");
+                cuda_check(launch_transpose_f64(cb[k].dur_major, L, cb[k].dur_minor, C, m, L, st), "transpose");
+            }
+            KArgs a = base_args(g);
+            a.n = m;
+            a.ld = C;
+            a.realized = cb[k].real_minor;
+            a.cause = cause ? cb[k].cause_minor : nullptr;
+            a.dur_in = cb[k].dur_minor;
+            a.ld_in = C;
+            cuda_check(launch_propagate(a, true, g->h.win_smem, st), "propagate launch");
+            if (realized) {
+                cuda_check(launch_transpose_f64(cb[k].real_minor, C, cb[k].real_major, E, E, m, st), "transpose");
+                cuda_check(cudaMemcpyAsync(realized + off * E, cb[k].real_major, (size_t)(m * E) * 8,
+                                           cudaMemcpyDeviceToHost, st),
+                           "realized download");
+            }
+            if (cause) {
+                cuda_check(launch_transpose_i32(cb[k].cause_minor, C, cb[k].cause_major, E, E, m, st),
+                           "transpose");
+                cuda_check(cudaMemcpyAsync(cause + off * E, cb[k].cause_major, (size_t)(m * E) * 4,
+                                           cudaMemcpyDeviceToHost, st),
+                           "cause download");
+            }
+        }
+        check_device_error(g);
+    });
+}
+
+int mcd_host_alloc(size_t bytes, void **out) {
+    return guarded([&] {
+        if (!out) throw McdError(MCD_ERR_INVALID, "null output pointer");
+        *out = nullptr;
+        cuda_check(cudaHostAlloc(out, std::max<size_t>(bytes, 1), cudaHostAllocDefault), "pinned allocation");
+    });
+}
+
+void mcd_host_free(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

@@ -1,0 +1,430 @@
+// mcd_compile.cpp -- host DAG compiler: DagContext + GenericDelayGenerator ->
+// level-ordered CSR records for the kernels.
+//
+// Mirrors Simulator::Simulator (src/mc_dagprop/monte_carlo/_core.cpp:193-307):
+//   - the same three RuntimeError cases with the same messages
+//     (reserved type -1 :196-198, negative max_delay :199-201, cycle :262-264);
+//   - dense link array of max idx + 1 entries, gaps of duration 0 with no delay,
+//     unmapped types with no delay (:213-229);
+//   - predecessors of each event kept in precedence-list order (:267-285).
+// Where the reference has undefined behaviour (indices out of range, a target
+// listed twice, empty tables, parameters for which its rejection loops never
+// end) this compiler rejects the input with MCD_ERR_INVALID instead.
+//
+// Compiled with -ffp-contract=off: `base + base*factor` and `earliest +
+// max_delay` must round exactly as the reference's two separate operations.
+#include "mcd_host.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <deque>
+#include <limits>
+#include <string>
+#include <unordered_map>
+
+namespace mcd {
+
+int64_t order_key_host(int64_t b) {
+    const int64_t mag = b & 0x7FFFFFFFFFFFFFFFll;
+    const int64_t k = b < 0 ? -mag : mag;
+    return mag > 0x7FF0000000000000ll ? std::numeric_limits<int64_t>::min() : k;
+}
+
+static int64_t bits_of(double x) {
+    int64_t b;
+    std::memcpy(&b, &x, sizeof(b));
+    return b;
+}
+
+// Largest float not above x (x may be +inf).
+static float float_at_or_below(double x) {
+    float f = (float)x;
+    if ((double)f > x) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
+    return f;
+}
+
+static uint32_t keep_threshold(double prob) {
+    if (!(prob < 1.0)) return 0xFFFFFFFFu;
+    if (!(prob > 0.0)) return 0u;
+    const double t = std::floor(prob * 4294967296.0);
+    return t >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)t;
+}
+
+// Walker/Vose alias table over weights w (validated: finite, >= 0, sum > 0).
+static void build_alias(const std::vector<double> &values, const std::vector<double> &w,
+                        std::vector<AliasEntry> &out) {
+    const size_t n = w.size();
+    double sum = 0.0;
+    for (double x : w) sum += x;
+    std::vector<double> q(n);
+    for (size_t i = 0; i < n; ++i) q[i] = w[i] / sum * (double)n;
+    std::vector<int64_t> small, large;
+    for (size_t i = 0; i < n; ++i) (q[i] < 1.0 ? small : large).push_back((int64_t)i);
+    std::vector<double> prob(n, 1.0);
+    std::vector<int64_t> alias(n);
+    for (size_t i = 0; i < n; ++i) alias[i] = (int64_t)i;
+    while (!small.empty() && !large.empty()) {
+        const int64_t s = small.back();
+        small.pop_back();
+        const int64_t l = large.back();
+        large.pop_back();
+        prob[s] = q[s];
+        alias[s] = l;
+        q[l] = (q[l] + q[s]) - 1.0;
+        (q[l] < 1.0 ? small : large).push_back(l);
+    }
+    // Leftovers (rounding) keep their own bin.
+    for (size_t i = 0; i < n; ++i) {
+        AliasEntry e{};
+        e.v_self = values[i];
+        e.thresh = keep_threshold(prob[i]);
+        e.v_alias = e.thresh == 0xFFFFFFFFu ? values[i] : values[(size_t)alias[i]];
+        out.push_back(e);
+    }
+}
+
+static void check_table(const DistSpec &d) {
+    if (d.values.empty()) throw McdError(MCD_ERR_INVALID, "empirical distribution needs at least one value");
+    double sum = 0.0;
+    for (double x : d.weights) {
+        if (!(x >= 0.0) || !std::isfinite(x))
+            throw McdError(MCD_ERR_INVALID, "empirical weights must be finite and non-negative");
+        sum += x;
+    }
+    if (!(sum > 0.0)) throw McdError(MCD_ERR_INVALID, "empirical weights must not all be zero");
+}
+
+void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H) {
+    // ---- 1) distributions: the last add_* per type wins (README semantics of dist_map_)
+    std::unordered_map<int32_t, size_t> type_spec;
+    for (size_t i = 0; i < g.dists.size(); ++i) type_spec[g.dists[i].type] = i;
+    if (type_spec.count(-1)) throw McdError(MCD_ERR_RUNTIME, "Activity type -1 is reserved for no delay");
+    if (d.max_delay < 0.0) throw McdError(MCD_ERR_RUNTIME, "max_delay must be non-negative");
+    if (d.n_events < 0 || d.n_activities < 0 || d.n_targets < 0)
+        throw McdError(MCD_ERR_INVALID, "negative array length in DAG description");
+
+    // Per-type compiled form: constant and degenerate laws become FIXED.
+    struct TypeForm {
+        int32_t kind;    // K_FIXED when duration = f(base) without randomness
+        int32_t dist;    // index into H.dist
+        int32_t fixed;   // 0: none, 1: base*(1+factor) style constant, 2: emp single value
+        double factor;   // constant factor / single empirical value
+        bool relative;
+    };
+    std::unordered_map<int32_t, TypeForm> form;
+    H.dist.clear();
+    H.alias.clear();
+    for (const auto &kv : type_spec) {
+        const DistSpec &s = g.dists[kv.second];
+        TypeForm f{K_FIXED, -1, 0, 0.0, false};
+        switch (s.kind) {
+            case MCD_KIND_CONSTANT:
+                f.fixed = 1;
+                f.factor = s.p0;
+                break;
+            case MCD_KIND_EXPONENTIAL: {
+                const double lam = s.p0;
+                double ms = s.p1;
+                if (std::isnan(lam) || lam < 0.0 || std::isinf(lam))
+                    throw McdError(MCD_ERR_INVALID, "exponential lambda_ must be finite and non-negative");
+                if (std::isnan(ms)) ms = INFINITY;  // x > NaN is never true: no truncation
+                if (ms < 0.0) throw McdError(MCD_ERR_INVALID, "exponential max_scale must be non-negative");
+                if (lam == 0.0) {  // rate 1/0: every draw is 0
+                    f.fixed = 1;
+                    f.factor = 0.0;
+                    break;
+                }
+                DistParam p{};
+                p.kind = K_EXP;
+                const double ratio = ms / lam;
+                const double c = std::isinf(ratio) ? 1.0 : -std::expm1(-ratio);
+                const double omc = std::isinf(ratio) ? 0.0 : std::exp(-ratio);
+                p.f0 = (float)lam;
+                p.f1 = (float)c;
+                p.f2 = (float)omc;
+                p.f3 = float_at_or_below(ms);
+                f.kind = K_EXP;
+                f.dist = (int32_t)H.dist.size();
+                H.dist.push_back(p);
+                break;
+            }
+            case MCD_KIND_GAMMA: {
+                const double k = s.p0, theta = s.p1;
+                double ms = s.p2;
+                if (!(k > 0.0) || std::isinf(k))
+                    throw McdError(MCD_ERR_INVALID, "gamma shape must be finite and positive");
+                if (!(theta >= 0.0) || std::isinf(theta))
+                    throw McdError(MCD_ERR_INVALID, "gamma scale must be finite and non-negative");
+                if (std::isnan(ms)) ms = INFINITY;
+                if (theta == 0.0) {
+                    f.fixed = 1;
+                    f.factor = 0.0;
+                    break;
+                }
+                if (!(ms > 0.0))
+                    throw McdError(MCD_ERR_INVALID, "gamma max_scale must be positive (no draw would be accepted)");
+                DistParam p{};
+                p.kind = K_GAMMA;
+                const double kk = k < 1.0 ? k + 1.0 : k;
+                const double dd = kk - 1.0 / 3.0;
+                p.boost = k < 1.0 ? 1 : 0;
+                p.f0 = (float)dd;
+                p.f1 = (float)(1.0 / std::sqrt(9.0 * dd));
+                p.f2 = (float)(1.0 / k);
+                p.f3 = (float)theta;
+                p.f4 = float_at_or_below(ms);
+                f.kind = K_GAMMA;
+                f.dist = (int32_t)H.dist.size();
+                H.dist.push_back(p);
+                break;
+            }
+            case MCD_KIND_EMP_ABS:
+            case MCD_KIND_EMP_REL: {
+                check_table(s);
+                f.relative = s.kind == MCD_KIND_EMP_REL;
+                if (s.values.size() == 1) {  // the reference draws nothing for one entry
+                    f.fixed = 2;
+                    f.factor = s.values[0];
+                    break;
+                }
+                DistParam p{};
+                p.kind = f.relative ? K_EMP_REL : K_EMP_ABS;
+                p.tab_off = (int32_t)H.alias.size();
+                p.tab_n = (int32_t)s.values.size();
+                build_alias(s.values, s.weights, H.alias);
+                f.kind = p.kind;
+                f.dist = (int32_t)H.dist.size();
+                H.dist.push_back(p);
+                break;
+            }
+            default: throw McdError(MCD_ERR_INVALID, "unknown distribution kind");
+        }
+        form[kv.first] = f;
+    }
+
+    // ---- 2) dense links (_core.cpp:213-229)
+    int32_t max_idx = -1;
+    for (int32_t k = 0; k < d.n_activities; ++k) {
+        if (d.act_idx[k] < 0) throw McdError(MCD_ERR_INVALID, "Activity.idx must be non-negative");
+        max_idx = std::max(max_idx, d.act_idx[k]);
+    }
+    const int32_t L = max_idx + 1;
+    H.L = L;
+    H.link_kd.assign((size_t)L, K_FIXED);
+    H.link_v.assign((size_t)L, 0.0);  // gaps: duration 0, no delay
+    for (int32_t k = 0; k < d.n_activities; ++k) {
+        const int32_t l = d.act_idx[k];
+        const double base = d.act_duration[k];
+        auto it = form.find(d.act_type[k]);
+        if (it == form.end()) {
+            H.link_kd[l] = K_FIXED;
+            H.link_v[l] = base;
+            continue;
+        }
+        const TypeForm &f = it->second;
+        if (f.kind == K_FIXED) {
+            double extra;
+            if (f.fixed == 1) extra = base * f.factor;            // _core.cpp:75
+            else extra = f.relative ? f.factor * base : f.factor;  // _core.cpp:125, 140
+            H.link_kd[l] = K_FIXED;
+            H.link_v[l] = base + extra;                           // _core.cpp:328
+        } else {
+            H.link_kd[l] = f.kind | (f.dist << 8);
+            H.link_v[l] = base;
+        }
+    }
+
+    // ---- 3) precedence list, predecessors by target
+    const int32_t E = d.n_events;
+    H.E = E;
+    std::vector<int64_t> tstart((size_t)E, -1), tlen((size_t)E, 0);
+    for (int32_t t = 0; t < d.n_targets; ++t) {
+        const int32_t tgt = d.target[t];
+        if (tgt < 0 || tgt >= E) throw McdError(MCD_ERR_INVALID, "precedence_list target out of range");
+        if (tstart[tgt] != -1)
+            throw McdError(MCD_ERR_INVALID, "precedence_list names target " + std::to_string(tgt) + " twice");
+        const int64_t b = d.pred_offsets[t], e = d.pred_offsets[t + 1];
+        if (e < b) throw McdError(MCD_ERR_INVALID, "pred_offsets must be non-decreasing");
+        tstart[tgt] = b;
+        tlen[tgt] = e - b;
+        for (int64_t p = b; p < e; ++p) {
+            if (d.pred_src[p] < 0 || d.pred_src[p] >= E)
+                throw McdError(MCD_ERR_INVALID, "predecessor event index out of range");
+            if (d.pred_act[p] < 0) throw McdError(MCD_ERR_INVALID, "predecessor activity index is negative");
+        }
+    }
+    if (d.n_targets > 0 && d.pred_offsets[d.n_targets] > (int64_t)std::numeric_limits<int32_t>::max())
+        throw McdError(MCD_ERR_INVALID, "too many predecessor entries");
+
+    // ---- 4) Kahn order (_core.cpp:235-264), with levels = longest path from a source
+    std::vector<int64_t> adj_off((size_t)E + 1, 0);
+    for (int32_t e = 0; e < E; ++e)
+        for (int64_t k = 0; k < tlen[e]; ++k) adj_off[(size_t)d.pred_src[tstart[e] + k] + 1]++;
+    for (int32_t e = 0; e < E; ++e) adj_off[e + 1] += adj_off[e];
+    std::vector<int32_t> adj((size_t)adj_off[E]);
+    {
+        std::vector<int64_t> fill(adj_off.begin(), adj_off.end() - 1);
+        for (int32_t e = 0; e < E; ++e)
+            for (int64_t k = 0; k < tlen[e]; ++k) adj[(size_t)fill[(size_t)d.pred_src[tstart[e] + k]]++] = e;
+    }
+    std::vector<int64_t> indeg(tlen);
+    std::vector<int32_t> level((size_t)E, 0);
+    std::vector<int32_t> queue;
+    queue.reserve((size_t)E);
+    for (int32_t e = 0; e < E; ++e)
+        if (indeg[e] == 0) queue.push_back(e);
+    for (size_t qh = 0; qh < queue.size(); ++qh) {
+        const int32_t nd = queue[qh];
+        for (int64_t k = adj_off[nd]; k < adj_off[nd + 1]; ++k) {
+            const int32_t c = adj[(size_t)k];
+            level[c] = std::max(level[c], level[nd] + 1);
+            if (--indeg[c] == 0) queue.push_back(c);
+        }
+    }
+    if ((int64_t)queue.size() != (int64_t)E)
+        throw McdError(MCD_ERR_RUNTIME, "Invalid DAG: cycle detected in precedence list");
+    int32_t n_levels = 0;
+    for (int32_t e = 0; e < E; ++e) n_levels = std::max(n_levels, level[e] + 1);
+    H.n_levels = n_levels;
+
+    // ---- 5) last level at which each event is read
+    std::vector<int32_t> last_use((size_t)E, -1);
+    for (int32_t e = 0; e < E; ++e)
+        for (int64_t k = 0; k < tlen[e]; ++k) {
+            const int32_t s = d.pred_src[tstart[e] + k];
+            last_use[s] = std::max(last_use[s], level[e]);
+        }
+
+    // ---- 6) events by level (stable in caller order)
+    std::vector<int32_t> lvl_off((size_t)n_levels + 1, 0);
+    for (int32_t e = 0; e < E; ++e) lvl_off[(size_t)level[e] + 1]++;
+    for (int32_t l = 0; l < n_levels; ++l) lvl_off[l + 1] += lvl_off[l];
+    std::vector<int32_t> by_level((size_t)E);
+    {
+        std::vector<int32_t> fill(lvl_off.begin(), lvl_off.end() - 1);
+        for (int32_t e = 0; e < E; ++e) by_level[(size_t)fill[(size_t)level[e]]++] = e;
+    }
+
+    // ---- 7) warps per CTA and per-(level, warp) chunks balanced by edge count
+    int32_t nw = 1;
+    if (n_levels > 0) {
+        const double avg_width = (double)E / (double)n_levels;
+        nw = (int32_t)std::ceil(avg_width / 6.0);
+    }
+    if (const char *env = std::getenv("MCD_WARPS")) nw = std::atoi(env);
+    nw = std::max(1, std::min(16, nw));
+    H.n_warps = nw;
+    H.wk_off.assign((size_t)n_levels * nw + 1, 0);
+    std::vector<int32_t> order;  // compiled order
+    order.reserve((size_t)E);
+    for (int32_t l = 0; l < n_levels; ++l) {
+        const int32_t b = lvl_off[l], e = lvl_off[l + 1];
+        double total = 0.0;
+        for (int32_t i = b; i < e; ++i) total += 1.0 + (double)tlen[by_level[i]];
+        double acc = 0.0;
+        int32_t w = 0;
+        H.wk_off[(size_t)l * nw] = (int32_t)order.size();
+        for (int32_t i = b; i < e; ++i) {
+            const double c = 1.0 + (double)tlen[by_level[i]];
+            // start the next warp's chunk once this one holds its share
+            while (w + 1 < nw && acc + 0.5 * c > total * (double)(w + 1) / (double)nw) {
+                ++w;
+                H.wk_off[(size_t)l * nw + w] = (int32_t)order.size();
+            }
+            order.push_back(by_level[i]);
+            acc += c;
+        }
+        while (w + 1 < nw) {
+            ++w;
+            H.wk_off[(size_t)l * nw + w] = (int32_t)order.size();
+        }
+    }
+    H.wk_off[(size_t)n_levels * nw] = (int32_t)order.size();
+
+    // ---- 8) window slots: linear scan over levels, a slot is free again after
+    // the last level that reads its event
+    std::vector<int32_t> slot((size_t)E, -1);
+    {
+        std::vector<int32_t> free_slots;
+        std::vector<std::vector<int32_t>> release((size_t)n_levels + 1);
+        int32_t n_slots = 0;
+        for (int32_t l = 0; l < n_levels; ++l) {
+            for (int32_t s : release[l]) free_slots.push_back(s);
+            for (int32_t i = lvl_off[l]; i < lvl_off[l + 1]; ++i) {
+                const int32_t e = by_level[i];
+                if (last_use[e] < 0) continue;
+                int32_t s;
+                if (!free_slots.empty()) {
+                    s = free_slots.back();
+                    free_slots.pop_back();
+                } else {
+                    s = n_slots++;
+                }
+                slot[e] = s;
+                release[(size_t)last_use[e] + 1].push_back(s);
+            }
+        }
+        H.window_slots = n_slots;
+    }
+    const size_t win_bytes = (size_t)H.window_slots * kTile * sizeof(double);
+    H.win_smem = win_bytes <= kMaxWindowBytes && std::getenv("MCD_NO_SMEM_WINDOW") == nullptr;
+
+    // ---- 9) records in compiled order
+    H.ev.resize((size_t)E);
+    H.pred.clear();
+    H.pred.reserve((size_t)(d.n_targets > 0 ? d.pred_offsets[d.n_targets] : 0));
+    std::vector<char> referenced((size_t)L, 0), written((size_t)L, 0);
+    H.earliest.assign(d.earliest, d.earliest + E);
+    H.max_delay = d.max_delay;
+    for (int32_t i = 0; i < E; ++i) {
+        const int32_t e = order[i];
+        EvRec r{};
+        r.user = e;
+        r.slot = H.win_smem ? slot[e] : -1;
+        r.pred_begin = (int32_t)H.pred.size();
+        const double earliest = d.earliest[e];
+        const double ub = earliest + d.max_delay;  // _core.cpp:334
+        r.init_bits = bits_of(earliest);
+        r.init_key = std::isnan(earliest) ? std::numeric_limits<int64_t>::max() : order_key_host(r.init_bits);
+        r.ub_bits = bits_of(ub);
+        r.ub_key = std::isnan(ub) ? std::numeric_limits<int64_t>::max() : order_key_host(r.ub_bits);
+        for (int64_t k = 0; k < tlen[e]; ++k) {
+            const int32_t src = d.pred_src[tstart[e] + k];
+            const int32_t l = d.pred_act[tstart[e] + k];
+            PredRec p{};
+            p.src_slot = H.win_smem ? slot[src] : -1;
+            p.src_user = src;
+            if (l >= L) {
+                // Past the last link the reference reads beyond its duration
+                // buffer (_core.cpp:340-341, undefined); in practice it reads 0.0
+                // and its own chain test (test_simulator.py:175-199) relies on
+                // that, so such an edge has duration 0 here.
+                p.link = -1;
+                p.kd = K_FIXED;
+                p.v = 0.0;
+            } else {
+                p.link = l;
+                p.kd = H.link_kd[l];
+                p.v = H.link_v[l];
+                if ((p.kd & KD_KIND_MASK) != K_FIXED && !written[l]) {
+                    p.kd |= KD_WRITE;
+                    written[l] = 1;
+                }
+                referenced[l] = 1;
+            }
+            H.pred.push_back(p);
+        }
+        r.pred_end = (int32_t)H.pred.size();
+        H.ev[i] = r;
+    }
+    H.aux.clear();
+    H.n_orphan = 0;
+    for (int32_t l = 0; l < L; ++l) {
+        if (!referenced[l]) ++H.n_orphan;
+        if (!written[l]) H.aux.push_back(LinkRec{l, H.link_kd[l], H.link_v[l]});
+    }
+}
+
+}  // namespace mcd

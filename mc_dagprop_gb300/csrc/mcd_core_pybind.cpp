@@ -1,0 +1,484 @@
+// mcd_core_pybind.cpp -- the Python module `mc_dagprop_gb300._core`.
+//
+// Same classes, constructor arguments, properties, reprs and error types as the
+// reference's pybind11 module (src/mc_dagprop/monte_carlo/_core.cpp:366-552, stub
+// _core.pyi:8-101), so code written against `mc_dagprop` runs unchanged.  All
+// work goes through the C ABI of include/mc_dagprop_gb300.h; nothing here touches
+// CUDA directly.  The data classes are turned into frozen, slotted dataclasses
+// the way the reference does it (_core.cpp:445-488).
+//
+// Additions beyond the reference surface (array in, array out):
+//   MonteCarloPropagator.from_arrays(...)   flat-array DagContext, no Python objects per event
+//   MonteCarloPropagator.run_many_arrays    (S,E)/(S,L)/(S,E) numpy arrays instead of S SimResults
+//   MonteCarloPropagator.propagate          propagation alone from given durations
+//   MonteCarloPropagator.info               compiled-DAG facts
+#include <pybind11/numpy.h>
+#include <pybind11/pybind11.h>
+#include <pybind11/stl.h>
+
+#include <cstdint>
+#include <limits>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+#include "../../include/mc_dagprop_gb300.h"
+
+namespace py = pybind11;
+
+// Own namespace: the reference's module binds C++ types of the same names, and
+// pybind11 identifies bound types by their C++ type name across modules.
+namespace mcd_py {
+
+using EventIndex = int;
+using ActivityIndex = int;
+using ActivityType = int;
+using Preds = std::vector<std::pair<EventIndex, ActivityIndex>>;
+
+struct PairHash {
+    size_t operator()(const std::pair<int, int> &p) const noexcept {
+        return std::hash<int>{}(p.first) * 1000003u ^ std::hash<int>{}(p.second);
+    }
+};
+
+struct EventTimestamp {
+    double earliest, latest, actual;
+};
+struct Event {
+    std::string event_id;
+    EventTimestamp ts;
+};
+struct Activity {
+    ActivityIndex idx;
+    double duration;
+    ActivityType activity_type;
+};
+using ActivityMap = std::unordered_map<std::pair<EventIndex, EventIndex>, Activity, PairHash>;
+
+struct DagContext {
+    std::vector<Event> events;
+    ActivityMap activity_map;
+    std::vector<std::pair<EventIndex, Preds>> precedence_list;
+    double max_delay;
+    DagContext(std::vector<Event> ev, ActivityMap am, std::vector<std::pair<EventIndex, Preds>> pl, double md)
+        : events(std::move(ev)), activity_map(std::move(am)), precedence_list(std::move(pl)), max_delay(md) {}
+};
+
+static void raise_status(int rc) {
+    if (rc == MCD_OK) return;
+    const std::string msg = mcd_last_error();
+    if (rc == MCD_ERR_INVALID) throw py::value_error(msg);
+    throw std::runtime_error(msg);  // -> RuntimeError, as the reference's C++ exceptions
+}
+
+// ---- GenericDelayGenerator: a value type (copied into each propagator).
+struct Generator {
+    std::shared_ptr<mcd_generator> g;
+    Generator() {
+        mcd_generator *p = nullptr;
+        raise_status(mcd_generator_create(&p));
+        g.reset(p, mcd_generator_destroy);
+    }
+    Generator(const Generator &o) : Generator() { replay_from(o); }
+    Generator &operator=(const Generator &o) {
+        if (this != &o) {
+            Generator fresh(o);
+            g = fresh.g;
+            calls = fresh.calls;
+        }
+        return *this;
+    }
+    // The add_* calls so far, replayed on copies.
+    struct Call {
+        int kind;
+        int type;
+        double a, b, c;
+        std::vector<double> v, w;
+    };
+    std::vector<Call> calls;
+    int64_t seed = 0;
+    void replay_from(const Generator &o) {
+        for (const Call &c : o.calls) apply(c);
+        seed = o.seed;
+        raise_status(mcd_generator_set_seed(g.get(), seed));
+    }
+    void apply(const Call &c) {
+        int rc = MCD_OK;
+        switch (c.kind) {
+            case 0: rc = mcd_generator_add_constant(g.get(), c.type, c.a); break;
+            case 1: rc = mcd_generator_add_exponential(g.get(), c.type, c.a, c.b); break;
+            case 2: rc = mcd_generator_add_gamma(g.get(), c.type, c.a, c.b, c.c); break;
+            case 3:
+                rc = mcd_generator_add_empirical_absolute(g.get(), c.type, c.v.data(), (int64_t)c.v.size(),
+                                                          c.w.data(), (int64_t)c.w.size());
+                break;
+            default:
+                rc = mcd_generator_add_empirical_relative(g.get(), c.type, c.v.data(), (int64_t)c.v.size(),
+                                                          c.w.data(), (int64_t)c.w.size());
+        }
+        raise_status(rc);
+        calls.push_back(c);
+    }
+};
+
+// ---- SimResult: one sample of a result block, exposed as zero-copy numpy views.
+struct SimBlock {
+    int64_t E = 0, L = 0;
+    std::vector<double> realized, durations;
+    std::vector<int32_t> cause;
+};
+struct SimResult {
+    std::shared_ptr<SimBlock> blk;
+    int64_t i = 0;
+    double *realized() const { return blk->realized.data() + i * blk->E; }
+    double *durations() const { return blk->durations.data() + i * blk->L; }
+    int32_t *cause() const { return blk->cause.data() + i * blk->E; }
+};
+
+// ---- MonteCarloPropagator
+struct FlatDag {
+    std::vector<double> earliest, act_duration;
+    std::vector<int32_t> act_idx, act_type, target, pred_src, pred_act;
+    std::vector<int64_t> pred_offsets{0};
+    double max_delay = 0.0;
+    mcd_dag_desc desc() const {
+        mcd_dag_desc d{};
+        d.n_events = (int32_t)earliest.size();
+        d.earliest = earliest.data();
+        d.n_activities = (int32_t)act_idx.size();
+        d.act_idx = act_idx.data();
+        d.act_duration = act_duration.data();
+        d.act_type = act_type.data();
+        d.n_targets = (int32_t)target.size();
+        d.target = target.data();
+        d.pred_offsets = pred_offsets.data();
+        d.pred_src = pred_src.data();
+        d.pred_act = pred_act.data();
+        d.max_delay = max_delay;
+        return d;
+    }
+};
+
+class Propagator {
+   public:
+    Propagator(const FlatDag &f, const Generator &gen) {
+        mcd_dag *p = nullptr;
+        const mcd_dag_desc d = f.desc();
+        int rc;
+        {
+            py::gil_scoped_release release;
+            rc = mcd_dag_create(&d, gen.g.get(), &p);
+        }
+        raise_status(rc);
+        dag_.reset(p, mcd_dag_destroy);
+        E_ = mcd_dag_node_count(p);
+        L_ = mcd_dag_activity_count(p);
+    }
+    static FlatDag flatten(const DagContext &c) {
+        FlatDag f;
+        f.max_delay = c.max_delay;
+        f.earliest.reserve(c.events.size());
+        for (const Event &e : c.events) f.earliest.push_back(e.ts.earliest);
+        for (const auto &kv : c.activity_map) {
+            f.act_idx.push_back(kv.second.idx);
+            f.act_duration.push_back(kv.second.duration);
+            f.act_type.push_back(kv.second.activity_type);
+        }
+        for (const auto &t : c.precedence_list) {
+            f.target.push_back(t.first);
+            for (const auto &pr : t.second) {
+                f.pred_src.push_back(pr.first);
+                f.pred_act.push_back(pr.second);
+            }
+            f.pred_offsets.push_back((int64_t)f.pred_src.size());
+        }
+        return f;
+    }
+    int node_count() const { return (int)E_; }
+    int activity_count() const { return (int)L_; }
+
+    std::shared_ptr<SimBlock> run_block(const std::vector<int64_t> &seeds, bool want_dur = true) {
+        auto blk = std::make_shared<SimBlock>();
+        const int64_t n = (int64_t)seeds.size();
+        blk->E = E_;
+        blk->L = L_;
+        blk->realized.resize((size_t)(n * E_));
+        if (want_dur) blk->durations.resize((size_t)(n * L_));
+        blk->cause.resize((size_t)(n * E_));
+        int rc;
+        {
+            py::gil_scoped_release release;
+            rc = mcd_run_many_host(dag_.get(), seeds.data(), n, blk->realized.data(),
+                                   want_dur ? blk->durations.data() : nullptr, blk->cause.data());
+        }
+        raise_status(rc);
+        return blk;
+    }
+    SimResult run(int seed) {
+        SimResult r;
+        r.blk = run_block({(int64_t)seed});
+        r.i = 0;
+        return r;
+    }
+    std::vector<SimResult> run_many(const std::vector<int> &seeds) {
+        std::vector<int64_t> s(seeds.begin(), seeds.end());
+        auto blk = run_block(s);
+        std::vector<SimResult> out(seeds.size());
+        for (size_t i = 0; i < seeds.size(); ++i) out[i] = SimResult{blk, (int64_t)i};
+        return out;
+    }
+    py::tuple run_many_arrays(py::array_t<int64_t, py::array::c_style | py::array::forcecast> seeds,
+                              bool durations) {
+        const int64_t n = (int64_t)seeds.size();
+        py::array_t<double> real({n, E_});
+        py::array_t<int32_t> cause({n, E_});
+        py::object dur = py::none();
+        double *dp = nullptr;
+        if (durations) {
+            py::array_t<double> d({n, L_});
+            dp = d.mutable_data();
+            dur = d;
+        }
+        const int64_t *sp = seeds.data();
+        double *rp = real.mutable_data();
+        int32_t *cp = cause.mutable_data();
+        int rc;
+        {
+            py::gil_scoped_release release;
+            rc = mcd_run_many_host(dag_.get(), sp, n, rp, dp, cp);
+        }
+        raise_status(rc);
+        return py::make_tuple(real, dur, cause);
+    }
+    py::tuple propagate(py::array_t<double, py::array::c_style | py::array::forcecast> durations) {
+        if (durations.ndim() != 2 || durations.shape(1) != L_)
+            throw py::value_error("durations must have shape (n_samples, activity_count())");
+        const int64_t n = durations.shape(0);
+        py::array_t<double> real({n, E_});
+        py::array_t<int32_t> cause({n, E_});
+        const double *dp = durations.data();
+        double *rp = real.mutable_data();
+        int32_t *cp = cause.mutable_data();
+        int rc;
+        {
+            py::gil_scoped_release release;
+            rc = mcd_propagate_host(dag_.get(), dp, n, rp, cp);
+        }
+        raise_status(rc);
+        return py::make_tuple(real, cause);
+    }
+    py::dict info() const {
+        mcd_dag_info i{};
+        raise_status(mcd_dag_get_info(dag_.get(), &i));
+        py::dict d;
+        d["n_events"] = i.n_events;
+        d["n_links"] = i.n_links;
+        d["n_levels"] = i.n_levels;
+        d["n_warps"] = i.n_warps;
+        d["n_preds"] = i.n_preds;
+        d["window_slots"] = i.window_slots;
+        d["window_in_smem"] = (bool)i.window_in_smem;
+        d["n_orphan_links"] = i.n_orphan_links;
+        d["device"] = i.device;
+        d["device_bytes"] = i.device_bytes;
+        return d;
+    }
+    mcd_dag *handle() const { return dag_.get(); }
+
+   private:
+    std::shared_ptr<mcd_dag> dag_;
+    int64_t E_ = 0, L_ = 0;
+};
+
+template <typename T>
+static std::vector<T> to_vec(py::handle h) {
+    auto a = py::array_t<T, py::array::c_style | py::array::forcecast>::ensure(h);
+    if (!a) throw py::type_error("expected an array-like argument");
+    if (a.ndim() != 1) throw py::value_error("expected a 1-D array");
+    return std::vector<T>(a.data(), a.data() + a.size());
+}
+
+}  // namespace mcd_py
+
+PYBIND11_MODULE(_core, m) {
+    using namespace mcd_py;
+    m.doc() = "GB300 Monte Carlo DAG-propagation engine (drop-in for mc_dagprop.monte_carlo._core)";
+
+    py::class_<EventTimestamp> ts_cls(m, "EventTimestamp");
+    ts_cls
+        .def(py::init<double, double, double>(), py::arg("earliest"), py::arg("latest"), py::arg("actual"),
+             "Create an event timestamp (earliest, latest, actual).")
+        .def_readwrite("earliest", &EventTimestamp::earliest, "Earliest bound")
+        .def_readwrite("latest", &EventTimestamp::latest, "Latest bound")
+        .def_readwrite("actual", &EventTimestamp::actual, "Scheduled time")
+        .def("__repr__", [](const EventTimestamp &t) {
+            return py::str("EventTimestamp(earliest={}, latest={}, actual={})").format(t.earliest, t.latest, t.actual);
+        });
+
+    py::class_<Event> ev_cls(m, "Event");
+    ev_cls
+        .def(py::init<std::string, EventTimestamp>(), py::arg("event_id"), py::arg("timestamp"),
+             "An event node with its ID and timestamp")
+        .def_readwrite("event_id", &Event::event_id, "Node identifier")
+        .def_readwrite("timestamp", &Event::ts, "Event timing info")
+        .def("__repr__", [](const Event &e) {
+            return py::str("Event(event_id={}, timestamp={})").format(py::repr(py::cast(e.event_id)),
+                                                                       py::repr(py::cast(e.ts)));
+        });
+
+    py::class_<Activity> act_cls(m, "Activity");
+    act_cls
+        .def(py::init<ActivityIndex, double, ActivityType>(), py::arg("idx"), py::arg("minimal_duration"),
+             py::arg("activity_type"), "An activity (edge) with index, base duration and type")
+        .def_readwrite("idx", &Activity::idx, "Index of the activity")
+        .def_readwrite("minimal_duration", &Activity::duration, "Base duration")
+        .def_readwrite("activity_type", &Activity::activity_type, "Type ID for delay dist.")
+        .def("__repr__", [](const Activity &a) {
+            return py::str("Activity(idx={}, minimal_duration={}, activity_type={})")
+                .format(a.idx, a.duration, a.activity_type);
+        });
+
+    py::class_<DagContext> ctx_cls(m, "DagContext");
+    ctx_cls
+        .def(py::init<std::vector<Event>, ActivityMap, std::vector<std::pair<EventIndex, Preds>>, double>(),
+             py::arg("events"), py::arg("activities"), py::arg("precedence_list"), py::arg("max_delay"),
+             "Wraps a DAG: events, activity_map, precedence_list, max_delay")
+        .def_readwrite("events", &DagContext::events)
+        .def_readwrite("activities", &DagContext::activity_map)
+        .def_readwrite("precedence_list", &DagContext::precedence_list)
+        .def_readwrite("max_delay", &DagContext::max_delay)
+        .def("__repr__", [](const DagContext &c) {
+            return py::str("DagContext(events={}, activities={}, precedence_list={}, max_delay={})")
+                .format(py::repr(py::cast(c.events)), py::repr(py::cast(c.activity_map)),
+                        py::repr(py::cast(c.precedence_list)), c.max_delay);
+        });
+
+    // Frozen, slotted dataclasses over the bound classes, as the reference does.
+    {
+        py::dict opts;
+        opts["frozen"] = true;
+        opts["slots"] = true;
+        opts["init"] = false;
+        py::object dataclass = py::module_::import("dataclasses").attr("dataclass")(**opts);
+        py::module_ types = py::module_::import("mc_dagprop_gb300.types");
+        py::object Second = types.attr("Second");
+        py::dict a1;
+        a1["earliest"] = Second;
+        a1["latest"] = Second;
+        a1["actual"] = Second;
+        ts_cls.attr("__annotations__") = a1;
+        dataclass(ts_cls);
+        py::dict a2;
+        a2["event_id"] = types.attr("EventId");
+        a2["timestamp"] = ts_cls;
+        ev_cls.attr("__annotations__") = a2;
+        dataclass(ev_cls);
+        py::dict a3;
+        a3["idx"] = types.attr("ActivityIndex");
+        a3["minimal_duration"] = Second;
+        a3["activity_type"] = types.attr("ActivityType");
+        act_cls.attr("__annotations__") = a3;
+        dataclass(act_cls);
+        py::module_ typing = py::module_::import("typing");
+        py::dict a4;
+        a4["events"] = typing.attr("Sequence");
+        a4["activities"] = typing.attr("Mapping");
+        a4["precedence_list"] = typing.attr("Sequence");
+        a4["max_delay"] = Second;
+        ctx_cls.attr("__annotations__") = a4;
+        dataclass(ctx_cls);
+    }
+
+    py::class_<SimResult>(m, "SimResult", py::buffer_protocol())
+        .def_buffer([](SimResult &r) -> py::buffer_info {
+            return py::buffer_info(r.realized(), sizeof(double), py::format_descriptor<double>::format(), 1,
+                                   {r.blk->E}, {(py::ssize_t)sizeof(double)});
+        })
+        .def_property_readonly(
+            "realized", [](const SimResult &r) { return py::array(r.blk->E, r.realized(), py::cast(r)); },
+            "Final event times as a NumPy array")
+        .def_property_readonly(
+            "durations", [](const SimResult &r) { return py::array(r.blk->L, r.durations(), py::cast(r)); },
+            "Per-link durations (incl. extra) as a NumPy array")
+        .def_property_readonly(
+            "cause_event", [](const SimResult &r) { return py::array(r.blk->E, r.cause(), py::cast(r)); },
+            "Index of predecessor causing each event as a NumPy array");
+
+    py::class_<Generator>(m, "GenericDelayGenerator")
+        .def(py::init<>(), "Create a new delay-generator")
+        .def(
+            "set_seed",
+            [](Generator &g, int s) {
+                g.seed = s;
+                raise_status(mcd_generator_set_seed(g.g.get(), s));
+            },
+            py::arg("seed"), "Set RNG seed for reproducibility")
+        .def(
+            "add_constant", [](Generator &g, ActivityType t, double f) { g.apply({0, t, f, 0.0, 0.0, {}, {}}); },
+            py::arg("activity_type"), py::arg("factor"), "Constant: delay = factor * duration")
+        .def(
+            "add_exponential",
+            [](Generator &g, ActivityType t, double lam, double mx) { g.apply({1, t, lam, mx, 0.0, {}, {}}); },
+            py::arg("activity_type"), py::arg("lambda_"), py::arg("max_scale"),
+            "Exponential(lambda) truncated at max_scale")
+        .def(
+            "add_gamma",
+            [](Generator &g, ActivityType t, double k, double s, double mx) { g.apply({2, t, k, s, mx, {}, {}}); },
+            py::arg("activity_type"), py::arg("shape"), py::arg("scale"),
+            py::arg("max_scale") = std::numeric_limits<double>::infinity(), "Gamma(shape,scale) truncated at max_scale")
+        .def(
+            "add_empirical_absolute",
+            [](Generator &g, ActivityType t, std::vector<double> values, std::vector<double> weights) {
+                g.apply({3, t, 0.0, 0.0, 0.0, std::move(values), std::move(weights)});
+            },
+            py::arg("activity_type"), py::arg("values"), py::arg("weights"),
+            "Empirical absolute: draw one of your provided values, weighted by weights.")
+        .def(
+            "add_empirical_relative",
+            [](Generator &g, ActivityType t, std::vector<double> factors, std::vector<double> weights) {
+                g.apply({4, t, 0.0, 0.0, 0.0, std::move(factors), std::move(weights)});
+            },
+            py::arg("activity_type"), py::arg("factors"), py::arg("weights"),
+            "Empirical relative: draw a factor in [0,inf), then multiply by the activity duration.");
+
+    py::class_<Propagator>(m, "MonteCarloPropagator")
+        .def(py::init([](const DagContext &c, const Generator &g) { return new Propagator(Propagator::flatten(c), g); }),
+             py::arg("context"), py::arg("generator"), "Construct simulator with context and delay-generator")
+        .def_static(
+            "from_arrays",
+            [](py::handle earliest, py::handle act_idx, py::handle act_duration, py::handle act_type,
+               py::handle target, py::handle pred_offsets, py::handle pred_src, py::handle pred_act,
+               double max_delay, const Generator &g) {
+                FlatDag f;
+                f.earliest = to_vec<double>(earliest);
+                f.act_idx = to_vec<int32_t>(act_idx);
+                f.act_duration = to_vec<double>(act_duration);
+                f.act_type = to_vec<int32_t>(act_type);
+                f.target = to_vec<int32_t>(target);
+                f.pred_offsets = to_vec<int64_t>(pred_offsets);
+                f.pred_src = to_vec<int32_t>(pred_src);
+                f.pred_act = to_vec<int32_t>(pred_act);
+                f.max_delay = max_delay;
+                if (f.act_duration.size() != f.act_idx.size() || f.act_type.size() != f.act_idx.size())
+                    throw py::value_error("activity arrays must have equal length");
+                if (f.pred_offsets.size() != f.target.size() + 1 || f.pred_offsets.front() != 0 ||
+                    f.pred_offsets.back() != (int64_t)f.pred_src.size() || f.pred_src.size() != f.pred_act.size())
+                    throw py::value_error("inconsistent precedence arrays");
+                return new Propagator(f, g);
+            },
+            py::arg("earliest"), py::arg("act_idx"), py::arg("act_duration"), py::arg("act_type"), py::arg("target"),
+            py::arg("pred_offsets"), py::arg("pred_src"), py::arg("pred_act"), py::arg("max_delay"),
+            py::arg("generator"), "Construct from a DagContext in flat-array form")
+        .def("node_count", &Propagator::node_count, "Number of events")
+        .def("activity_count", &Propagator::activity_count, "Number of links")
+        .def("run", &Propagator::run, py::arg("seed"), "Run single sim")
+        .def("run_many", &Propagator::run_many, py::arg("seeds"), "Run batch sims")
+        .def("run_many_arrays", &Propagator::run_many_arrays, py::arg("seeds"), py::arg("durations") = true,
+             "Batch run returning (realized (S,E), durations (S,L) or None, cause_event (S,E)) arrays")
+        .def("propagate", &Propagator::propagate, py::arg("durations"),
+             "Propagation alone from given durations (S,L): returns (realized, cause_event)")
+        .def("info", &Propagator::info, "Compiled-DAG facts")
+        .def("_handle", [](const Propagator &p) { return (uintptr_t)p.handle(); });
+}

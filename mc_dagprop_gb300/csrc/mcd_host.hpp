@@ -1,0 +1,66 @@
+// mcd_host.hpp -- host-side types of the engine (generator, compiled DAG, errors).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/mc_dagprop_gb300.h"
+#include "mcd_internal.hpp"
+
+// Distribution kinds as the generator records them (one per add_* method).
+enum : int32_t {
+    MCD_KIND_CONSTANT = 0,
+    MCD_KIND_EXPONENTIAL = 1,
+    MCD_KIND_GAMMA = 2,
+    MCD_KIND_EMP_ABS = 3,
+    MCD_KIND_EMP_REL = 4,
+};
+
+struct DistSpec {
+    int32_t type;
+    int32_t kind;
+    double p0, p1, p2;
+    std::vector<double> values, weights;
+};
+
+// GenericDelayGenerator (_core.cpp:146-159): the add_* calls in order; the
+// compiler keeps the last one per activity type.
+struct mcd_generator {
+    int64_t seed = 0;
+    std::vector<DistSpec> dists;
+};
+
+namespace mcd {
+
+struct McdError : std::runtime_error {
+    int code;
+    McdError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+// Shared memory the propagation window may take per CTA.
+constexpr size_t kMaxWindowBytes = 200 * 1024;
+
+// Output of compile_dag: everything the kernels need, host copies.
+struct HostDag {
+    int32_t E = 0, L = 0, n_levels = 0, n_warps = 1, window_slots = 0;
+    bool win_smem = true;
+    std::vector<EvRec> ev;
+    std::vector<PredRec> pred;
+    std::vector<LinkRec> aux;  // links stored by the aux pass
+    int32_t n_orphan = 0;      // sampled links no precedence entry references
+    std::vector<DistParam> dist;
+    std::vector<AliasEntry> alias;
+    std::vector<int32_t> wk_off;
+    std::vector<int32_t> link_kd;
+    std::vector<double> link_v;
+    std::vector<double> earliest;  // caller order
+    double max_delay = 0.0;
+};
+
+void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &out);
+int64_t order_key_host(int64_t bits);
+
+}  // namespace mcd

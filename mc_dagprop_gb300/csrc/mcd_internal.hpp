@@ -1,0 +1,110 @@
+// mcd_internal.hpp -- records shared by the host DAG compiler and the CUDA kernels.
+//
+// The compiled DAG is a level-ordered CSR: events are sorted by level (longest
+// path from a source), each level is split into one contiguous chunk per warp,
+// and every event's predecessors keep their precedence-list order (the tie rule
+// of the reference's propagation loop, _core.cpp:338-347, depends on it).
+#pragma once
+
+#include <cstdint>
+
+namespace mcd {
+
+// Delay kinds as the kernels see them.  FIXED covers links whose duration does
+// not vary between samples: unmapped types, gaps in the link index space and the
+// constant distribution, whose `base + base*factor` the host evaluates once with
+// the reference's two roundings (_core.cpp:75, 328).
+enum Kind : int32_t { K_FIXED = 0, K_EXP = 1, K_GAMMA = 2, K_EMP_ABS = 3, K_EMP_REL = 4 };
+
+// Packed kind word of a link reference: kind | KD_WRITE | dist << 8.  KD_WRITE
+// marks the one reference of a sampled link that stores its duration row; fixed
+// links and unreferenced links are stored by the kernel's aux-link pass.
+constexpr int32_t KD_KIND_MASK = 0x7F;
+constexpr int32_t KD_WRITE = 0x80;
+
+// One event, in compiled (level) order.  48 bytes.
+struct alignas(16) EvRec {
+    int32_t user;        // event index as the caller numbers it (output row)
+    int32_t slot;        // window slot holding this event's realized value, -1 if no consumer
+    int32_t pred_begin;  // range in the PredRec array
+    int32_t pred_end;
+    int64_t init_bits;   // earliest (bits): the running max starts here (_core.cpp:336)
+    int64_t init_key;    // order key of earliest; INT64_MAX when earliest is NaN
+    int64_t ub_bits;     // earliest + max_delay (bits), evaluated on the host (_core.cpp:334)
+    int64_t ub_key;      // order key of ub; INT64_MAX when ub is NaN (std::min then keeps t)
+};
+
+// One predecessor edge.  32 bytes.
+struct alignas(16) PredRec {
+    int32_t src_slot;  // window slot of the predecessor's realized value (-1: read its global row)
+    int32_t src_user;  // predecessor event index (cause_event value, global row)
+    int32_t link;      // link index: durations row and Philox counter; -1 for an index
+                       // past the last link, which has duration 0 (see the compiler)
+    int32_t kd;        // kind | KD_WRITE | dist << 8
+    double v;          // FIXED: the duration; otherwise the base (minimal_duration)
+    int64_t pad;
+};
+
+// A link whose duration row the aux pass stores: fixed links (one value for all
+// samples) and sampled links no precedence entry references (their durations are
+// still part of SimResult.durations).  16 bytes.
+struct alignas(16) LinkRec {
+    int32_t link;
+    int32_t kd;
+    double v;
+};
+
+// Per-distribution constants, single precision where the sampler works in FP32.
+struct alignas(16) DistParam {
+    int32_t kind;
+    int32_t tab_off;   // empirical: first alias entry
+    int32_t tab_n;     // empirical: number of bins
+    int32_t boost;     // gamma: shape < 1 (Marsaglia-Tsang on shape+1, times U^(1/shape))
+    float f0, f1, f2, f3, f4, f5;
+    // exponential: f0 = lambda_ (mean), f1 = c = 1 - exp(-max_scale/lambda_), f2 = 1 - c,
+    //              f3 = largest float <= max_scale
+    // gamma:       f0 = d = shape' - 1/3, f1 = 1/sqrt(9 d), f2 = 1/shape, f3 = scale,
+    //              f4 = largest float <= max_scale
+    int32_t pad[2];
+};
+
+// Walker/Vose alias entry: bin j is kept when a 32-bit uniform is below
+// `thresh`, otherwise its alias is taken.  The two candidate values are stored
+// inline so a draw costs one gather.  32 bytes.
+struct alignas(16) AliasEntry {
+    double v_self;
+    double v_alias;
+    uint32_t thresh;
+    uint32_t pad[3];
+};
+
+// Arguments of the propagation kernels.
+struct KArgs {
+    const EvRec *ev;
+    const PredRec *pred;
+    const LinkRec *aux;
+    const DistParam *dist;
+    const AliasEntry *alias;
+    const int32_t *wk_off;  // [n_levels * n_warps + 1] event chunk per (level, warp)
+    int32_t n_levels;
+    int32_t n_warps;
+    int32_t n_aux;
+    int32_t window_slots;
+    const int64_t *seeds;  // [n] per-sample seeds
+    int64_t n;
+    int64_t ld;            // leading dimension of the sample-minor outputs
+    double *realized;      // [E][ld] or null (then `scratch` holds the rows the window spills)
+    double *durations;     // [L][ld] or null
+    int32_t *cause;        // [E][ld] or null
+    const double *dur_in;  // given durations [L][ld_in] (propagation-only mode)
+    int64_t ld_in;
+    double *scratch;       // [E][ld] realized rows when the window is not on chip and realized is null
+    int32_t *err;          // latched device error flags
+};
+
+// Device error flags.
+enum : int32_t { ERR_GAMMA_REJECTION = 1 };
+
+constexpr int kTile = 32;  // samples per tile: one per lane
+
+}  // namespace mcd

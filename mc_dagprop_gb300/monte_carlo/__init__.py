@@ -1,0 +1,17 @@
+"""Monte Carlo propagation on the GPU (the reference's ``mc_dagprop.monte_carlo``)."""
+from __future__ import annotations
+
+from .._core import Activity, DagContext, Event, EventTimestamp, GenericDelayGenerator, MonteCarloPropagator, SimResult
+
+Simulator = MonteCarloPropagator
+
+__all__ = [
+    "GenericDelayGenerator",
+    "DagContext",
+    "SimResult",
+    "Event",
+    "Activity",
+    "MonteCarloPropagator",
+    "Simulator",
+    "EventTimestamp",
+]

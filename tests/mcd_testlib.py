@@ -1,0 +1,177 @@
+"""Test helpers: ctypes bindings of the C ABI, fixture loading, DAG builders."""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import re
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "mc_dagprop_gb300.h")
+LIB = os.path.join(ROOT, "mc_dagprop_gb300", "_lib", "libmcdagprop_gb300.so")
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+MCD_OK, MCD_ERR_INVALID, MCD_ERR_RUNTIME, MCD_ERR_CUDA, MCD_ERR_NOMEM, MCD_ERR_DEVICE = 0, 1, 2, 3, 4, 5
+
+
+class DagDesc(C.Structure):
+    _fields_ = [("n_events", C.c_int32), ("earliest", C.c_void_p), ("n_activities", C.c_int32),
+                ("act_idx", C.c_void_p), ("act_duration", C.c_void_p), ("act_type", C.c_void_p),
+                ("n_targets", C.c_int32), ("target", C.c_void_p), ("pred_offsets", C.c_void_p),
+                ("pred_src", C.c_void_p), ("pred_act", C.c_void_p), ("max_delay", C.c_double)]
+
+
+class DagInfo(C.Structure):
+    _fields_ = [("n_events", C.c_int32), ("n_links", C.c_int32), ("n_levels", C.c_int32), ("n_warps", C.c_int32),
+                ("n_preds", C.c_int64), ("window_slots", C.c_int32), ("window_in_smem", C.c_int32),
+                ("n_orphan_links", C.c_int32), ("device", C.c_int32), ("device_bytes", C.c_int64)]
+
+
+def header_functions() -> list[str]:
+    """Names of every function the public header declares."""
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(mcd_[a-z0-9_]+)\s*\(", src)))
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(LIB)
+        P, I64, I32, D = C.c_void_p, C.c_int64, C.c_int32, C.c_double
+        L.mcd_last_error.restype = C.c_char_p
+        L.mcd_generator_create.argtypes = [C.POINTER(P)]
+        L.mcd_generator_destroy.argtypes = [P]
+        L.mcd_generator_set_seed.argtypes = [P, I64]
+        L.mcd_generator_add_constant.argtypes = [P, I32, D]
+        L.mcd_generator_add_exponential.argtypes = [P, I32, D, D]
+        L.mcd_generator_add_gamma.argtypes = [P, I32, D, D, D]
+        L.mcd_generator_add_empirical_absolute.argtypes = [P, I32, P, I64, P, I64]
+        L.mcd_generator_add_empirical_relative.argtypes = [P, I32, P, I64, P, I64]
+        L.mcd_dag_create.argtypes = [C.POINTER(DagDesc), P, C.POINTER(P)]
+        L.mcd_dag_destroy.argtypes = [P]
+        L.mcd_dag_node_count.argtypes = [P]
+        L.mcd_dag_activity_count.argtypes = [P]
+        L.mcd_dag_get_info.argtypes = [P, C.POINTER(DagInfo)]
+        L.mcd_dag_stream.argtypes = [P]
+        L.mcd_dag_stream.restype = P
+        L.mcd_run_many_host.argtypes = [P, P, I64, P, P, P]
+        L.mcd_propagate_host.argtypes = [P, P, I64, P, P]
+        L.mcd_run_device.argtypes = [P, P, I64, P, P, P, I64, P]
+        L.mcd_propagate_device.argtypes = [P, P, I64, I64, P, P, I64, P]
+        L.mcd_dag_check.argtypes = [P]
+        L.mcd_host_alloc.argtypes = [C.c_size_t, C.POINTER(P)]
+        L.mcd_host_free.argtypes = [P]
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().mcd_last_error().decode()
+
+
+def ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def make_generator(gen: list):
+    """C-ABI generator from a list of (kind, type, *params) tuples; returns (handle, rc, keepalive)."""
+    L = lib()
+    h = C.c_void_p()
+    assert L.mcd_generator_create(C.byref(h)) == MCD_OK
+    keep = []
+    for spec in gen:
+        kind, t = spec[0], int(spec[1])
+        if kind == "constant":
+            rc = L.mcd_generator_add_constant(h, t, float(spec[2]))
+        elif kind == "exponential":
+            rc = L.mcd_generator_add_exponential(h, t, float(spec[2]), float(spec[3]))
+        elif kind == "gamma":
+            rc = L.mcd_generator_add_gamma(h, t, float(spec[2]), float(spec[3]),
+                                           float(spec[4]) if len(spec) > 4 else float("inf"))
+        else:
+            v = np.ascontiguousarray(spec[2], np.float64)
+            w = np.ascontiguousarray(spec[3], np.float64)
+            keep += [v, w]
+            fn = L.mcd_generator_add_empirical_absolute if kind == "empirical_absolute" else \
+                L.mcd_generator_add_empirical_relative
+            rc = fn(h, t, ptr(v), len(v), ptr(w), len(w))
+        if rc != MCD_OK:
+            return h, rc, keep
+    return h, MCD_OK, keep
+
+
+def make_desc(flat: dict):
+    arrs = {
+        "earliest": np.ascontiguousarray(flat["earliest"], np.float64),
+        "act_idx": np.ascontiguousarray(flat["act_idx"], np.int32),
+        "act_duration": np.ascontiguousarray(flat["act_duration"], np.float64),
+        "act_type": np.ascontiguousarray(flat["act_type"], np.int32),
+        "target": np.ascontiguousarray(flat["target"], np.int32),
+        "pred_offsets": np.ascontiguousarray(flat["pred_offsets"], np.int64),
+        "pred_src": np.ascontiguousarray(flat["pred_src"], np.int32),
+        "pred_act": np.ascontiguousarray(flat["pred_act"], np.int32),
+    }
+    d = DagDesc(len(arrs["earliest"]), ptr(arrs["earliest"]), len(arrs["act_idx"]), ptr(arrs["act_idx"]),
+                ptr(arrs["act_duration"]), ptr(arrs["act_type"]), len(arrs["target"]), ptr(arrs["target"]),
+                ptr(arrs["pred_offsets"]), ptr(arrs["pred_src"]), ptr(arrs["pred_act"]), float(flat["max_delay"]))
+    return d, arrs
+
+
+def load_golden(name: str):
+    z = np.load(os.path.join(GOLDEN, name))
+    flat = {k: z[k] for k in ("earliest", "act_idx", "act_duration", "act_type", "act_src", "act_dst", "target",
+                              "pred_offsets", "pred_src", "pred_act")}
+    flat["max_delay"] = float(z["max_delay"])
+    gen = [tuple([g[0], g[1]] + [np.asarray(p) if isinstance(p, list) else p for p in g[2:]])
+           for g in json.loads(str(z["gen"]))]
+    return flat, gen, z
+
+
+def flat_from_lists(earliest, links, precedence, max_delay):
+    """Flat DAG from python lists: links = {(src,dst): (idx, duration, type)}."""
+    act_src = np.array([k[0] for k in links], np.int32)
+    act_dst = np.array([k[1] for k in links], np.int32)
+    vals = list(links.values())
+    off = [0]
+    src, act = [], []
+    for _, preds in precedence:
+        for s, a in preds:
+            src.append(s)
+            act.append(a)
+        off.append(len(src))
+    return {
+        "earliest": np.asarray(earliest, np.float64),
+        "act_idx": np.array([v[0] for v in vals], np.int32),
+        "act_duration": np.array([v[1] for v in vals], np.float64),
+        "act_type": np.array([v[2] for v in vals], np.int32),
+        "act_src": act_src, "act_dst": act_dst,
+        "target": np.array([t for t, _ in precedence], np.int32),
+        "pred_offsets": np.array(off, np.int64),
+        "pred_src": np.array(src, np.int32),
+        "pred_act": np.array(act, np.int32),
+        "max_delay": float(max_delay),
+    }
+
+
+def propagator_from_flat(mod, flat, gen):
+    from mc_dagprop_gb300 import workloads as W
+
+    g = W.to_generator(mod, gen)
+    return mod.MonteCarloPropagator.from_arrays(flat["earliest"], flat["act_idx"], flat["act_duration"],
+                                                flat["act_type"], flat["target"], flat["pred_offsets"],
+                                                flat["pred_src"], flat["pred_act"], flat["max_delay"], g)
+
+
+# The 6-event DAG of the reference's test_simulator.py:11-35.
+def six_event_flat():
+    earliest = [0.0, 5.0, 10.0, 22.0, 20.0, 100.0]
+    links = {(0, 1): (0, 3.0, 1), (1, 2): (1, 5.0, 1), (1, 3): (2, 5.0, 1), (2, 4): (3, 15.0, 2),
+             (3, 4): (4, 10.0, 3)}
+    prec = [(1, [(0, 0)]), (2, [(1, 1)]), (3, [(1, 2)]), (4, [(2, 3), (3, 4)])]
+    return flat_from_lists(earliest, links, prec, 1e6)

@@ -1,0 +1,101 @@
+"""numpy model of the GPU delay sampler (test infrastructure).
+
+Restates, on the CPU, what ``mc_dagprop_gb300/csrc/mcd_kernels.cu`` draws for one
+(sample seed, link): Philox4x32-10 (Salmon et al., SC'11) keyed by the 64-bit
+seed with counter (link, attempt, 0, salt), and the per-kind transforms.  The
+integer parts (Philox words, alias-table bin choice) must match the GPU bit for
+bit; the FP32 transforms match to float rounding, so tests compare those with a
+tolerance.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+M0, M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
+W0, W1 = np.uint64(0x9E3779B9), np.uint64(0xBB67AE85)
+MASK = np.uint64(0xFFFFFFFF)
+SALT = 0x6D636470
+
+
+def philox4x32_10(c0, c1, c2, c3, k0, k1):
+    """Vectorised Philox4x32-10 over uint32 arrays (broadcast); returns 4 uint32 arrays."""
+    c0, c1, c2, c3, k0, k1 = (np.asarray(x, dtype=np.uint64) & MASK for x in (c0, c1, c2, c3, k0, k1))
+    c0, c1, c2, c3, k0, k1 = np.broadcast_arrays(c0, c1, c2, c3, k0, k1)
+    c0, c1, c2, c3, k0, k1 = (x.copy() for x in (c0, c1, c2, c3, k0, k1))
+    for _ in range(10):
+        p0 = M0 * c0
+        p1 = M1 * c2
+        hi0, lo0 = p0 >> np.uint64(32), p0 & MASK
+        hi1, lo1 = p1 >> np.uint64(32), p1 & MASK
+        n0 = hi1 ^ c1 ^ k0
+        n2 = hi0 ^ c3 ^ k1
+        c0, c1, c2, c3 = n0, lo1, n2, lo0
+        k0 = (k0 + W0) & MASK
+        k1 = (k1 + W1) & MASK
+    return tuple(x.astype(np.uint32) for x in (c0, c1, c2, c3))
+
+
+def words(seeds, link, attempt=0, word2=0):
+    s = np.asarray(seeds, dtype=np.int64).view(np.uint64)
+    return philox4x32_10(link, attempt, word2, SALT, s & MASK, s >> np.uint64(32))
+
+
+def u01_open0(r):
+    """(r + 1/2) / 2^32 as the kernel rounds it to float32."""
+    f = np.asarray(r, dtype=np.uint32).astype(np.float32)
+    return (f.astype(np.float64) * 2.0 ** -32 + 2.0 ** -33).astype(np.float32)
+
+
+def exponential_durations(seeds, link, base, lam, max_scale):
+    """Truncated exponential by inverse CDF, the kernel's formula in float32."""
+    r0, _, _, _ = words(seeds, link)
+    w = u01_open0(r0).astype(np.float64)
+    ratio = max_scale / lam
+    c = 1.0 if np.isinf(ratio) else -np.expm1(-ratio)
+    omc = 0.0 if np.isinf(ratio) else np.exp(-ratio)
+    V = np.float32(c) * w + np.float32(omc)
+    X = np.minimum(-lam * np.log(V), max_scale)
+    X = np.maximum(X, 0.0)
+    return base + X * base
+
+
+def alias_table(values, weights):
+    """Walker/Vose table as the host compiler builds it: (thresh u32, self value, alias value)."""
+    w = np.asarray(weights, np.float64)
+    v = np.asarray(values, np.float64)
+    n = len(w)
+    q = list(w / w.sum() * n)
+    small = [i for i in range(n) if q[i] < 1.0]
+    large = [i for i in range(n) if q[i] >= 1.0]
+    prob = [1.0] * n
+    alias = list(range(n))
+    while small and large:
+        s = small.pop()
+        l = large.pop()
+        prob[s] = q[s]
+        alias[s] = l
+        q[l] = (q[l] + q[s]) - 1.0
+        (small if q[l] < 1.0 else large).append(l)
+    th = np.empty(n, np.uint64)
+    va = np.empty(n, np.float64)
+    for i in range(n):
+        p = prob[i]
+        if not p < 1.0:
+            th[i] = 0xFFFFFFFF
+        elif not p > 0.0:
+            th[i] = 0
+        else:
+            t = np.floor(p * 4294967296.0)
+            th[i] = 0xFFFFFFFF if t >= 4294967295.0 else int(t)
+        va[i] = v[i] if th[i] == 0xFFFFFFFF else v[alias[i]]
+    return th, v, va
+
+
+def empirical_values(seeds, link, values, weights):
+    """The table value the kernel picks for each seed (exact)."""
+    r0, r1, _, _ = words(seeds, link)
+    th, vs, va = alias_table(values, weights)
+    n = len(vs)
+    j = ((r0.astype(np.uint64) * np.uint64(n)) >> np.uint64(32)).astype(np.int64)
+    keep = r1.astype(np.uint64) < th[j]
+    return np.where(keep, vs[j], va[j])

@@ -1,0 +1,194 @@
+"""GPU delay sampler: draw-for-draw against the numpy model, in distribution
+against the reference's laws, and propagated statistics against the oracle
+(which reproduces the reference's run_many bit for bit).
+
+Tolerances stated here:
+  * model parity: empirical draws exact; exponential within 2e-6 relative (FP32 log);
+  * distribution tests: Kolmogorov-Smirnov / chi-square at alpha = 0.01 on fixed seeds;
+  * propagated statistics vs the oracle on the same DAG: per-event two-sample KS at
+    alpha = 0.01 (at most 3% of events may reject, 1% expected by chance) and
+    per-event means within 3 standard errors (at most 1% outside, 0.27% expected).
+"""
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+import pytest
+from scipy import stats
+
+import mc_dagprop_gb300 as m
+import oracle
+import philox_model as PM
+from mc_dagprop_gb300 import workloads as W
+from mcd_testlib import flat_from_lists, propagator_from_flat
+
+pytestmark = pytest.mark.gpu
+
+
+def _one_link(base=100.0):
+    """Two events, one link of the given base duration, no clamping."""
+    return flat_from_lists([0.0, 0.0], {(0, 1): (0, base, 1)}, [(1, [(0, 0)])], 1e12)
+
+
+def _draw(gen, seeds, base=100.0, link=0):
+    prop = propagator_from_flat(m, _one_link(base), gen)
+    _, dur, _ = prop.run_many_arrays(np.asarray(seeds, np.int64))
+    return dur[:, link]
+
+
+SEEDS = np.concatenate([np.arange(-2000, 2000), np.random.default_rng(5).integers(-2**62, 2**62, 4000)])
+
+
+def test_constant_exact(cuda):
+    d = _draw([("constant", 1, 1.5)], SEEDS[:100], base=37.3)
+    assert (d == 37.3 + 37.3 * 1.5).all()
+
+
+@pytest.mark.parametrize("kind", ["empirical_absolute", "empirical_relative"])
+def test_empirical_matches_model_exactly(cuda, kind):
+    values = np.array([0.0, 3.5, 7.25, 100.0, 0.125])
+    weights = np.array([0.1, 0.0, 2.0, 0.7, 1.2])
+    d = _draw([(kind, 1, values, weights)], SEEDS, base=40.0)
+    v = PM.empirical_values(SEEDS, 0, values, weights)
+    expect = 40.0 + v if kind == "empirical_absolute" else 40.0 + v * 40.0
+    assert np.array_equal(d, expect)
+
+
+def test_exponential_matches_model(cuda):
+    for lam, ms in ((0.1, math.inf), (2.0, 0.5), (1.0, 3.0)):
+        d = _draw([("exponential", 1, lam, ms)], SEEDS, base=10.0)
+        ref = PM.exponential_durations(SEEDS, 0, 10.0, lam, ms)
+        np.testing.assert_allclose(d, ref, rtol=2e-6)
+        assert (d >= 10.0).all() and (d <= 10.0 * (1 + ms)).all()
+
+
+def test_exponential_distribution(cuda):
+    n = 200_000
+    seeds = np.arange(n) + 123_456
+    for lam, ms in ((0.1, math.inf), (2.0, 0.5)):
+        x = (_draw([("exponential", 1, lam, ms)], seeds, base=1.0) - 1.0)
+        if math.isinf(ms):
+            p = stats.kstest(x, stats.expon(scale=lam).cdf).pvalue
+        else:
+            p = stats.kstest(x, stats.truncexpon(b=ms / lam, scale=lam).cdf).pvalue
+        assert p > 0.01, (lam, ms, p)
+
+
+@pytest.mark.parametrize("shape,scale,ms", [(2.0, 0.05, math.inf), (0.4, 1.5, math.inf), (2.0, 1.0, 0.5),
+                                            (9.0, 0.3, 3.0)])
+def test_gamma_distribution(cuda, shape, scale, ms):
+    n = 200_000
+    x = _draw([("gamma", 1, shape, scale, ms)], np.arange(n) + 77, base=1.0) - 1.0
+    assert (x >= 0.0).all() and (x <= ms).all()
+    g = stats.gamma(shape, scale=scale)
+    if math.isinf(ms):
+        cdf = g.cdf
+    else:
+        cut = g.cdf(ms)
+        cdf = lambda t: np.minimum(g.cdf(t) / cut, 1.0)  # noqa: E731
+    assert stats.kstest(x, cdf).pvalue > 0.01
+
+
+def test_empirical_frequencies(cuda):
+    n = 200_000
+    values = np.linspace(0.0, 300.0, 16)
+    w = np.random.default_rng(3).dirichlet(np.ones(16))
+    x = _draw([("empirical_absolute", 1, values, w)], np.arange(n), base=0.0)
+    idx = np.searchsorted(values, x)
+    counts = np.bincount(idx, minlength=16)
+    assert stats.chisquare(counts, w * n).pvalue > 0.01
+
+
+def test_gamma_rejection_cap_reports_error(cuda):
+    """A truncation that accepts (almost) nothing ends in a RuntimeError, not a hang."""
+    prop = propagator_from_flat(m, _one_link(1.0), [("gamma", 1, 60.0, 1.0, 1.0)])
+    with pytest.raises(RuntimeError, match="gamma"):
+        prop.run_many_arrays(np.arange(64))
+    # the handle stays usable afterwards
+    prop2 = propagator_from_flat(m, _one_link(1.0), [("gamma", 1, 2.0, 1.0)])
+    assert np.isfinite(prop2.run_many_arrays(np.arange(64))[1]).all()
+
+
+def _per_event_agreement(real_a, real_b, earliest):
+    ks_fail = 0
+    mean_fail = 0
+    E = real_a.shape[1]
+    for e in range(E):
+        a, b = real_a[:, e], real_b[:, e]
+        if np.all(a == a[0]) and np.all(b == b[0]):
+            assert a[0] == b[0]
+            continue
+        if stats.ks_2samp(a, b).pvalue < 0.01:
+            ks_fail += 1
+        se = math.sqrt(a.var() / len(a) + b.var() / len(b))
+        if abs(a.mean() - b.mean()) > 3.0 * se + 1e-9:
+            mean_fail += 1
+    return ks_fail / E, mean_fail / E
+
+
+@pytest.mark.parametrize("cfg", ["config0", "five_types"])
+def test_propagated_statistics_match_oracle(cuda, cfg):
+    """Per-event realized distributions of the GPU sampler vs the reference's
+    algorithm (the oracle) on the same DAG, independent seeds."""
+    if cfg == "config0":
+        flat, gen = W.config0()
+    else:
+        flat, gen = W.config1(seed=21, n_layers=25, width=40)
+    n = 100_000
+    prop = propagator_from_flat(m, flat, gen)
+    real_g, _, _ = prop.run_many_arrays(np.arange(n, dtype=np.int64) + 10**9, durations=False)
+    real_o, _, _ = oracle.OracleSim(flat, gen).run_many(np.arange(n), threads=os.cpu_count() or 1,
+                                                          want=("realized",))
+    ks_rate, mean_rate = _per_event_agreement(real_g, real_o, flat["earliest"])
+    assert ks_rate <= 0.03, ks_rate
+    assert mean_rate <= 0.01, mean_rate
+
+
+def test_reference_suite_bounds_and_known_answers(cuda):
+    """test/test_monte_carlo_extra.py:27-57 and test/test_simulator.py:37-137 on the GPU."""
+    ev = [m.Event("0", m.EventTimestamp(0.0, 100.0, 0.0)), m.Event("1", m.EventTimestamp(0.0, 100.0, 0.0)),
+          m.Event("2", m.EventTimestamp(0.0, 100.0, 0.0))]
+    acts = {(0, 1): m.Activity(idx=0, minimal_duration=1.0, activity_type=1),
+            (1, 2): m.Activity(idx=1, minimal_duration=2.0, activity_type=1)}
+    ctx = m.DagContext(events=ev, activities=acts, precedence_list=[(1, [(0, 0)]), (2, [(1, 1)])], max_delay=1e6)
+    g = m.GenericDelayGenerator()
+    g.add_constant(activity_type=1, factor=1.0)
+    r = m.Simulator(ctx, g).run(seed=42)
+    np.testing.assert_allclose(r.durations, [2.0, 4.0])
+    np.testing.assert_allclose(r.realized, [0.0, 2.0, 6.0])
+    for add in (lambda gg: gg.add_exponential(activity_type=1, lambda_=2.0, max_scale=0.5),
+                lambda gg: gg.add_gamma(activity_type=1, shape=2.0, scale=1.0, max_scale=0.5)):
+        gg = m.GenericDelayGenerator()
+        add(gg)
+        sim = m.Simulator(ctx, gg)
+        for res in sim.run_many(list(range(200))):
+            assert 1.0 <= res.durations[0] <= 1.5 and 2.0 <= res.durations[1] <= 3.0
+            assert res.realized[2] >= res.realized[1]
+        batch = sim.run_many(list(range(5)))
+        solo = [sim.run(s) for s in range(5)]
+        for b, s in zip(batch, solo):
+            np.testing.assert_array_equal(b.realized, s.realized)
+            np.testing.assert_array_equal(b.durations, s.durations)
+            np.testing.assert_array_equal(b.cause_event, s.cause_event)
+    # six-event DAG with an unmapped type and reversed precedence (test_simulator.py:64-137)
+    events = [m.Event(str(i), m.EventTimestamp(t, 100.0, 0.0)) for i, t in enumerate([0.0, 5.0, 10.0, 22.0, 20.0, 100.0])]
+    links = {(0, 1): m.Activity(0, 3.0, 1), (1, 2): m.Activity(1, 5.0, 1), (1, 3): m.Activity(2, 5.0, 1),
+             (2, 4): m.Activity(3, 15.0, 2), (3, 4): m.Activity(4, 10.0, 3)}
+    prec = [(1, [(0, 0)]), (2, [(1, 1)]), (3, [(1, 2)]), (4, [(2, 3), (3, 4)])]
+    g = m.GenericDelayGenerator()
+    g.add_constant(activity_type=1, factor=1.0)
+    g.add_constant(activity_type=3, factor=3.0)
+    for pl in (prec, list(reversed(prec))):
+        res = m.Simulator(m.DagContext(events, links, pl, 1e6), g).run_many(tuple(range(5)))[3]
+        assert list(res.durations) == [6.0, 10.0, 10.0, 15.0, 40.0]
+        assert list(res.realized) == [0.0, 6.0, 16.0, 22.0, 62.0, 100.0]
+        assert list(res.cause_event) == [-1, 0, 1, -1, 3, -1]
+    # empirical absolute: every realized value is one the table allows
+    g = m.GenericDelayGenerator()
+    g.add_empirical_absolute(activity_type=1, values=[10, 20, 40, 50], weights=[0.1, 0.2, 0.3, 0.4])
+    sim = m.Simulator(m.DagContext(events, links, prec, 1e6), g)
+    for res in sim.run_many(list(range(50))):
+        assert res.realized[3] in (5.0 + 3.0 + 10 + 5.0 + d for d in (10, 20, 40, 50)) or res.realized[3] >= 22.0
+        assert res.realized[5] == 100.0

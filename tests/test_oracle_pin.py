@@ -1,0 +1,175 @@
+"""Pins the C oracle to the reference (CPU only).
+
+1. Against the committed golden fixtures, which the reference itself produced
+   (tests/golden/make_golden.py): bit-exact on x86-64, where they were made.
+2. Against the known answers of the reference's own tests
+   (test/test_simulator.py, test/test_monte_carlo_extra.py, test/test_parity_suite.py).
+3. Against the reference compiled from source, when oracle/_ref is built here.
+"""
+from __future__ import annotations
+
+import math
+import platform
+
+import numpy as np
+import pytest
+
+import oracle
+import ref_loader
+from mcd_testlib import flat_from_lists, load_golden, six_event_flat
+
+EXACT_HOST = platform.machine() in ("x86_64", "AMD64")
+
+
+def _bits_equal(a, b):
+    return np.array_equal(np.asarray(a, np.float64).view(np.int64), np.asarray(b, np.float64).view(np.int64))
+
+
+@pytest.mark.parametrize("name", ["config0_ref.npz", "five_types_ref.npz", "gamma_state_ref.npz"])
+def test_oracle_matches_golden(name):
+    flat, gen, z = load_golden(name)
+    sim = oracle.OracleSim(flat, gen)
+    assert sim.node_count() == int(z["node_count"])
+    assert sim.activity_count() == int(z["activity_count"])
+    # propagation alone is pure IEEE add/compare: exact on every host
+    real, cause = sim.propagate_given(z["durations"])
+    assert _bits_equal(real, z["realized"])
+    assert np.array_equal(cause, z["cause"])
+    # the sampled stream (Xoshiro256++ + libstdc++ transforms over glibc's log)
+    r2, d2, c2 = sim.run_many(z["seeds"])
+    if EXACT_HOST:
+        assert _bits_equal(d2, z["durations"])
+        assert _bits_equal(r2, z["realized"])
+        assert np.array_equal(c2, z["cause"])
+    else:  # another libm may round log differently in the last place
+        np.testing.assert_allclose(d2, z["durations"], rtol=1e-12)
+
+
+def test_gamma_state_carries_across_runs():
+    """The reference's gamma draws depend on call history (cached normal)."""
+    _, _, z = load_golden("gamma_state_ref.npz")
+    assert list(z["seeds"]) == [5, 5, 6]
+    assert not np.array_equal(z["durations"][0], z["durations"][1])
+
+
+def _six(gen):
+    return oracle.OracleSim(six_event_flat(), gen)
+
+
+def test_known_answer_propagation():
+    """test/test_simulator.py:107-137."""
+    sim = _six([("constant", 1, 1.0), ("constant", 3, 3.0)])
+    real, dur, cause = sim.run_many(np.arange(5))
+    assert list(dur[3]) == [6.0, 10.0, 10.0, 15.0, 40.0]
+    assert list(real[3]) == [0.0, 6.0, 16.0, 22.0, 62.0, 100.0]
+    assert list(cause[3]) == [-1, 0, 1, -1, 3, -1]
+
+
+def test_known_answer_constant_small():
+    """test/test_monte_carlo_extra.py:27-34."""
+    flat = flat_from_lists([0.0, 0.0, 0.0], {(0, 1): (0, 1.0, 1), (1, 2): (1, 2.0, 1)},
+                           [(1, [(0, 0)]), (2, [(1, 1)])], 1e6)
+    real, dur, _ = oracle.OracleSim(flat, [("constant", 1, 1.0)]).run_many([42])
+    assert list(dur[0]) == [2.0, 4.0]
+    assert list(real[0]) == [0.0, 2.0, 6.0]
+
+
+def test_known_answer_empirical_streams():
+    """test/test_simulator.py:139-172: exact Xoshiro256++ / discrete_distribution streams."""
+    real, _, _ = _six([("empirical_absolute", 1, [10, 20, 40, 50], [0.1, 0.2, 0.3, 0.4])]).run_many([7])
+    assert real[0, 3] == 68.0 and real[0, 5] == 100.0
+    real, _, _ = _six([("empirical_relative", 1, [1.2, 1.3, 1.35, 4.5], [0.1, 0.2, 0.3, 0.4])]).run_many([7])
+    assert abs(real[0, 3] - 34.10) < 5e-5 and real[0, 5] == 100.0
+    # 1000-bin relative table from a truncated numpy exponential sample (seed 7)
+    rs = np.random.RandomState(7)
+    draws = rs.exponential(3.0, size=1_700_000)
+    values = draws[draws <= 5.0][:1_000_000]
+    assert len(values) == 1_000_000
+    hist, edges = np.histogram(values, bins=1000, density=True)
+    centers = 0.5 * (edges[:-1] + edges[1:])
+    real, _, _ = _six([("empirical_relative", 1, centers, hist)]).run_many([7])
+    assert abs(real[0, 3] - 23.062461393412335) < 5e-4 and real[0, 5] == 100.0
+
+
+def test_known_answer_chain():
+    """test/test_simulator.py:175-199: 10,000-event chain."""
+    n = 10_000
+    flat = flat_from_lists([float(i) for i in range(n)], {(i, i + 1): (i, 3.0, 1) for i in range(n - 1)},
+                           [(i, [(i - 1, i)]) for i in range(1, n)], 1e6)
+    real, dur, cause = oracle.OracleSim(flat, [("constant", 1, 1.0)]).run_many([7])
+    assert real.shape == (1, n) and dur.shape == (1, n - 1)
+    assert real[0, 9999] == 59988.0 and real[0, 0] == 0.0
+
+
+def test_bounds_exponential_gamma():
+    """test/test_monte_carlo_extra.py:36-57."""
+    flat = flat_from_lists([0.0, 0.0, 0.0], {(0, 1): (0, 1.0, 1), (1, 2): (1, 2.0, 1)},
+                           [(1, [(0, 0)]), (2, [(1, 1)])], 1e6)
+    for gen in ([("exponential", 1, 2.0, 0.5)], [("gamma", 1, 2.0, 1.0, 0.5)]):
+        _, dur, _ = oracle.OracleSim(flat, gen).run_many(np.arange(200))
+        assert (dur[:, 0] >= 1.0).all() and (dur[:, 0] <= 1.5).all()
+        assert (dur[:, 1] >= 2.0).all() and (dur[:, 1] <= 3.0).all()
+
+
+@pytest.mark.parametrize("case,msg", [
+    ("cycle", "cycle detected"), ("reserved", "reserved"), ("max_delay", "max_delay must be non-negative")])
+def test_errors(case, msg):
+    """test/test_monte_carlo_extra.py:60-92."""
+    if case == "cycle":
+        flat = flat_from_lists([0.0, 0.0], {(0, 1): (0, 1.0, 1), (1, 0): (1, 1.0, 1)},
+                               [(1, [(0, 0)]), (0, [(1, 1)])], 1e6)
+        gen = [("constant", 1, 0.0)]
+    else:
+        flat = flat_from_lists([0.0, 0.0, 0.0], {(0, 1): (0, 1.0, 1), (1, 2): (1, 2.0, 1)},
+                               [(1, [(0, 0)]), (2, [(1, 1)])], -1.0 if case == "max_delay" else 1e6)
+        gen = [("constant", -1 if case == "reserved" else 1, 0.0)]
+    with pytest.raises(oracle.OracleError, match=msg):
+        oracle.OracleSim(flat, gen)
+
+
+def test_table_length_mismatch():
+    with pytest.raises(oracle.OracleError, match="same length"):
+        oracle.OracleSim(six_event_flat(), [("empirical_absolute", 1, [1.0, 2.0], [1.0])])
+
+
+def _edge_flats():
+    """Small DAGs with the awkward cases: NaN/inf/-0 times, gaps in the link index
+    space, orphan links, unmapped types, reversed precedence order, ties."""
+    yield "six", six_event_flat()
+    yield "reversed", flat_from_lists(
+        [0.0, 5.0, 10.0, 22.0, 20.0, 100.0],
+        {(0, 1): (0, 3.0, 1), (1, 2): (1, 5.0, 1), (1, 3): (2, 5.0, 1), (2, 4): (3, 15.0, 2), (3, 4): (4, 10.0, 3)},
+        list(reversed([(1, [(0, 0)]), (2, [(1, 1)]), (3, [(1, 2)]), (4, [(2, 3), (3, 4)])])), 1e6)
+    yield "ties", flat_from_lists([0.0, 0.0, 0.0, 0.0], {(0, 3): (0, 5.0, 9), (1, 3): (1, 5.0, 9), (2, 3): (2, 5.0, 9)},
+                                  [(3, [(0, 0), (1, 1), (2, 2)])], 1e6)
+    yield "special", flat_from_lists(
+        [math.nan, -0.0, math.inf, 0.0, -math.inf, 3.0, 1.0],
+        {(0, 3): (0, 1.0, 1), (1, 3): (2, -0.0, 9), (2, 5): (5, 1.0, 1), (3, 5): (6, 2.0, 2), (4, 6): (7, 1.0, 1),
+         (1, 6): (9, 0.0, 9)},
+        [(3, [(0, 0), (1, 2)]), (5, [(2, 5), (3, 6)]), (6, [(4, 7), (1, 9)])], 1e6)
+    yield "zero_max_delay", flat_from_lists([0.0, 1.0, 2.0], {(0, 1): (0, 10.0, 1), (1, 2): (1, 10.0, 1)},
+                                            [(1, [(0, 0)]), (2, [(1, 1)])], 0.0)
+    yield "nan_max_delay", flat_from_lists([0.0, 1.0, 2.0], {(0, 1): (0, 10.0, 1), (1, 2): (1, 10.0, 1)},
+                                           [(1, [(0, 0)]), (2, [(1, 1)])], math.nan)
+
+
+@pytest.mark.skipif(not ref_loader.available(), reason="reference not compiled here (oracle/_ref)")
+@pytest.mark.parametrize("gen", [
+    [("constant", 1, 1.5), ("exponential", 2, 0.1, math.inf)],
+    [("gamma", 1, 0.4, 2.0), ("gamma", 2, 3.0, 0.5, 2.0)],
+    [("empirical_absolute", 1, [1.0, 2.0, 7.0], [0.0, 2.0, 1.0]), ("empirical_relative", 2, [0.5], [3.0])],
+    [("exponential", 1, 2.0, 0.5), ("constant", 2, -0.5), ("constant", 1, 0.25)],
+])
+def test_oracle_matches_reference_live(gen):
+    from mc_dagprop_gb300 import workloads as W
+
+    ref = ref_loader.load()
+    for name, flat in _edge_flats():
+        sim = oracle.OracleSim(flat, gen)
+        rsim = ref.MonteCarloPropagator(W.to_context(ref, flat), W.to_generator(ref, gen))
+        seeds = [-3, 0, 1, 2, 99, 2**31 - 1]
+        rr = rsim.run_many(seeds)
+        real, dur, cause = sim.run_many(seeds)
+        assert _bits_equal(dur, [r.durations for r in rr]), name
+        assert _bits_equal(real, [r.realized for r in rr]), name
+        assert np.array_equal(cause, [r.cause_event for r in rr]), name

@@ -2,10 +2,13 @@
 
 Workload (one "step"): the single-large-DAG configuration -- 200,000 events in
 2,000 layers of 100, ~500,000 links, five activity types, max_delay 3,600 s --
-for one chunk of `--samples` samples (default 4,864 = 152 SMs x 32) with full
-outputs (realized, durations, cause_event) written to HBM.  A step is one launch
-of the fused sampler+propagation kernel; its outputs (~31 GB) are far larger
-than L2, so no flush is needed between steps.
+for one chunk of `--samples` samples (default 19,456 = 4 waves of 152 SMs x 32
+samples) with full outputs (realized, durations, cause_event) resident in HBM.
+The configuration's 65,536-sample chunks would need 419 GB of outputs, more
+than HBM holds, so a step is the largest chunk that keeps all outputs resident
+with room to spare (125 GB).  A step is one launch of the fused
+sampler+propagation kernel; its outputs are far larger than L2, so no flush is
+needed between steps.
 
 Printed (one JSON line, rank 0):
   value      sample-edges/s with inputs resident in HBM (device-timed, CUDA events
@@ -186,7 +189,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--samples", type=int, default=4864)
+    ap.add_argument("--samples", type=int, default=19456)
     ap.add_argument("--e2e-samples", type=int, default=512)
     ap.add_argument("--layers", type=int, default=2000)
     ap.add_argument("--impl", default="gb300")
@@ -219,7 +222,12 @@ def main():
     real = torch.empty((E, ld), dtype=torch.float64, device=dev)
     durs = torch.empty((L, ld), dtype=torch.float64, device=dev)
     cause = torch.empty((E, ld), dtype=torch.int32, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    # Launch on the handle's own stream and time with events recorded on that
+    # same stream (torch's default stream handle is 0, which the C ABI reads as
+    # "the handle's stream", so wrap the handle's stream explicitly).
+    lib.mcd_dag_stream.argtypes = [C.c_void_p]
+    lib.mcd_dag_stream.restype = C.c_void_p
+    stream = torch.cuda.ExternalStream(lib.mcd_dag_stream(h), device=dev)
 
     def step():
         rc = lib.mcd_run_device(h, seeds.data_ptr(), S, real.data_ptr(), durs.data_ptr(), cause.data_ptr(), ld,
@@ -273,11 +281,9 @@ def main():
     peak, peak_kind = _peaks()
     traffic = None
     tf = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tf):
+    if os.path.exists(tf):  # one ncu capture of a smaller case, scaled by samples x links
         with open(tf) as f:
-            t = json.load(f)
-        if t.get("samples") and t.get("layers") == args.layers:
-            traffic = t["bytes_per_sample"] * S + t.get("fixed_bytes", 0)
+            traffic = json.load(f)["dram_bytes_per_sample_edge"] * S * L
 
     # e2e through the C ABI with pinned host buffers
     e2e = None

@@ -15,8 +15,9 @@
  *   mcd_run_many_host         Simulator::run_many / run        _core.cpp:312-361
  *   mcd_run_device            the same, device buffers, sample-minor layout
  *   mcd_propagate_*           the propagation loop alone       _core.cpp:331-350
- *   mcd_stats_*               per-event statistics (no reference counterpart;
- *                             the reference's users stack run_many results in numpy)
+ *   mcd_stats_*               per-event statistics (no reference counterpart; the
+ *                             reference's users stack run_many results in numpy,
+ *                             demo/monte_carlo.py:48-49)
  *
  * Layouts.  "Sample-major" (host entry points) is the reference's SimResult
  * layout: one contiguous row per sample, realized[s*E + e], durations[s*L + l],
@@ -141,6 +142,28 @@ int mcd_propagate_device(mcd_dag *dag, const double *durations, int64_t ld_in, i
                          int32_t *cause_event, int64_t ld, void *stream);
 /* Synchronises the handle's stream and reports a latched kernel error, if any. */
 int mcd_dag_check(mcd_dag *dag);
+
+/* ---- Per-event statistics (the full sample matrix never leaves the chip) ----
+ * For each event over n samples: mean of realized (FP64, accumulated exactly as
+ * integer ticks of 2^-q s when all times are finite), p50/p90/p99 from a
+ * 256-bin histogram over [earliest, earliest + max_delay] whose exact atoms --
+ * realized == earliest ("on time") and realized == earliest + max_delay
+ * ("capped") -- are counted apart, and the on-time fraction.
+ * seeds[n] or, when seeds is NULL, seeds seed0 .. seed0+n-1.  Any output may be NULL.
+ * hist: [n_events][MCD_HIST_STRIDE] counts: bins 0..255, then on-time, capped, 2 unused. */
+#define MCD_HIST_BINS 256
+#define MCD_HIST_STRIDE 260
+typedef struct mcd_stats {
+    double *mean, *p50, *p90, *p99, *p_on_time; /* [n_events] each */
+    uint32_t *hist;                             /* [n_events][MCD_HIST_STRIDE] */
+} mcd_stats;
+/* Host outputs; returns when they are written. */
+int mcd_stats_host(mcd_dag *dag, const int64_t *seeds, int64_t seed0, int64_t n, const mcd_stats *out);
+/* Device outputs (and device seeds), asynchronous on `stream` (NULL = the handle's stream). */
+int mcd_stats_device(mcd_dag *dag, const int64_t *seeds, int64_t seed0, int64_t n, const mcd_stats *out,
+                     void *stream);
+/* Width in seconds of one histogram bin for a run of n samples. */
+int mcd_stats_bin_width(const mcd_dag *dag, int64_t n, double *out);
 
 /* ---- Pinned host memory ---- */
 int mcd_host_alloc(size_t bytes, void **out);

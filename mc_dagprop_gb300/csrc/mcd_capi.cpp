@@ -14,7 +14,8 @@
 #include "mcd_host.hpp"
 
 namespace mcd {
-cudaError_t launch_propagate(const KArgs &a, bool given, bool win_smem, cudaStream_t st);
+cudaError_t launch_propagate(const KArgs &a, bool given, bool win_smem, bool stats, cudaStream_t st);
+cudaError_t launch_stats_finish(const FArgs &f, cudaStream_t st);
 cudaError_t launch_transpose_f64(const double *in, int64_t ld_in, double *out, int64_t ld_out, int64_t rows,
                                  int64_t cols, cudaStream_t st);
 cudaError_t launch_transpose_i32(const int32_t *in, int64_t ld_in, int32_t *out, int64_t ld_out, int64_t rows,
@@ -35,6 +36,8 @@ struct mcd_dag {
     DistParam *d_dist = nullptr;
     AliasEntry *d_alias = nullptr;
     int32_t *d_wk = nullptr;
+    double *d_earliest = nullptr;  // caller order, for the statistics finish
+    double *d_ub = nullptr;
     int32_t *d_err = nullptr;
     char *ws = nullptr;  // workspace
     size_t ws_bytes = 0;
@@ -236,8 +239,9 @@ int mcd_dag_create(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag *
                      s_aux = align_up(h.aux.size() * sizeof(LinkRec), 256),
                      s_dist = align_up(h.dist.size() * sizeof(DistParam), 256),
                      s_alias = align_up(h.alias.size() * sizeof(AliasEntry), 256),
-                     s_wk = align_up(h.wk_off.size() * sizeof(int32_t), 256), s_err = 256;
-        g->dbytes = s_ev + s_pred + s_aux + s_dist + s_alias + s_wk + s_err;
+                     s_wk = align_up(h.wk_off.size() * sizeof(int32_t), 256),
+                     s_times = align_up(h.earliest.size() * sizeof(double), 256), s_err = 256;
+        g->dbytes = s_ev + s_pred + s_aux + s_dist + s_alias + s_wk + 2 * s_times + s_err;
         cuda_check(cudaMalloc(&g->dmem, g->dbytes), "compiled DAG allocation");
         char *p = g->dmem;
         auto place = [&](auto *&dst, const auto &vec, size_t sz) {
@@ -253,6 +257,8 @@ int mcd_dag_create(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag *
         place(g->d_dist, h.dist, s_dist);
         place(g->d_alias, h.alias, s_alias);
         place(g->d_wk, h.wk_off, s_wk);
+        place(g->d_earliest, h.earliest, s_times);
+        place(g->d_ub, h.ub, s_times);
         g->d_err = reinterpret_cast<int32_t *>(p);
         cuda_check(cudaMemset(g->d_err, 0, sizeof(int32_t)), "error flag init");
         *out = g;
@@ -328,7 +334,7 @@ int mcd_run_device(mcd_dag *g, const int64_t *seeds, int64_t n, double *realized
             ensure_ws(g, (size_t)g->h.E * (size_t)ld * 8);
             a.scratch = (double *)g->ws;
         }
-        cuda_check(launch_propagate(a, false, g->h.win_smem, st), "propagate launch");
+        cuda_check(launch_propagate(a, false, g->h.win_smem, false, st), "propagate launch");
     });
 }
 
@@ -351,7 +357,7 @@ int mcd_propagate_device(mcd_dag *g, const double *dur, int64_t ld_in, int64_t n
             ensure_ws(g, (size_t)g->h.E * (size_t)ld * 8);
             a.scratch = (double *)g->ws;
         }
-        cuda_check(launch_propagate(a, true, g->h.win_smem, st), "propagate launch");
+        cuda_check(launch_propagate(a, true, g->h.win_smem, false, st), "propagate launch");
     });
 }
 
@@ -381,7 +387,7 @@ int mcd_run_many_host(mcd_dag *g, const int64_t *seeds, int64_t n, double *reali
             a.realized = cb[k].real_minor;  // always: also the spill rows of a global window
             a.durations = durations ? cb[k].dur_minor : nullptr;
             a.cause = cause ? cb[k].cause_minor : nullptr;
-            cuda_check(launch_propagate(a, false, g->h.win_smem, st), "propagate launch");
+            cuda_check(launch_propagate(a, false, g->h.win_smem, false, st), "propagate launch");
             if (realized) {
                 cuda_check(launch_transpose_f64(cb[k].real_minor, C, cb[k].real_major, E, E, m, st), "transpose");
                 cuda_check(cudaMemcpyAsync(realized + off * E, cb[k].real_major, (size_t)(m * E) * 8,
@@ -435,7 +441,7 @@ int mcd_propagate_host(mcd_dag *g, const double *durations, int64_t n, double *r
             a.cause = cause ? cb[k].cause_minor : nullptr;
             a.dur_in = cb[k].dur_minor;
             a.ld_in = C;
-            cuda_check(launch_propagate(a, true, g->h.win_smem, st), "propagate launch");
+            cuda_check(launch_propagate(a, true, g->h.win_smem, false, st), "propagate launch");
             if (realized) {
                 cuda_check(launch_transpose_f64(cb[k].real_minor, C, cb[k].real_major, E, E, m, st), "transpose");
                 cuda_check(cudaMemcpyAsync(realized + off * E, cb[k].real_major, (size_t)(m * E) * 8,
@@ -451,6 +457,122 @@ int mcd_propagate_host(mcd_dag *g, const double *durations, int64_t n, double *r
             }
         }
         check_device_error(g);
+    });
+}
+
+// Statistics of n samples into device outputs, asynchronously on st.  The
+// handle's workspace holds the per-event accumulators (and, when the window is
+// not on chip, scratch realized rows for one chunk of samples at a time).
+static void stats_device(mcd_dag *g, const int64_t *seeds, int64_t seed0, int64_t n, const mcd_stats *out,
+                         cudaStream_t st) {
+    const HostDag &h = g->h;
+    const size_t E = (size_t)h.E;
+    const StatsParams sp = stats_params(h, n);
+    int64_t C = n;
+    size_t scratch_bytes = 0;
+    if (!h.win_smem) {
+        C = std::max<int64_t>(32, std::min<int64_t>(n, (int64_t)((512ull << 20) / std::max<size_t>(E * 8, 1)) / 32 * 32));
+        scratch_bytes = align_up(E * (size_t)C * 8, 256);
+    }
+    const size_t acc_bytes = align_up(E * 8, 256), hist_bytes = align_up(E * kHistStride * 4, 256);
+    ensure_ws(g, acc_bytes + hist_bytes + scratch_bytes);
+    auto *acc = reinterpret_cast<unsigned long long *>(g->ws);
+    auto *hist = reinterpret_cast<uint32_t *>(g->ws + acc_bytes);
+    double *scratch = scratch_bytes ? reinterpret_cast<double *>(g->ws + acc_bytes + hist_bytes) : nullptr;
+    cuda_check(cudaMemsetAsync(g->ws, 0, acc_bytes + hist_bytes, st), "accumulator reset");
+    for (int64_t off = 0; off < n; off += C) {
+        const int64_t m = std::min(C, n - off);
+        KArgs a = base_args(g);
+        a.seeds = seeds ? seeds + off : nullptr;
+        a.seed0 = seed0 + off;
+        a.n = m;
+        a.ld = C;
+        a.scratch = scratch;
+        a.stats_fixed = sp.fixed;
+        a.tick_q = sp.q;
+        a.bin_mul = sp.bin_mul;
+        a.hist_inv_w = sp.inv_w;
+        a.acc = acc;
+        a.hist = hist;
+        cuda_check(launch_propagate(a, false, h.win_smem, true, st), "statistics launch");
+    }
+    FArgs f{};
+    f.acc = acc;
+    f.hist = hist;
+    f.earliest = g->d_earliest;
+    f.ub = g->d_ub;
+    f.E = h.E;
+    f.stats_fixed = sp.fixed;
+    f.tick_q = sp.q;
+    f.bin_w = sp.bin_w;
+    f.n = n;
+    f.mean = out->mean;
+    f.p50 = out->p50;
+    f.p90 = out->p90;
+    f.p99 = out->p99;
+    f.p_on_time = out->p_on_time;
+    cuda_check(launch_stats_finish(f, st), "statistics finish");
+    if (out->hist)
+        cuda_check(cudaMemcpyAsync(out->hist, hist, E * kHistStride * 4, cudaMemcpyDeviceToDevice, st),
+                   "histogram copy");
+}
+
+int mcd_stats_device(mcd_dag *g, const int64_t *seeds, int64_t seed0, int64_t n, const mcd_stats *out,
+                     void *stream) {
+    return guarded([&] {
+        if (!g || !out) throw McdError(MCD_ERR_INVALID, "null argument");
+        if (n <= 0 || n > (int64_t)1 << 31) throw McdError(MCD_ERR_INVALID, "need 0 < n <= 2^31 samples");
+        cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
+        stats_device(g, seeds, seed0, n, out, stream ? (cudaStream_t)stream : g->stream[0]);
+    });
+}
+
+int mcd_stats_host(mcd_dag *g, const int64_t *seeds, int64_t seed0, int64_t n, const mcd_stats *out) {
+    return guarded([&] {
+        if (!g || !out) throw McdError(MCD_ERR_INVALID, "null argument");
+        if (n <= 0 || n > (int64_t)1 << 31) throw McdError(MCD_ERR_INVALID, "need 0 < n <= 2^31 samples");
+        cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
+        cudaStream_t st = g->stream[0];
+        const size_t E = (size_t)g->h.E;
+        // device copies of the seeds and the outputs live after the accumulators
+        const size_t acc_bytes = align_up(E * 8, 256), hist_bytes = align_up(E * kHistStride * 4, 256);
+        const size_t seeds_bytes = seeds ? align_up((size_t)n * 8, 256) : 0;
+        const size_t out_bytes = align_up(E * 8, 256);
+        const size_t hist_out = out->hist ? hist_bytes : 0;
+        // reserve: [outputs (5 x E doubles) | hist copy | seeds], then the accumulators
+        const size_t head = 5 * out_bytes + hist_out + seeds_bytes;
+        if (!g->h.win_smem) {
+            const int64_t C = std::max<int64_t>(32, std::min<int64_t>(n, (int64_t)((512ull << 20) / std::max<size_t>(E * 8, 1)) / 32 * 32));
+            ensure_ws(g, head + acc_bytes + hist_bytes + align_up(E * (size_t)C * 8, 256));
+        } else {
+            ensure_ws(g, head + acc_bytes + hist_bytes);
+        }
+        // stats_device carves its accumulators from the start of the workspace,
+        // so the staging area goes at the end
+        char *tail = g->ws + g->ws_bytes - head;
+        double *o[5];
+        for (int k = 0; k < 5; ++k) o[k] = reinterpret_cast<double *>(tail + k * out_bytes);
+        uint32_t *dh = out->hist ? reinterpret_cast<uint32_t *>(tail + 5 * out_bytes) : nullptr;
+        int64_t *ds = seeds ? reinterpret_cast<int64_t *>(tail + 5 * out_bytes + hist_out) : nullptr;
+        if (seeds) cuda_check(cudaMemcpyAsync(ds, seeds, (size_t)n * 8, cudaMemcpyHostToDevice, st), "seed upload");
+        mcd_stats dev{out->mean ? o[0] : nullptr, out->p50 ? o[1] : nullptr, out->p90 ? o[2] : nullptr,
+                      out->p99 ? o[3] : nullptr, out->p_on_time ? o[4] : nullptr, dh};
+        stats_device(g, ds, seed0, n, &dev, st);
+        double *host_out[5] = {out->mean, out->p50, out->p90, out->p99, out->p_on_time};
+        for (int k = 0; k < 5; ++k)
+            if (host_out[k])
+                cuda_check(cudaMemcpyAsync(host_out[k], o[k], E * 8, cudaMemcpyDeviceToHost, st), "stats download");
+        if (out->hist)
+            cuda_check(cudaMemcpyAsync(out->hist, dh, E * kHistStride * 4, cudaMemcpyDeviceToHost, st),
+                       "histogram download");
+        check_device_error(g);
+    });
+}
+
+int mcd_stats_bin_width(const mcd_dag *g, int64_t n, double *out) {
+    return guarded([&] {
+        if (!g || !out) throw McdError(MCD_ERR_INVALID, "null argument");
+        *out = stats_params(g->h, n).bin_w;
     });
 }
 

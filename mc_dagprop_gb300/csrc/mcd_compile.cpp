@@ -377,7 +377,17 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H) {
     H.pred.reserve((size_t)(d.n_targets > 0 ? d.pred_offsets[d.n_targets] : 0));
     std::vector<char> referenced((size_t)L, 0), written((size_t)L, 0);
     H.earliest.assign(d.earliest, d.earliest + E);
+    H.ub.resize((size_t)E);
     H.max_delay = d.max_delay;
+    H.times_finite = std::isfinite(d.max_delay);
+    H.max_abs_time = 0.0;
+    H.max_span = 0.0;
+    for (int32_t e = 0; e < E; ++e) {
+        H.ub[e] = d.earliest[e] + d.max_delay;
+        if (!std::isfinite(d.earliest[e]) || !std::isfinite(H.ub[e])) H.times_finite = false;
+        H.max_abs_time = std::max(H.max_abs_time, std::max(std::fabs(d.earliest[e]), std::fabs(H.ub[e])));
+        H.max_span = std::max(H.max_span, H.ub[e] - d.earliest[e]);
+    }
     for (int32_t i = 0; i < E; ++i) {
         const int32_t e = order[i];
         EvRec r{};
@@ -425,6 +435,40 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H) {
         if (!referenced[l]) ++H.n_orphan;
         if (!written[l]) H.aux.push_back(LinkRec{l, H.link_kd[l], H.link_v[l]});
     }
+}
+
+// Ticks of 2^-q seconds: every |time| * 2^q must stay below 2^62, and the sum
+// over n samples of (realized - earliest) * 2^q below 2^63.
+StatsParams stats_params(const HostDag &h, int64_t n) {
+    StatsParams p;
+    const double span = std::max(h.max_span, 0.0);
+    if (h.times_finite) {
+        const int lg_abs = (int)std::ceil(std::log2(std::max(h.max_abs_time, 1.0) * 1.001));
+        const int lg_span = (int)std::ceil(std::log2(std::max(span, 1e-300) * 1.001 + 1e-300));
+        const int lg_n = (int)std::ceil(std::log2((double)std::max<int64_t>(n, 2)));
+        int q = std::min(61 - lg_abs, 62 - lg_n - std::max(lg_span, -1000));
+        q = std::min(q, 1000);
+        if (q >= -60) {
+            p.fixed = 1;
+            p.q = q;
+            const long double dt = std::ceil((long double)span * std::ldexp(1.0L, q)) + 1.0L;  // span in ticks
+            if (dt <= (long double)kHistBins) {
+                p.bin_mul = ~0ull;  // spans under 256 ticks: the tick count is the bin
+                p.bin_w = 1.0 / std::ldexp(1.0, q);
+            } else {
+                const long double mul = std::ldexp((long double)kHistBins, 64) / dt;
+                p.bin_mul = mul >= 18446744073709551615.0L ? ~0ull : (unsigned long long)mul;
+                p.bin_w = (double)(dt / kHistBins / std::ldexp(1.0L, q));
+            }
+            return p;
+        }
+    }
+    p.fixed = 0;
+    if (std::isfinite(span) && span > 0.0) {
+        p.inv_w = (double)kHistBins / span;
+        p.bin_w = span / kHistBins;
+    }
+    return p;
 }
 
 }  // namespace mcd

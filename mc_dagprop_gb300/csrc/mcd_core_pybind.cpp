@@ -269,6 +269,44 @@ class Propagator {
         raise_status(rc);
         return py::make_tuple(real, cause);
     }
+    py::dict run_stats(py::object seeds, int64_t n, int64_t seed0, bool hist) {
+        std::vector<int64_t> sv;
+        if (!seeds.is_none()) {
+            auto a = py::array_t<int64_t, py::array::c_style | py::array::forcecast>::ensure(seeds);
+            if (!a || a.ndim() != 1) throw py::value_error("seeds must be a 1-D integer array");
+            sv.assign(a.data(), a.data() + a.size());
+            n = (int64_t)sv.size();
+        }
+        if (n <= 0) throw py::value_error("need seeds or n > 0");
+        py::array_t<double> mean(E_), p50(E_), p90(E_), p99(E_), pot(E_);
+        py::object h = py::none();
+        uint32_t *hp = nullptr;
+        if (hist) {
+            py::array_t<uint32_t> ha({E_, (int64_t)MCD_HIST_STRIDE});
+            hp = ha.mutable_data();
+            h = ha;
+        }
+        mcd_stats st{mean.mutable_data(), p50.mutable_data(), p90.mutable_data(), p99.mutable_data(),
+                     pot.mutable_data(), hp};
+        int rc;
+        {
+            py::gil_scoped_release release;
+            rc = mcd_stats_host(dag_.get(), sv.empty() ? nullptr : sv.data(), seed0, n, &st);
+        }
+        raise_status(rc);
+        double bw = 0.0;
+        raise_status(mcd_stats_bin_width(dag_.get(), n, &bw));
+        py::dict d;
+        d["mean"] = mean;
+        d["p50"] = p50;
+        d["p90"] = p90;
+        d["p99"] = p99;
+        d["p_on_time"] = pot;
+        d["hist"] = h;
+        d["bin_width"] = bw;
+        d["n"] = n;
+        return d;
+    }
     py::dict info() const {
         mcd_dag_info i{};
         raise_status(mcd_dag_get_info(dag_.get(), &i));
@@ -479,6 +517,10 @@ PYBIND11_MODULE(_core, m) {
              "Batch run returning (realized (S,E), durations (S,L) or None, cause_event (S,E)) arrays")
         .def("propagate", &Propagator::propagate, py::arg("durations"),
              "Propagation alone from given durations (S,L): returns (realized, cause_event)")
+        .def("run_stats", &Propagator::run_stats, py::arg("seeds") = py::none(), py::arg("n") = 0,
+             py::arg("seed0") = 0, py::arg("hist") = false,
+             "Per-event statistics over samples (seeds, or seed0..seed0+n-1) computed on the GPU: "
+             "dict of mean, p50, p90, p99, p_on_time (and the raw histogram when hist=True)")
         .def("info", &Propagator::info, "Compiled-DAG facts")
         .def("_handle", [](const Propagator &p) { return (uintptr_t)p.handle(); });
 }

@@ -57,8 +57,23 @@ struct HostDag {
     std::vector<int32_t> link_kd;
     std::vector<double> link_v;
     std::vector<double> earliest;  // caller order
+    std::vector<double> ub;        // earliest + max_delay, caller order
     double max_delay = 0.0;
+    // statistics: all times finite -> exact integer-tick accumulation is possible
+    bool times_finite = true;
+    double max_abs_time = 0.0;  // max |earliest|, |ub|
+    double max_span = 0.0;      // max (ub - earliest)
 };
+
+// Per-call parameters of the statistics mode (depend on the sample count).
+struct StatsParams {
+    int32_t fixed = 0;
+    int32_t q = 0;
+    unsigned long long bin_mul = 0;
+    double inv_w = 0.0;
+    double bin_w = 0.0;  // seconds per bin
+};
+StatsParams stats_params(const HostDag &h, int64_t n);
 
 void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &out);
 int64_t order_key_host(int64_t bits);

@@ -78,6 +78,14 @@ struct alignas(16) AliasEntry {
     uint32_t pad[3];
 };
 
+// Per-event statistics layout: 256 equal bins over [earliest, earliest +
+// max_delay] plus two exact atoms -- realized == earliest (not delayed) and
+// realized == earliest + max_delay (capped) -- padded to 260 counters.
+constexpr int kHistBins = 256;
+constexpr int kBinLo = 256;
+constexpr int kBinHi = 257;
+constexpr int kHistStride = 260;
+
 // Arguments of the propagation kernels.
 struct KArgs {
     const EvRec *ev;
@@ -90,7 +98,8 @@ struct KArgs {
     int32_t n_warps;
     int32_t n_aux;
     int32_t window_slots;
-    const int64_t *seeds;  // [n] per-sample seeds
+    const int64_t *seeds;  // [n] per-sample seeds; null: sample s uses seed0 + s
+    int64_t seed0;
     int64_t n;
     int64_t ld;            // leading dimension of the sample-minor outputs
     double *realized;      // [E][ld] or null (then `scratch` holds the rows the window spills)
@@ -100,6 +109,27 @@ struct KArgs {
     int64_t ld_in;
     double *scratch;       // [E][ld] realized rows when the window is not on chip and realized is null
     int32_t *err;          // latched device error flags
+    // statistics mode
+    int32_t stats_fixed;          // 1: realized - earliest accumulated as exact integer ticks
+    int32_t tick_q;               // tick = 2^-tick_q seconds
+    unsigned long long bin_mul;   // bin = mulhi64(delta_ticks, bin_mul)
+    double hist_inv_w;            // FP64 fallback: 256 / max_delay, 0 when not finite
+    unsigned long long *acc;      // [E] sum of delta ticks (fixed) or FP64 sum bits (fallback)
+    uint32_t *hist;               // [E][kHistStride]
+};
+
+// Arguments of the statistics finishing kernel.
+struct FArgs {
+    const unsigned long long *acc;
+    const uint32_t *hist;
+    const double *earliest;  // caller order
+    const double *ub;        // earliest + max_delay, caller order
+    int32_t E;
+    int32_t stats_fixed;
+    int32_t tick_q;
+    double bin_w;            // seconds per bin
+    int64_t n;               // samples accumulated
+    double *mean, *p50, *p90, *p99, *p_on_time;  // [E] each, any may be null
 };
 
 // Device error flags.

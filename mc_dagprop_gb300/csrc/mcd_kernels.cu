@@ -146,11 +146,56 @@ __device__ __forceinline__ double link_duration(int32_t kd, double v, uint32_t l
     }
 }
 
+// ---------------------------------------------------------------- statistics helpers
+// x * 2^q truncated toward zero, from the bits of a finite double x with
+// |x| * 2^q < 2^62 (the host picks q so that every realized time qualifies).
+__device__ __forceinline__ long long to_ticks(long long b, int q) {
+    const int e = (int)((b >> 52) & 0x7FF);
+    const long long m = (b & 0xFFFFFFFFFFFFFll) | (e ? (1ll << 52) : 0ll);
+    const int sh = (e ? e : 1) - 1075 + q;
+    long long t;
+    if (sh >= 0) t = m << sh;
+    else t = sh > -63 ? (m >> -sh) : 0ll;
+    return b < 0 ? -t : t;
+}
+
+// One event's realized values of the tile into the per-event accumulators:
+// the tile's sum of (realized - earliest) with one 64-bit atomic, and the
+// histogram with one atomic per distinct bin of the warp.
+__device__ __forceinline__ void accumulate_stats(const KArgs &a, const EvRec &ev, long long lbits, bool active,
+                                                 unsigned active_mask) {
+    int bin;
+    if (a.stats_fixed) {
+        const long long te = to_ticks(ev.init_bits, a.tick_q);
+        long long d = active ? to_ticks(lbits, a.tick_q) - te : 0ll;
+        const unsigned long long du = (unsigned long long)(d > 0 ? d : 0ll);
+        bin = (int)__umul64hi(du, a.bin_mul);
+        bin = bin > kHistBins - 1 ? kHistBins - 1 : bin;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xFFFFFFFFu, d, off);
+        if ((threadIdx.x & 31) == 0 && d != 0) atomicAdd(&a.acc[ev.user], (unsigned long long)d);
+    } else {
+        const double dd = active ? __longlong_as_double(lbits) - __longlong_as_double(ev.init_bits) : 0.0;
+        const double x = dd * a.hist_inv_w;
+        bin = x >= (double)(kHistBins - 1) ? kHistBins - 1 : (x > 0.0 ? (int)x : 0);
+        if (active && dd != 0.0) atomicAdd(reinterpret_cast<double *>(&a.acc[ev.user]), dd);
+    }
+    if (lbits == ev.init_bits) bin = kBinLo;
+    else if (lbits == ev.ub_bits) bin = kBinHi;
+    if (active) {
+        const unsigned same = __match_any_sync(active_mask, bin);
+        if ((threadIdx.x & 31) == __ffs(same) - 1)
+            atomicAdd(&a.hist[(int64_t)ev.user * kHistStride + bin], (unsigned)__popc(same));
+    }
+}
+
 // ---------------------------------------------------------------- propagation
-// GIVEN: durations come from a_.dur_in instead of the sampler.
+// GIVEN: durations come from a.dur_in instead of the sampler.
 // WIN_SMEM: predecessor values come from the shared-memory window; otherwise
 // from the realized rows in global memory (the output, or scratch).
-template <bool GIVEN, bool WIN_SMEM>
+// STATS: instead of output rows, each event's realized values feed the
+// per-event accumulators (mean, histogram); nothing per sample leaves the chip.
+template <bool GIVEN, bool WIN_SMEM, bool STATS>
 __global__ void __launch_bounds__(512) k_propagate(const KArgs a) {
     extern __shared__ double win[];  // [window_slots][kTile]
     const int lane = threadIdx.x & 31;
@@ -158,10 +203,12 @@ __global__ void __launch_bounds__(512) k_propagate(const KArgs a) {
     const int NW = a.n_warps;
     const int64_t s = (int64_t)blockIdx.x * kTile + lane;
     const bool active = s < a.n;
+    const unsigned active_mask = __ballot_sync(0xFFFFFFFFu, active);
     uint64_t seed = 0;
-    if (!GIVEN && active) seed = (uint64_t)a.seeds[s];
+    if (!GIVEN && active) seed = a.seeds ? (uint64_t)a.seeds[s] : (uint64_t)(a.seed0 + s);
     const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
     double *rows = a.realized ? a.realized : a.scratch;  // global realized rows
+    if (STATS && WIN_SMEM) rows = nullptr;
 
     for (int l = 0; l < a.n_levels; ++l) {
         const int ib = __ldg(&a.wk_off[l * NW + warp]);
@@ -177,7 +224,8 @@ __global__ void __launch_bounds__(512) k_propagate(const KArgs a) {
                     dur = (active && pr.link >= 0) ? __ldg(&a.dur_in[(int64_t)pr.link * a.ld_in + s]) : 0.0;
                 } else {
                     dur = link_duration(pr.kd, pr.v, (uint32_t)pr.link, k0, k1, a.dist, a.alias, a.err);
-                    if ((pr.kd & KD_WRITE) && a.durations && active) a.durations[(int64_t)pr.link * a.ld + s] = dur;
+                    if (!STATS && (pr.kd & KD_WRITE) && a.durations && active)
+                        a.durations[(int64_t)pr.link * a.ld + s] = dur;
                 }
                 double src;
                 if (WIN_SMEM && pr.src_slot >= 0) {
@@ -201,22 +249,61 @@ __global__ void __launch_bounds__(512) k_propagate(const KArgs a) {
             if (ev.ub_key < lk) lbits = ev.ub_bits;  // realized = std::min(latest, ub)
             const double real = __longlong_as_double(lbits);
             if (WIN_SMEM && ev.slot >= 0) win[ev.slot * kTile + lane] = real;
+            if (STATS) accumulate_stats(a, ev, lbits, active, active_mask);
             if (active) {
                 const int64_t o = (int64_t)ev.user * a.ld + s;
                 if (rows) rows[o] = real;
-                if (a.cause) a.cause[o] = cause;
+                if (!STATS && a.cause) a.cause[o] = cause;
             }
         }
         __syncthreads();
     }
     // Aux pass: duration rows of fixed links and of links no precedence entry references.
-    if (!GIVEN && a.durations) {
+    if (!STATS && !GIVEN && a.durations) {
         for (int i = warp; i < a.n_aux; i += NW) {
             const LinkRec lr = a.aux[i];
             const double dur = link_duration(lr.kd, lr.v, (uint32_t)lr.link, k0, k1, a.dist, a.alias, a.err);
             if (active) a.durations[(int64_t)lr.link * a.ld + s] = dur;
         }
     }
+}
+
+// Quantile at probability p of one event from its histogram: rank p*(n-1) as
+// numpy's default ("linear") takes it, atoms exact, samples spread evenly
+// inside a bin.
+__device__ double hist_quantile(const uint32_t *h, int64_t n, double p, double lo, double hi, double w) {
+    const double k = p * (double)(n - 1);
+    const double c_lo = h[kBinLo], c_hi = h[kBinHi];
+    if (k < c_lo) return lo;
+    if (k >= (double)n - c_hi) return hi;
+    double cum = c_lo;
+    for (int b = 0; b < kHistBins; ++b) {
+        const double c = h[b];
+        if (c > 0.0 && k < cum + c) {
+            const double v = lo + ((double)b + (k - cum + 0.5) / c) * w;
+            return v < hi ? v : hi;
+        }
+        cum += c;
+    }
+    return hi;
+}
+
+__global__ void k_stats_finish(const FArgs f) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= f.E) return;
+    const double lo = f.earliest[e], hi = f.ub[e];
+    const double n = (double)f.n;
+    if (f.mean) {
+        double sum;
+        if (f.stats_fixed) sum = ldexp((double)(long long)f.acc[e], -f.tick_q);
+        else sum = __longlong_as_double((long long)f.acc[e]);
+        f.mean[e] = lo + sum / n;
+    }
+    const uint32_t *h = f.hist + (int64_t)e * kHistStride;
+    if (f.p50) f.p50[e] = hist_quantile(h, f.n, 0.50, lo, hi, f.bin_w);
+    if (f.p90) f.p90[e] = hist_quantile(h, f.n, 0.90, lo, hi, f.bin_w);
+    if (f.p99) f.p99[e] = hist_quantile(h, f.n, 0.99, lo, hi, f.bin_w);
+    if (f.p_on_time) f.p_on_time[e] = (double)h[kBinLo] / n;
 }
 
 // ---------------------------------------------------------------- layout change
@@ -238,19 +325,30 @@ __global__ void k_transpose(const T *__restrict__ in, int64_t ld_in, T *__restri
 }
 
 // ---------------------------------------------------------------- launchers
-cudaError_t launch_propagate(const KArgs &a, bool given, bool win_smem, cudaStream_t st) {
+cudaError_t launch_propagate(const KArgs &a, bool given, bool win_smem, bool stats, cudaStream_t st) {
     if (a.n <= 0) return cudaSuccess;
     const dim3 grid((unsigned)((a.n + kTile - 1) / kTile));
     const dim3 block((unsigned)(a.n_warps * 32));
     const size_t smem = win_smem ? (size_t)a.window_slots * kTile * sizeof(double) : 0;
     void (*fn)(const KArgs);
-    if (given) fn = win_smem ? k_propagate<true, true> : k_propagate<true, false>;
-    else fn = win_smem ? k_propagate<false, true> : k_propagate<false, false>;
+    if (stats) {
+        if (given) fn = win_smem ? k_propagate<true, true, true> : k_propagate<true, false, true>;
+        else fn = win_smem ? k_propagate<false, true, true> : k_propagate<false, false, true>;
+    } else {
+        if (given) fn = win_smem ? k_propagate<true, true, false> : k_propagate<true, false, false>;
+        else fn = win_smem ? k_propagate<false, true, false> : k_propagate<false, false, false>;
+    }
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     fn<<<grid, block, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stats_finish(const FArgs &f, cudaStream_t st) {
+    if (f.E <= 0) return cudaSuccess;
+    k_stats_finish<<<(unsigned)((f.E + 255) / 256), 256, 0, st>>>(f);
     return cudaGetLastError();
 }
 

@@ -162,6 +162,23 @@ int mcd_stats_host(mcd_dag *dag, const int64_t *seeds, int64_t seed0, int64_t n,
 /* Device outputs (and device seeds), asynchronous on `stream` (NULL = the handle's stream). */
 int mcd_stats_device(mcd_dag *dag, const int64_t *seeds, int64_t seed0, int64_t n, const mcd_stats *out,
                      void *stream);
+/* The same statistics without allocating device memory.  No counterpart in the
+ * reference.  Some callers cannot call cudaMalloc: their GPU memory is owned by
+ * another allocator (a framework's caching allocator that has reserved the
+ * device), or an allocation would synchronise the device inside their
+ * latency-critical loop.  This entry point keeps the per-event accumulators in a
+ * fixed 32 MiB device array that the library holds on every GPU it is loaded on
+ * until the process exits, so it supports DAGs of at most MCD_NOALLOC_MAX_EVENTS
+ * events whose propagation window fits in shared memory (larger ones fail with
+ * MCD_ERR_INVALID).  Inputs, outputs and the compiled DAG are the caller's, as in
+ * mcd_stats_device (device pointers; asynchronous on `stream`, NULL = the
+ * handle's stream).  The first call on a device looks the array's device address
+ * up; make that first call before any stream capture.  All calls share the one
+ * array, and each call clears it first: calls that overlap on the GPU (other
+ * streams, other threads, other handles) race and corrupt each other's results. */
+#define MCD_NOALLOC_MAX_EVENTS 32000
+int mcd_stats_device_noalloc(mcd_dag *dag, const int64_t *seeds, int64_t seed0, int64_t n, const mcd_stats *out,
+                             void *stream);
 /* Width in seconds of one histogram bin for a run of n samples. */
 int mcd_stats_bin_width(const mcd_dag *dag, int64_t n, double *out);
 

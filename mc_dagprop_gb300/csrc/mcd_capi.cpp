@@ -16,6 +16,7 @@
 namespace mcd {
 cudaError_t launch_propagate(const KArgs &a, bool given, bool win_smem, bool stats, cudaStream_t st);
 cudaError_t launch_stats_finish(const FArgs &f, cudaStream_t st);
+cudaError_t noalloc_scratch(void **ptr, size_t *bytes);
 cudaError_t launch_transpose_f64(const double *in, int64_t ld_in, double *out, int64_t ld_out, int64_t rows,
                                  int64_t cols, cudaStream_t st);
 cudaError_t launch_transpose_i32(const int32_t *in, int64_t ld_in, int32_t *out, int64_t ld_out, int64_t rows,
@@ -566,6 +567,71 @@ int mcd_stats_host(mcd_dag *g, const int64_t *seeds, int64_t seed0, int64_t n, c
             cuda_check(cudaMemcpyAsync(out->hist, dh, E * kHistStride * 4, cudaMemcpyDeviceToHost, st),
                        "histogram download");
         check_device_error(g);
+    });
+}
+
+// Statistics without any device allocation: the per-event accumulators live in
+// the library's fixed 32 MiB device array instead of the handle's workspace.
+// For callers that cannot allocate (their device memory belongs to another
+// allocator, or a cudaMalloc would stall their latency-critical loop).  The
+// first call on a device looks the array's address up; calls share the array,
+// so calls that overlap on the GPU race.
+int mcd_stats_device_noalloc(mcd_dag *g, const int64_t *seeds, int64_t seed0, int64_t n, const mcd_stats *out,
+                             void *stream) {
+    return guarded([&] {
+        if (!g || !out) throw McdError(MCD_ERR_INVALID, "null argument");
+        if (n <= 0 || n > (int64_t)1 << 31) throw McdError(MCD_ERR_INVALID, "need 0 < n <= 2^31 samples");
+        const HostDag &h = g->h;
+        if (!h.win_smem)
+            throw McdError(MCD_ERR_INVALID,
+                           "mcd_stats_device_noalloc needs a DAG whose window fits in shared memory");
+        cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
+        void *base = nullptr;
+        size_t cap = 0;
+        cuda_check(noalloc_scratch(&base, &cap), "fixed scratch lookup");
+        const size_t E = (size_t)h.E;
+        const size_t acc_bytes = align_up(E * 8, 256), hist_bytes = align_up(E * kHistStride * 4, 256);
+        if (h.E > MCD_NOALLOC_MAX_EVENTS || acc_bytes + hist_bytes > cap)
+            throw McdError(MCD_ERR_INVALID, "mcd_stats_device_noalloc supports at most " +
+                                                std::to_string(MCD_NOALLOC_MAX_EVENTS) + " events; this DAG has " +
+                                                std::to_string(h.E));
+        cudaStream_t st = stream ? (cudaStream_t)stream : g->stream[0];
+        auto *acc = reinterpret_cast<unsigned long long *>(base);
+        auto *hist = reinterpret_cast<uint32_t *>(static_cast<char *>(base) + acc_bytes);
+        // the array keeps the previous call's counts: start from zero
+        cuda_check(cudaMemsetAsync(base, 0, acc_bytes + hist_bytes, st), "fixed scratch reset");
+        const StatsParams sp = stats_params(h, n);
+        KArgs a = base_args(g);
+        a.seeds = seeds;
+        a.seed0 = seed0;
+        a.n = n;
+        a.ld = n;
+        a.stats_fixed = sp.fixed;
+        a.tick_q = sp.q;
+        a.bin_mul = sp.bin_mul;
+        a.hist_inv_w = sp.inv_w;
+        a.acc = acc;
+        a.hist = hist;
+        cuda_check(launch_propagate(a, false, true, true, st), "statistics launch");
+        FArgs f{};
+        f.acc = acc;
+        f.hist = hist;
+        f.earliest = g->d_earliest;
+        f.ub = g->d_ub;
+        f.E = h.E;
+        f.stats_fixed = sp.fixed;
+        f.tick_q = sp.q;
+        f.bin_w = sp.bin_w;
+        f.n = n;
+        f.mean = out->mean;
+        f.p50 = out->p50;
+        f.p90 = out->p90;
+        f.p99 = out->p99;
+        f.p_on_time = out->p_on_time;
+        cuda_check(launch_stats_finish(f, st), "statistics finish");
+        if (out->hist)
+            cuda_check(cudaMemcpyAsync(out->hist, hist, E * kHistStride * 4, cudaMemcpyDeviceToDevice, st),
+                       "histogram copy");
     });
 }
 

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "mcd_internal.hpp"
 
@@ -344,6 +345,37 @@ cudaError_t launch_propagate(const KArgs &a, bool given, bool win_smem, bool sta
     }
     fn<<<grid, block, smem, st>>>(a);
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- fixed scratch
+// Device scratch for mcd_stats_device_noalloc: the per-event accumulators
+// (8 bytes of sum + kHistStride 32-bit counters per event) of callers that
+// cannot allocate device memory.  32 MiB, held by every GPU that loads this
+// library until the process exits.  Host code must not use the symbol as an
+// address; noalloc_scratch() below looks the device address up.
+constexpr size_t kNoAllocScratchBytes = 32ull << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_noalloc_scratch on the current device, looked up once per
+// device (cudaGetSymbolAddress, with that device current) and cached.
+cudaError_t noalloc_scratch(void **ptr, size_t *bytes) {
+    constexpr int kMaxDevices = 64;
+    static void *cached[kMaxDevices] = {};
+    static std::mutex mu;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!cached[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        cached[dev] = p;
+    }
+    *ptr = cached[dev];
+    *bytes = kNoAllocScratchBytes;
+    return cudaSuccess;
 }
 
 cudaError_t launch_stats_finish(const FArgs &f, cudaStream_t st) {

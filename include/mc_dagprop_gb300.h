@@ -15,6 +15,7 @@
  *   mcd_run_many_host         Simulator::run_many / run        _core.cpp:312-361
  *   mcd_run_device            the same, device buffers, sample-minor layout
  *   mcd_propagate_*           the propagation loop alone       _core.cpp:331-350
+ *   mcd_batch_*               many DAGs in one persistent launch (no reference counterpart)
  *   mcd_stats_*               per-event statistics (no reference counterpart; the
  *                             reference's users stack run_many results in numpy,
  *                             demo/monte_carlo.py:48-49)
@@ -105,6 +106,10 @@ typedef struct mcd_dag_info {
     int32_t n_orphan_links;    /* links sampled but not referenced by precedence_list */
     int32_t device;
     int64_t device_bytes;      /* resident compiled-DAG bytes */
+    int32_t n_stages;          /* barrier-separated steps of the kernel (levels, wide ones split) */
+    int32_t smem_bytes;        /* shared memory per CTA */
+    int32_t positive;          /* 1: all times non-negative and finite (cheaper comparisons) */
+    int32_t tables_in_smem;    /* 1: distribution tables held in shared memory */
 } mcd_dag_info;
 
 /* Simulator::Simulator: validates, compiles to level-ordered CSR and uploads to
@@ -112,7 +117,16 @@ typedef struct mcd_dag_info {
  * afterwards.  Each handle owns one CUDA stream; a handle is not reentrant,
  * separate handles run concurrently. */
 int mcd_dag_create(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag **out);
+/* Compile options (the same call with explicit choices). */
+typedef struct mcd_dag_options {
+    int32_t n_warps; /* warps per CTA, 1..16; 0 = chosen from the DAG's level width */
+} mcd_dag_options;
+int mcd_dag_create_ex(const mcd_dag_desc *desc, const mcd_generator *gen, const mcd_dag_options *opts,
+                      mcd_dag **out);
 void mcd_dag_destroy(mcd_dag *dag);
+/* Compiles on the host only (no CUDA call) and reports what mcd_dag_create
+ * would build: validation errors are the same; device and device_bytes are -1. */
+int mcd_dag_describe(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag_info *info);
 int32_t mcd_dag_node_count(const mcd_dag *dag);
 int32_t mcd_dag_activity_count(const mcd_dag *dag);
 int mcd_dag_get_info(const mcd_dag *dag, mcd_dag_info *info);
@@ -181,6 +195,27 @@ int mcd_stats_device_noalloc(mcd_dag *dag, const int64_t *seeds, int64_t seed0, 
                              void *stream);
 /* Width in seconds of one histogram bin for a run of n samples. */
 int mcd_stats_bin_width(const mcd_dag *dag, int64_t n, double *out);
+
+/* ---- Batches: many DAGs, each with its own samples, in one persistent launch ----
+ * (no reference counterpart: the reference runs one DAG per run_many call).
+ * DAG i runs samples with seeds seed0[i] .. seed0[i]+n_samples[i]-1 and produces
+ * the same statistics as mcd_stats_* would for it alone.  All DAGs must share a
+ * device and be compiled with the same n_warps (mcd_dag_create_ex); they must
+ * outlive the batch.  A run is one CUDA graph (recorded on the first run,
+ * replayed after): accumulator reset, the persistent kernel over (DAG, tile)
+ * work items in longest-first order, the batched finish.  mcd_batch_run is
+ * asynchronous on the batch's own stream; mcd_batch_sync waits and reports
+ * kernel errors; mcd_batch_download copies DAG i's statistics to the host. */
+typedef struct mcd_batch mcd_batch;
+int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0, const int64_t *n_samples,
+                     mcd_batch **out);
+void mcd_batch_destroy(mcd_batch *batch);
+int mcd_batch_run(mcd_batch *batch);
+int mcd_batch_sync(mcd_batch *batch);
+int mcd_batch_download(mcd_batch *batch, int32_t i, const mcd_stats *host);
+void *mcd_batch_stream(const mcd_batch *batch);
+int64_t mcd_batch_items(const mcd_batch *batch);
+int32_t mcd_batch_grid(const mcd_batch *batch);
 
 /* ---- Pinned host memory ---- */
 int mcd_host_alloc(size_t bytes, void **out);

@@ -12,6 +12,7 @@ __version__ = "0.9.0+gb300"
 try:
     from .monte_carlo import (
         Activity,
+        Batch,
         DagContext,
         Event,
         EventTimestamp,
@@ -27,6 +28,7 @@ except ImportError as exc:  # the compiled module is missing: fail loudly
     ) from exc
 
 __all__ = [
+    "Batch",
     "GenericDelayGenerator",
     "DagContext",
     "SimResult",

@@ -1,0 +1,244 @@
+// mcd_batch.cpp -- many DAGs, each with its own samples, in one persistent launch.
+//
+// The work is a queue of (DAG, 32-sample tile) items, most expensive DAG first
+// (longest-processing-time order), consumed by a persistent grid of CTAs that
+// fills every SM whatever the DAGs' sizes -- a plain per-DAG launch of a DAG
+// with 1,000 samples keeps 32 CTAs busy and leaves the rest of the GPU idle.
+// Each run is one CUDA graph: reset the accumulators and the queue head, the
+// persistent statistics kernel, the batched finish.  The graph is recorded on
+// the first run and replayed afterwards.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <numeric>
+#include <string>
+
+#include "mcd_host.hpp"
+#include "mcd_handle.hpp"
+
+namespace mcd {
+cudaError_t launch_batch_stats(const BatchArgs &b, int n_warps, size_t smem, int grid, cudaStream_t st);
+cudaError_t batch_blocks_per_sm(int n_warps, size_t smem, int *out);
+cudaError_t launch_batch_finish(const FArgs *fs, int32_t n_dags, int32_t max_events, cudaStream_t st);
+}  // namespace mcd
+
+using namespace mcd;
+
+struct mcd_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<mcd_dag *> dags;
+    std::vector<int64_t> n, ev_off;
+    int n_warps = 1, grid = 1;
+    size_t smem = 0;
+    int32_t max_E = 0;
+    int64_t total_E = 0, n_items = 0;
+    char *dmem = nullptr;
+    size_t zero_bytes = 0;  // accumulators + queue head, cleared every run
+    double *out = nullptr;  // [5][total_E]: mean, p50, p90, p99, p_on_time
+    uint32_t *hist = nullptr;
+    FArgs *d_fargs = nullptr;
+    BatchArgs args{};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" {
+
+int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0, const int64_t *n_samples,
+                     mcd_batch **out) {
+    mcd_batch *B = nullptr;
+    int rc = guarded([&] {
+        if (!dags || !seed0 || !n_samples || !out || n_dags <= 0) throw McdError(MCD_ERR_INVALID, "bad arguments");
+        *out = nullptr;
+        B = new mcd_batch();
+        B->device = dags[0]->device;
+        B->n_warps = dags[0]->h.n_warps;
+        if (B->n_warps > kMaxBatchWarps)
+            throw McdError(MCD_ERR_INVALID, "DAGs of a batch must be compiled with n_warps <= 16");
+        for (int32_t i = 0; i < n_dags; ++i) {
+            const mcd_dag *g = dags[i];
+            if (!g) throw McdError(MCD_ERR_INVALID, "null DAG handle");
+            if (g->device != B->device) throw McdError(MCD_ERR_INVALID, "DAGs of a batch must share a device");
+            if (g->h.n_warps != B->n_warps)
+                throw McdError(MCD_ERR_INVALID, "DAGs of a batch must be compiled with the same n_warps");
+            if (n_samples[i] <= 0 || n_samples[i] > (int64_t)1 << 31)
+                throw McdError(MCD_ERR_INVALID, "each DAG needs 0 < n <= 2^31 samples");
+            B->dags.push_back(const_cast<mcd_dag *>(g));
+            B->n.push_back(n_samples[i]);
+        }
+        cuda_check(cudaSetDevice(B->device), "cudaSetDevice");
+        cuda_check(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking), "stream create");
+        // layout of the batch's device memory
+        bool any_global = false;
+        int32_t max_E_global = 0;
+        B->ev_off.resize((size_t)n_dags + 1, 0);
+        for (int32_t i = 0; i < n_dags; ++i) {
+            const HostDag &h = B->dags[i]->h;
+            B->smem = std::max(B->smem, (size_t)h.smem_total);
+            B->max_E = std::max(B->max_E, h.E);
+            if (!h.win_smem) {
+                any_global = true;
+                max_E_global = std::max(max_E_global, h.E);
+            }
+            B->ev_off[i + 1] = B->ev_off[i] + h.E;
+        }
+        B->total_E = B->ev_off[n_dags];
+        int per_sm = 0, sms = 0;
+        cuda_check(batch_blocks_per_sm(B->n_warps, B->smem, &per_sm), "occupancy query");
+        cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->device), "SM count");
+        B->grid = std::max(1, per_sm) * std::max(1, sms);
+        // items: DAGs by cost per tile, most expensive first; every tile of a DAG
+        std::vector<int32_t> order((size_t)n_dags);
+        std::iota(order.begin(), order.end(), 0);
+        auto cost = [&](int32_t i) { return (double)B->dags[i]->h.pred.size() + 2.0 * B->dags[i]->h.E; };
+        std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return cost(x) > cost(y); });
+        std::vector<int32_t> items;
+        for (int32_t i : order) {
+            const int64_t tiles = (B->n[i] + kTile - 1) / kTile;
+            for (int64_t t = 0; t < tiles; ++t) {
+                items.push_back(i);
+                items.push_back((int32_t)t);
+            }
+        }
+        B->n_items = (int64_t)items.size() / 2;
+        if (B->n_items > (int64_t)INT32_MAX) throw McdError(MCD_ERR_INVALID, "too many work items");
+        const size_t E = (size_t)B->total_E;
+        const size_t s_acc = align_up(E * 8, 256), s_hist = align_up(E * kHistStride * 4, 256), s_ctr = 256,
+                     s_out = align_up(5 * E * 8, 256), s_args = align_up((size_t)n_dags * sizeof(KArgs), 256),
+                     s_fargs = align_up((size_t)n_dags * sizeof(FArgs), 256),
+                     s_items = align_up(items.size() * 4, 256),
+                     s_scr = any_global ? align_up((size_t)B->grid * max_E_global * kTile * 8, 256) : 0;
+        B->zero_bytes = s_acc + s_hist + s_ctr;
+        cuda_check(cudaMalloc(&B->dmem, B->zero_bytes + s_out + s_args + s_fargs + s_items + s_scr),
+                   "batch allocation");
+        char *p = B->dmem;
+        auto *acc = reinterpret_cast<unsigned long long *>(p);
+        B->hist = reinterpret_cast<uint32_t *>(p + s_acc);
+        auto *counter = reinterpret_cast<unsigned int *>(p + s_acc + s_hist);
+        p += B->zero_bytes;
+        B->out = reinterpret_cast<double *>(p);
+        p += s_out;
+        auto *d_args = reinterpret_cast<KArgs *>(p);
+        p += s_args;
+        B->d_fargs = reinterpret_cast<FArgs *>(p);
+        p += s_fargs;
+        auto *d_items = reinterpret_cast<int32_t *>(p);
+        p += s_items;
+        double *scratch = s_scr ? reinterpret_cast<double *>(p) : nullptr;
+        // per-DAG kernel and finish arguments
+        std::vector<KArgs> ka((size_t)n_dags);
+        std::vector<FArgs> fa((size_t)n_dags);
+        for (int32_t i = 0; i < n_dags; ++i) {
+            mcd_dag *g = B->dags[i];
+            const StatsParams sp = stats_params(g->h, B->n[i]);
+            KArgs a = base_args(g);
+            a.seeds = nullptr;
+            a.seed0 = seed0[i];
+            a.n = B->n[i];
+            a.ld = 0;
+            a.stats_fixed = sp.fixed;
+            a.tick_q = sp.q;
+            a.bin_mul = sp.bin_mul;
+            a.hist_inv_w = sp.inv_w;
+            a.acc = acc + B->ev_off[i];
+            a.hist = B->hist + (size_t)B->ev_off[i] * kHistStride;
+            ka[i] = a;
+            FArgs f{};
+            f.acc = a.acc;
+            f.hist = a.hist;
+            f.earliest = g->d_earliest;
+            f.ub = g->d_ub;
+            f.E = g->h.E;
+            f.stats_fixed = sp.fixed;
+            f.tick_q = sp.q;
+            f.bin_w = sp.bin_w;
+            f.n = B->n[i];
+            for (int k = 0; k < 5; ++k) {
+                double *o = B->out + (size_t)k * E + (size_t)B->ev_off[i];
+                (k == 0 ? f.mean : k == 1 ? f.p50 : k == 2 ? f.p90 : k == 3 ? f.p99 : f.p_on_time) = o;
+            }
+            fa[i] = f;
+        }
+        cuda_check(cudaMemcpy(d_args, ka.data(), ka.size() * sizeof(KArgs), cudaMemcpyHostToDevice), "upload");
+        cuda_check(cudaMemcpy(B->d_fargs, fa.data(), fa.size() * sizeof(FArgs), cudaMemcpyHostToDevice), "upload");
+        cuda_check(cudaMemcpy(d_items, items.data(), items.size() * 4, cudaMemcpyHostToDevice), "upload");
+        B->args.dags = d_args;
+        B->args.items = d_items;
+        B->args.n_items = (int32_t)B->n_items;
+        B->args.counter = counter;
+        B->args.scratch = scratch;
+        B->args.scratch_stride = (int64_t)max_E_global * kTile;
+        *out = B;
+    });
+    if (rc != MCD_OK && B) {
+        std::string keep = mcd_last_error();
+        mcd_batch_destroy(B);
+        set_last_error(keep);
+    }
+    return rc;
+}
+
+void mcd_batch_destroy(mcd_batch *B) {
+    if (!B) return;
+    cudaSetDevice(B->device);
+    if (B->stream) cudaStreamSynchronize(B->stream);
+    if (B->exec) cudaGraphExecDestroy(B->exec);
+    if (B->graph) cudaGraphDestroy(B->graph);
+    if (B->stream) cudaStreamDestroy(B->stream);
+    if (B->dmem) cudaFree(B->dmem);
+    delete B;
+}
+
+int mcd_batch_run(mcd_batch *B) {
+    return guarded([&] {
+        if (!B) throw McdError(MCD_ERR_INVALID, "null batch");
+        cuda_check(cudaSetDevice(B->device), "cudaSetDevice");
+        if (!B->exec) {
+            cuda_check(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+            cudaError_t e = cudaMemsetAsync(B->dmem, 0, B->zero_bytes, B->stream);
+            if (e == cudaSuccess) e = launch_batch_stats(B->args, B->n_warps, B->smem, B->grid, B->stream);
+            if (e == cudaSuccess)
+                e = launch_batch_finish(B->d_fargs, (int32_t)B->dags.size(), B->max_E, B->stream);
+            cudaGraph_t graph = nullptr;
+            const cudaError_t e2 = cudaStreamEndCapture(B->stream, &graph);
+            cuda_check(e, "batch capture");
+            cuda_check(e2, "graph capture end");
+            B->graph = graph;
+            cuda_check(cudaGraphInstantiate(&B->exec, B->graph, 0), "graph instantiate");
+        }
+        cuda_check(cudaGraphLaunch(B->exec, B->stream), "graph launch");
+    });
+}
+
+int mcd_batch_sync(mcd_batch *B) {
+    return guarded([&] {
+        if (!B) throw McdError(MCD_ERR_INVALID, "null batch");
+        cuda_check(cudaSetDevice(B->device), "cudaSetDevice");
+        cuda_check(cudaStreamSynchronize(B->stream), "batch sync");
+        for (mcd_dag *g : B->dags) check_device_error(g);
+    });
+}
+
+void *mcd_batch_stream(const mcd_batch *B) { return B ? (void *)B->stream : nullptr; }
+int64_t mcd_batch_items(const mcd_batch *B) { return B ? B->n_items : -1; }
+int32_t mcd_batch_grid(const mcd_batch *B) { return B ? B->grid : -1; }
+
+int mcd_batch_download(mcd_batch *B, int32_t i, const mcd_stats *host) {
+    return guarded([&] {
+        if (!B || !host || i < 0 || i >= (int32_t)B->dags.size()) throw McdError(MCD_ERR_INVALID, "bad arguments");
+        cuda_check(cudaSetDevice(B->device), "cudaSetDevice");
+        cuda_check(cudaStreamSynchronize(B->stream), "batch sync");
+        const size_t E = (size_t)B->total_E, e0 = (size_t)B->ev_off[i], ne = (size_t)B->dags[i]->h.E;
+        double *dst[5] = {host->mean, host->p50, host->p90, host->p99, host->p_on_time};
+        for (int k = 0; k < 5; ++k)
+            if (dst[k])
+                cuda_check(cudaMemcpy(dst[k], B->out + k * E + e0, ne * 8, cudaMemcpyDeviceToHost), "download");
+        if (host->hist)
+            cuda_check(cudaMemcpy(host->hist, B->hist + e0 * kHistStride, ne * kHistStride * 4,
+                                  cudaMemcpyDeviceToHost),
+                       "download");
+    });
+}
+
+}  // extern "C"

@@ -11,7 +11,7 @@
 #include <cstring>
 #include <string>
 
-#include "mcd_host.hpp"
+#include "mcd_handle.hpp"
 
 namespace mcd {
 cudaError_t launch_propagate(const KArgs &a, bool given, bool win_smem, bool stats, cudaStream_t st);
@@ -25,33 +25,11 @@ cudaError_t launch_transpose_i32(const int32_t *in, int64_t ld_in, int32_t *out,
 
 using namespace mcd;
 
-struct mcd_dag {
-    int device = 0;
-    cudaStream_t stream[2] = {nullptr, nullptr};
-    HostDag h;
-    char *dmem = nullptr;
-    size_t dbytes = 0;
-    EvRec *d_ev = nullptr;
-    PredRec *d_pred = nullptr;
-    LinkRec *d_aux = nullptr;
-    DistParam *d_dist = nullptr;
-    AliasEntry *d_alias = nullptr;
-    int32_t *d_wk = nullptr;
-    double *d_earliest = nullptr;  // caller order, for the statistics finish
-    double *d_ub = nullptr;
-    int32_t *d_err = nullptr;
-    char *ws = nullptr;  // workspace
-    size_t ws_bytes = 0;
-};
-
-namespace {
+namespace mcd {
 
 thread_local std::string g_last_error;
 
-int fail(int code, const std::string &msg) {
-    g_last_error = msg;
-    return code;
-}
+void set_last_error(const std::string &msg) { g_last_error = msg; }
 
 void cuda_check(cudaError_t e, const char *what) {
     if (e != cudaSuccess) {
@@ -60,23 +38,6 @@ void cuda_check(cudaError_t e, const char *what) {
         throw McdError(MCD_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
     }
 }
-
-template <typename F>
-int guarded(F &&f) {
-    try {
-        f();
-        g_last_error.clear();
-        return MCD_OK;
-    } catch (const McdError &e) {
-        return fail(e.code, e.what());
-    } catch (const std::bad_alloc &) {
-        return fail(MCD_ERR_NOMEM, "host allocation failed");
-    } catch (const std::exception &e) {
-        return fail(MCD_ERR_RUNTIME, e.what());
-    }
-}
-
-size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 void ensure_ws(mcd_dag *g, size_t bytes) {
     if (bytes <= g->ws_bytes) return;
@@ -97,10 +58,22 @@ KArgs base_args(const mcd_dag *g) {
     a.dist = g->d_dist;
     a.alias = g->d_alias;
     a.wk_off = g->d_wk;
-    a.n_levels = g->h.n_levels;
+    a.stage_meta = g->d_stage_meta;
+    a.n_stages = g->h.n_stages;
     a.n_warps = g->h.n_warps;
     a.n_aux = (int32_t)g->h.aux.size();
     a.window_slots = g->h.window_slots;
+    a.n_dist = (int32_t)g->h.dist.size();
+    a.n_alias = (int32_t)g->h.alias.size();
+    a.tables_in_smem = g->h.tables_in_smem ? 1 : 0;
+    a.win_smem = g->h.win_smem ? 1 : 0;
+    a.positive = g->h.positive ? 1 : 0;
+    a.stage_bytes = g->h.stage_bytes;
+    a.stage_pred_off = g->h.stage_pred_off;
+    a.smem_stage_off = g->h.smem_stage_off;
+    a.smem_tables_off = g->h.smem_tables_off;
+    a.smem_bar_off = g->h.smem_bar_off;
+    a.smem_total = g->h.smem_total;
     a.err = g->d_err;
     return a;
 }
@@ -119,6 +92,10 @@ void check_device_error(mcd_dag *g) {
         throw McdError(MCD_ERR_DEVICE, "kernel reported error flags " + std::to_string(flags));
     }
 }
+
+}  // namespace mcd
+
+namespace {
 
 // Samples per chunk for the host-buffer entry points: two chunk buffer sets
 // (sample-minor rows + sample-major rows) within ~2 GiB, a multiple of 32.
@@ -167,7 +144,7 @@ void carve(mcd_dag *g, int64_t C, ChunkBufs cb[2]) {
 
 extern "C" {
 
-const char *mcd_last_error(void) { return g_last_error.c_str(); }
+const char *mcd_last_error(void) { return mcd::g_last_error.c_str(); }
 int mcd_abi_version(void) { return MCD_ABI_VERSION; }
 
 int mcd_generator_create(mcd_generator **out) {
@@ -225,12 +202,19 @@ int mcd_generator_add_empirical_relative(mcd_generator *g, int32_t t, const doub
 }
 
 int mcd_dag_create(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag **out) {
+    return mcd_dag_create_ex(desc, gen, nullptr, out);
+}
+
+int mcd_dag_create_ex(const mcd_dag_desc *desc, const mcd_generator *gen, const mcd_dag_options *opts,
+                      mcd_dag **out) {
     mcd_dag *g = nullptr;
     int rc = guarded([&] {
         if (!desc || !gen || !out) throw McdError(MCD_ERR_INVALID, "null argument");
         *out = nullptr;
+        const int32_t nw = opts ? opts->n_warps : 0;
+        if (nw < 0 || nw > kMaxWarps) throw McdError(MCD_ERR_INVALID, "n_warps must be 0 (automatic) or 1..24");
         g = new mcd_dag();
-        compile_dag(*desc, *gen, g->h);
+        compile_dag(*desc, *gen, g->h, nw);
         cuda_check(cudaGetDevice(&g->device), "cudaGetDevice");
         for (int k = 0; k < 2; ++k)
             cuda_check(cudaStreamCreateWithFlags(&g->stream[k], cudaStreamNonBlocking), "stream create");
@@ -241,8 +225,9 @@ int mcd_dag_create(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag *
                      s_dist = align_up(h.dist.size() * sizeof(DistParam), 256),
                      s_alias = align_up(h.alias.size() * sizeof(AliasEntry), 256),
                      s_wk = align_up(h.wk_off.size() * sizeof(int32_t), 256),
+                     s_meta = align_up(h.stage_meta.size() * sizeof(int32_t), 256),
                      s_times = align_up(h.earliest.size() * sizeof(double), 256), s_err = 256;
-        g->dbytes = s_ev + s_pred + s_aux + s_dist + s_alias + s_wk + 2 * s_times + s_err;
+        g->dbytes = s_ev + s_pred + s_aux + s_dist + s_alias + s_wk + s_meta + 2 * s_times + s_err;
         cuda_check(cudaMalloc(&g->dmem, g->dbytes), "compiled DAG allocation");
         char *p = g->dmem;
         auto place = [&](auto *&dst, const auto &vec, size_t sz) {
@@ -258,6 +243,7 @@ int mcd_dag_create(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag *
         place(g->d_dist, h.dist, s_dist);
         place(g->d_alias, h.alias, s_alias);
         place(g->d_wk, h.wk_off, s_wk);
+        place(g->d_stage_meta, h.stage_meta, s_meta);
         place(g->d_earliest, h.earliest, s_times);
         place(g->d_ub, h.ub, s_times);
         g->d_err = reinterpret_cast<int32_t *>(p);
@@ -265,9 +251,9 @@ int mcd_dag_create(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag *
         *out = g;
     });
     if (rc != MCD_OK && g) {
-        std::string keep = g_last_error;
+        std::string keep = mcd::g_last_error;
         mcd_dag_destroy(g);
-        g_last_error = keep;
+        mcd::g_last_error = keep;
     }
     return rc;
 }
@@ -292,19 +278,38 @@ int32_t mcd_dag_node_count(const mcd_dag *g) { return g ? g->h.E : -1; }
 int32_t mcd_dag_activity_count(const mcd_dag *g) { return g ? g->h.L : -1; }
 void *mcd_dag_stream(const mcd_dag *g) { return g ? (void *)g->stream[0] : nullptr; }
 
+static void fill_info(const HostDag &h, mcd_dag_info *info) {
+    info->n_events = h.E;
+    info->n_links = h.L;
+    info->n_levels = h.n_levels;
+    info->n_warps = h.n_warps;
+    info->n_preds = (int64_t)h.pred.size();
+    info->window_slots = h.window_slots;
+    info->window_in_smem = h.win_smem ? 1 : 0;
+    info->n_orphan_links = h.n_orphan;
+    info->n_stages = h.n_stages;
+    info->smem_bytes = h.smem_total;
+    info->positive = h.positive ? 1 : 0;
+    info->tables_in_smem = h.tables_in_smem ? 1 : 0;
+}
+
 int mcd_dag_get_info(const mcd_dag *g, mcd_dag_info *info) {
     return guarded([&] {
         if (!g || !info) throw McdError(MCD_ERR_INVALID, "null argument");
-        info->n_events = g->h.E;
-        info->n_links = g->h.L;
-        info->n_levels = g->h.n_levels;
-        info->n_warps = g->h.n_warps;
-        info->n_preds = (int64_t)g->h.pred.size();
-        info->window_slots = g->h.window_slots;
-        info->window_in_smem = g->h.win_smem ? 1 : 0;
-        info->n_orphan_links = g->h.n_orphan;
+        fill_info(g->h, info);
         info->device = g->device;
         info->device_bytes = (int64_t)g->dbytes;
+    });
+}
+
+int mcd_dag_describe(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag_info *info) {
+    return guarded([&] {
+        if (!desc || !gen || !info) throw McdError(MCD_ERR_INVALID, "null argument");
+        HostDag h;
+        compile_dag(*desc, *gen, h, 0);
+        fill_info(h, info);
+        info->device = -1;
+        info->device_bytes = -1;
     });
 }
 

@@ -96,7 +96,7 @@ static void check_table(const DistSpec &d) {
     if (!(sum > 0.0)) throw McdError(MCD_ERR_INVALID, "empirical weights must not all be zero");
 }
 
-void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H) {
+void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int32_t n_warps) {
     // ---- 1) distributions: the last add_* per type wins (README semantics of dist_map_)
     std::unordered_map<int32_t, size_t> type_spec;
     for (size_t i = 0; i < g.dists.size(); ++i) type_spec[g.dists[i].type] = i;
@@ -307,43 +307,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H) {
         for (int32_t e = 0; e < E; ++e) by_level[(size_t)fill[(size_t)level[e]]++] = e;
     }
 
-    // ---- 7) warps per CTA and per-(level, warp) chunks balanced by edge count
-    int32_t nw = 1;
-    if (n_levels > 0) {
-        const double avg_width = (double)E / (double)n_levels;
-        nw = (int32_t)std::ceil(avg_width / 6.0);
-    }
-    if (const char *env = std::getenv("MCD_WARPS")) nw = std::atoi(env);
-    nw = std::max(1, std::min(16, nw));
-    H.n_warps = nw;
-    H.wk_off.assign((size_t)n_levels * nw + 1, 0);
-    std::vector<int32_t> order;  // compiled order
-    order.reserve((size_t)E);
-    for (int32_t l = 0; l < n_levels; ++l) {
-        const int32_t b = lvl_off[l], e = lvl_off[l + 1];
-        double total = 0.0;
-        for (int32_t i = b; i < e; ++i) total += 1.0 + (double)tlen[by_level[i]];
-        double acc = 0.0;
-        int32_t w = 0;
-        H.wk_off[(size_t)l * nw] = (int32_t)order.size();
-        for (int32_t i = b; i < e; ++i) {
-            const double c = 1.0 + (double)tlen[by_level[i]];
-            // start the next warp's chunk once this one holds its share
-            while (w + 1 < nw && acc + 0.5 * c > total * (double)(w + 1) / (double)nw) {
-                ++w;
-                H.wk_off[(size_t)l * nw + w] = (int32_t)order.size();
-            }
-            order.push_back(by_level[i]);
-            acc += c;
-        }
-        while (w + 1 < nw) {
-            ++w;
-            H.wk_off[(size_t)l * nw + w] = (int32_t)order.size();
-        }
-    }
-    H.wk_off[(size_t)n_levels * nw] = (int32_t)order.size();
-
-    // ---- 8) window slots: linear scan over levels, a slot is free again after
+    // ---- 7) window slots: linear scan over levels, a slot is free again after
     // the last level that reads its event
     std::vector<int32_t> slot((size_t)E, -1);
     {
@@ -368,8 +332,130 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H) {
         }
         H.window_slots = n_slots;
     }
+
+    // ---- 8) warps per CTA; work cost of an event for balancing the warps
+    int32_t nw = 1;
+    if (n_levels > 0) {
+        const double avg_width = (double)E / (double)n_levels;
+        nw = (int32_t)std::ceil(avg_width / 6.0);
+    }
+    if (const char *env = std::getenv("MCD_WARPS")) nw = std::atoi(env);
+    if (n_warps > 0) nw = n_warps;
+    nw = std::max(1, std::min(kMaxWarps, nw));
+    H.n_warps = nw;
+    auto kind_cost = [&](int32_t l) -> double {
+        if (l >= L) return 1.0;
+        switch (H.link_kd[l] & KD_KIND_MASK) {
+            case K_FIXED: return 1.0;
+            case K_EXP: return 5.0;
+            case K_GAMMA: return 12.0;
+            default: return 4.0;
+        }
+    };
+    std::vector<double> cost((size_t)E, 2.0);
+    for (int32_t e = 0; e < E; ++e)
+        for (int64_t k = 0; k < tlen[e]; ++k) cost[e] += kind_cost(d.pred_act[tstart[e] + k]);
+
+    // ---- 9) shared-memory budget: window rows, two record staging buffers
+    // (each stage's event and predecessor records), distribution tables
+    const size_t table_bytes = H.dist.size() * sizeof(DistParam) + H.alias.size() * sizeof(AliasEntry);
+    H.tables_in_smem = table_bytes <= kMaxTableBytes;
+    const size_t fixed_bytes = (H.tables_in_smem ? table_bytes : 0) + 3 * 128;
     const size_t win_bytes = (size_t)H.window_slots * kTile * sizeof(double);
-    H.win_smem = win_bytes <= kMaxWindowBytes && std::getenv("MCD_NO_SMEM_WINDOW") == nullptr;
+    H.win_smem = win_bytes <= kMaxWindowBytes && win_bytes + fixed_bytes + 2 * kMinStageBytes <= kSmemMax &&
+                 std::getenv("MCD_NO_SMEM_WINDOW") == nullptr;
+    const size_t avail = kSmemMax - fixed_bytes - (H.win_smem ? win_bytes : 0);
+    size_t budget = std::min(kMaxStageBytes, avail / 2);
+
+    // ---- 10) stages (a level, or a slice of a wide level that fits a buffer)
+    // and per-(stage, warp) chunks balanced by cost
+    std::vector<int32_t> order;
+    std::vector<int32_t> meta;  // ev_first, n_ev (negated: unstaged), n_pred
+    std::vector<int32_t> wk;
+    for (;;) {
+        order.clear();
+        meta.clear();
+        wk.clear();
+        size_t max_ev = 0, max_pred = 0;
+        for (int32_t l = 0; l < n_levels; ++l) {
+            int32_t i = lvl_off[l];
+            while (i < lvl_off[l + 1]) {
+                // one stage: events i .. j-1 of this level
+                int32_t j = i;
+                size_t bytes = 0, nev = 0, npred = 0;
+                while (j < lvl_off[l + 1]) {
+                    const size_t add = sizeof(EvRec) + (size_t)tlen[by_level[j]] * sizeof(PredRec);
+                    if (j > i && bytes + add > budget) break;
+                    bytes += add;
+                    nev += 1;
+                    npred += (size_t)tlen[by_level[j]];
+                    ++j;
+                }
+                const bool staged = bytes <= budget;
+                if (staged) {
+                    max_ev = std::max(max_ev, nev);
+                    max_pred = std::max(max_pred, npred);
+                }
+                double total = 0.0;
+                for (int32_t k = i; k < j; ++k) total += cost[by_level[k]];
+                const int32_t first = (int32_t)order.size();
+                double acc = 0.0;
+                int32_t w = 0;
+                wk.push_back(first);
+                for (int32_t k = i; k < j; ++k) {
+                    const double c = cost[by_level[k]];
+                    while (w + 1 < nw && acc + 0.5 * c > total * (double)(w + 1) / (double)nw) {
+                        ++w;
+                        wk.push_back((int32_t)order.size());
+                    }
+                    order.push_back(by_level[k]);
+                    acc += c;
+                }
+                while (w + 1 < nw) {
+                    ++w;
+                    wk.push_back((int32_t)order.size());
+                }
+                meta.push_back(first);
+                meta.push_back(staged ? (int32_t)nev : -(int32_t)nev);
+                meta.push_back((int32_t)npred);
+                i = j;
+            }
+        }
+        wk.push_back((int32_t)order.size());
+        H.stage_pred_off = (int32_t)((max_ev * sizeof(EvRec) + 15) / 16 * 16);
+        H.stage_bytes = (int32_t)((H.stage_pred_off + max_pred * sizeof(PredRec) + 127) / 128 * 128);
+        if (2 * (size_t)H.stage_bytes <= avail || budget <= kMinStageBytes) break;
+        budget = std::max(kMinStageBytes, budget * 3 / 4);
+    }
+    H.n_stages = (int32_t)(meta.size() / 3);
+    H.wk_off = wk;
+    // stage_meta with predecessor offsets (records are laid out in compiled order)
+    H.stage_meta.assign((size_t)H.n_stages * 4, 0);
+    {
+        int64_t pos = 0;
+        for (int32_t st = 0; st < H.n_stages; ++st) {
+            H.stage_meta[(size_t)st * 4 + 0] = meta[(size_t)st * 3 + 0];
+            H.stage_meta[(size_t)st * 4 + 1] = meta[(size_t)st * 3 + 1];
+            H.stage_meta[(size_t)st * 4 + 2] = (int32_t)pos;
+            H.stage_meta[(size_t)st * 4 + 3] = meta[(size_t)st * 3 + 2];
+            pos += meta[(size_t)st * 3 + 2];
+        }
+    }
+    // layout: [window][stage buffer 0][stage buffer 1][tables][2 mbarriers]
+    {
+        size_t off = H.win_smem ? win_bytes : 0;
+        off = (off + 127) / 128 * 128;
+        H.smem_stage_off = (int32_t)off;
+        off += 2 * (size_t)H.stage_bytes;
+        off = (off + 127) / 128 * 128;
+        H.smem_tables_off = (int32_t)off;
+        if (H.tables_in_smem) off += table_bytes;
+        off = (off + 15) / 16 * 16;
+        H.smem_bar_off = (int32_t)off;
+        off += 16;
+        H.smem_total = (int32_t)off;
+        if (off > kSmemMax) throw McdError(MCD_ERR_INVALID, "compiled DAG does not fit the shared-memory budget");
+    }
 
     // ---- 9) records in compiled order
     H.ev.resize((size_t)E);
@@ -418,7 +504,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H) {
                 p.link = l;
                 p.kd = H.link_kd[l];
                 p.v = H.link_v[l];
-                if ((p.kd & KD_KIND_MASK) != K_FIXED && !written[l]) {
+                if (!written[l]) {  // the first reference stores the link's duration row
                     p.kd |= KD_WRITE;
                     written[l] = 1;
                 }
@@ -428,6 +514,17 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H) {
         }
         r.pred_end = (int32_t)H.pred.size();
         H.ev[i] = r;
+    }
+    // ---- 12) positive mode: every earliest, bound and duration is a non-negative
+    // finite double, so t = src + dur never is NaN or negative and the raw bit
+    // patterns order like the values
+    {
+        auto nonneg = [](double x) { return std::isfinite(x) && !std::signbit(x); };
+        bool pos = nonneg(d.max_delay);
+        for (int32_t e = 0; pos && e < E; ++e) pos = nonneg(d.earliest[e]) && nonneg(H.ub[e]);
+        for (int32_t l = 0; pos && l < L; ++l) pos = nonneg(H.link_v[l]) && H.link_v[l] < 1e300;
+        for (const AliasEntry &ae : H.alias) pos = pos && nonneg(ae.v_self) && nonneg(ae.v_alias) && ae.v_self < 1e300;
+        H.positive = pos;
     }
     H.aux.clear();
     H.n_orphan = 0;

@@ -163,13 +163,14 @@ struct FlatDag {
 
 class Propagator {
    public:
-    Propagator(const FlatDag &f, const Generator &gen) {
+    Propagator(const FlatDag &f, const Generator &gen, int n_warps = 0) {
         mcd_dag *p = nullptr;
         const mcd_dag_desc d = f.desc();
+        const mcd_dag_options opts{n_warps};
         int rc;
         {
             py::gil_scoped_release release;
-            rc = mcd_dag_create(&d, gen.g.get(), &p);
+            rc = mcd_dag_create_ex(&d, gen.g.get(), &opts, &p);
         }
         raise_status(rc);
         dag_.reset(p, mcd_dag_destroy);
@@ -321,6 +322,10 @@ class Propagator {
         d["n_orphan_links"] = i.n_orphan_links;
         d["device"] = i.device;
         d["device_bytes"] = i.device_bytes;
+        d["n_stages"] = i.n_stages;
+        d["smem_bytes"] = i.smem_bytes;
+        d["positive"] = (bool)i.positive;
+        d["tables_in_smem"] = (bool)i.tables_in_smem;
         return d;
     }
     mcd_dag *handle() const { return dag_.get(); }
@@ -337,6 +342,73 @@ static std::vector<T> to_vec(py::handle h) {
     if (a.ndim() != 1) throw py::value_error("expected a 1-D array");
     return std::vector<T>(a.data(), a.data() + a.size());
 }
+
+// Many propagators, each with its own samples, in one persistent launch.
+class Batch {
+   public:
+    Batch(const std::vector<Propagator *> &props, const std::vector<int64_t> &seed0, const std::vector<int64_t> &n)
+        : props_(props) {
+        if (props.empty() || seed0.size() != props.size() || n.size() != props.size())
+            throw py::value_error("need one seed0 and one sample count per propagator");
+        std::vector<mcd_dag *> h;
+        for (Propagator *p : props) {
+            if (!p) throw py::value_error("null propagator");
+            h.push_back(p->handle());
+            keep_.push_back(py::cast(p));
+        }
+        mcd_batch *b = nullptr;
+        raise_status(mcd_batch_create(h.data(), (int32_t)h.size(), seed0.data(), n.data(), &b));
+        b_.reset(b, mcd_batch_destroy);
+    }
+    void run(bool wait) {
+        int rc;
+        {
+            py::gil_scoped_release release;
+            rc = mcd_batch_run(b_.get());
+            if (rc == MCD_OK && wait) rc = mcd_batch_sync(b_.get());
+        }
+        raise_status(rc);
+    }
+    void sync() {
+        int rc;
+        {
+            py::gil_scoped_release release;
+            rc = mcd_batch_sync(b_.get());
+        }
+        raise_status(rc);
+    }
+    py::dict stats(int i, bool hist) {
+        if (i < 0 || i >= (int)props_.size()) throw py::index_error("batch index out of range");
+        const int64_t E = props_[i]->node_count();
+        py::array_t<double> mean(E), p50(E), p90(E), p99(E), pot(E);
+        py::object h = py::none();
+        uint32_t *hp = nullptr;
+        if (hist) {
+            py::array_t<uint32_t> ha({E, (int64_t)MCD_HIST_STRIDE});
+            hp = ha.mutable_data();
+            h = ha;
+        }
+        mcd_stats st{mean.mutable_data(), p50.mutable_data(), p90.mutable_data(), p99.mutable_data(),
+                     pot.mutable_data(), hp};
+        raise_status(mcd_batch_download(b_.get(), i, &st));
+        py::dict d;
+        d["mean"] = mean;
+        d["p50"] = p50;
+        d["p90"] = p90;
+        d["p99"] = p99;
+        d["p_on_time"] = pot;
+        d["hist"] = h;
+        return d;
+    }
+    int64_t items() const { return mcd_batch_items(b_.get()); }
+    int grid() const { return mcd_batch_grid(b_.get()); }
+    uintptr_t stream() const { return (uintptr_t)mcd_batch_stream(b_.get()); }
+
+   private:
+    std::vector<Propagator *> props_;
+    std::vector<py::object> keep_;  // the propagators outlive the batch
+    std::shared_ptr<mcd_batch> b_;
+};
 
 }  // namespace mcd_py
 
@@ -488,7 +560,7 @@ PYBIND11_MODULE(_core, m) {
             "from_arrays",
             [](py::handle earliest, py::handle act_idx, py::handle act_duration, py::handle act_type,
                py::handle target, py::handle pred_offsets, py::handle pred_src, py::handle pred_act,
-               double max_delay, const Generator &g) {
+               double max_delay, const Generator &g, int n_warps) {
                 FlatDag f;
                 f.earliest = to_vec<double>(earliest);
                 f.act_idx = to_vec<int32_t>(act_idx);
@@ -504,11 +576,12 @@ PYBIND11_MODULE(_core, m) {
                 if (f.pred_offsets.size() != f.target.size() + 1 || f.pred_offsets.front() != 0 ||
                     f.pred_offsets.back() != (int64_t)f.pred_src.size() || f.pred_src.size() != f.pred_act.size())
                     throw py::value_error("inconsistent precedence arrays");
-                return new Propagator(f, g);
+                return new Propagator(f, g, n_warps);
             },
             py::arg("earliest"), py::arg("act_idx"), py::arg("act_duration"), py::arg("act_type"), py::arg("target"),
             py::arg("pred_offsets"), py::arg("pred_src"), py::arg("pred_act"), py::arg("max_delay"),
-            py::arg("generator"), "Construct from a DagContext in flat-array form")
+            py::arg("generator"), py::arg("n_warps") = 0,
+            "Construct from a DagContext in flat-array form (n_warps: warps per CTA, 0 = automatic)")
         .def("node_count", &Propagator::node_count, "Number of events")
         .def("activity_count", &Propagator::activity_count, "Number of links")
         .def("run", &Propagator::run, py::arg("seed"), "Run single sim")
@@ -523,4 +596,17 @@ PYBIND11_MODULE(_core, m) {
              "dict of mean, p50, p90, p99, p_on_time (and the raw histogram when hist=True)")
         .def("info", &Propagator::info, "Compiled-DAG facts")
         .def("_handle", [](const Propagator &p) { return (uintptr_t)p.handle(); });
+
+    py::class_<Batch>(m, "Batch")
+        .def(py::init<const std::vector<Propagator *> &, const std::vector<int64_t> &,
+                      const std::vector<int64_t> &>(),
+             py::arg("propagators"), py::arg("seed0"), py::arg("n_samples"),
+             "Many propagators (compiled with the same n_warps), each with its own samples "
+             "(seeds seed0[i]..seed0[i]+n_samples[i]-1), run as one persistent launch")
+        .def("run", &Batch::run, py::arg("wait") = true, "Run the batch (one CUDA graph launch)")
+        .def("sync", &Batch::sync, "Wait for the last run and report kernel errors")
+        .def("stats", &Batch::stats, py::arg("i"), py::arg("hist") = false, "Statistics of propagator i")
+        .def_property_readonly("items", &Batch::items, "Work items (DAG, 32-sample tile)")
+        .def_property_readonly("grid", &Batch::grid, "CTAs of the persistent launch")
+        .def_property_readonly("stream", &Batch::stream, "The batch's CUDA stream");
 }

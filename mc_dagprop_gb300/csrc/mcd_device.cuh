@@ -1,0 +1,447 @@
+// mcd_device.cuh -- device code of the Monte Carlo DAG-propagation path (sm_103a).
+//
+// k_propagate: one CTA owns a tile of 32 samples (one per lane) and walks the
+// whole compiled DAG stage by stage (a stage is a level, or a slice of a wide
+// level); the warps of the CTA split each stage's events and meet at a barrier
+// between stages.  The records of the next stage are copied into shared memory
+// by the TMA bulk-copy engine (cp.async.bulk + mbarrier, double-buffered) while
+// the current one is processed, so no warp waits on L2 for DAG records.
+// Realized times of events that later stages still read live in a shared-memory
+// "window" (slot-major, one 256-byte row of 32 samples per live event), so
+// predecessor reads never touch HBM; every output row is written once,
+// coalesced (256 B per warp store).
+//
+// FP64 throughput on this part is ~1.6 ops/clk/SM (measured), against ~108 for
+// 32-bit integer logic, so FP64 is spent only where bit-exactness needs it: the
+// one IEEE add per edge of the reference's loop (_core.cpp:341).  Comparisons
+// run on 64-bit integer order keys that order doubles like the IEEE operators;
+// sampled durations base * (1 + X) are formed with integer mantissa products.
+//
+// Delays come from Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random
+// numbers: as easy as 1, 2, 3", SC'11) in counter mode: the counter holds the
+// sample's 64-bit seed, the link and the attempt.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "mcd_internal.hpp"
+
+namespace mcd {
+
+// ---------------------------------------------------------------- Philox4x32-10
+// Counter mode under one fixed key: the 128-bit counter is (seed low, seed high,
+// link, salt ^ attempt), so a draw depends only on (sample seed, link, attempt)
+// and the ten round keys are compile-time constants (no key registers, no key
+// schedule arithmetic in the loop).
+struct U4 {
+    uint32_t x, y, z, w;
+};
+
+constexpr uint32_t kPhiloxM0 = 0xD2511F53u, kPhiloxM1 = 0xCD9E8D57u;
+constexpr uint32_t kPhiloxW0 = 0x9E3779B9u, kPhiloxW1 = 0xBB67AE85u;
+constexpr uint32_t kKey0 = 0x243F6A88u, kKey1 = 0x85A308D3u;  // fixed key (hex digits of pi)
+constexpr uint32_t kStreamSalt = 0x6D636470u;               // counter word 3: separates this stream's use
+
+__device__ __forceinline__ U4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)kPhiloxM0 * c0;  // one wide multiply: hi and lo words
+        const uint64_t p1 = (uint64_t)kPhiloxM1 * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ (kKey0 + (uint32_t)r * kPhiloxW0);
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ (kKey1 + (uint32_t)r * kPhiloxW1);
+        c1 = (uint32_t)p1;
+        c3 = (uint32_t)p0;
+        c0 = n0;
+        c2 = n2;
+    }
+    return U4{c0, c1, c2, c3};
+}
+
+// The draw for (sample seed, link, attempt, sel): sel separates the calls one
+// attempt may make.
+__device__ __forceinline__ U4 draw_words(uint64_t seed, uint32_t link, uint32_t attempt, uint32_t sel) {
+    return philox((uint32_t)seed, (uint32_t)(seed >> 32), link, kStreamSalt ^ ((attempt << 1) | sel));
+}
+
+// Uniform in (0, 1]: (r + 1/2) / 2^32 rounded to float.
+__device__ __forceinline__ float u01_open0(uint32_t r) {
+    return fmaf(__uint2float_rn(r), 2.3283064365386963e-10f, 1.1641532182693481e-10f);
+}
+
+// ---------------------------------------------------------------- order keys
+// Signed 64-bit key with key(a) < key(b) <=> a < b for non-NaN doubles, and
+// key(-0) == key(+0) as the IEEE comparison has it.  NaN maps to INT64_MIN so
+// that `ub < t` and `t >= latest` are both false for a NaN t, as in C++.
+// POSITIVE: every time of the DAG is a non-negative finite double (checked by
+// the host), for which the bit pattern itself is the key.
+template <bool POSITIVE>
+__device__ __forceinline__ long long order_key(long long b) {
+    if (POSITIVE) return b;
+    const long long mag = b & 0x7FFFFFFFFFFFFFFFll;
+    const long long k = b < 0 ? -mag : mag;
+    return mag > 0x7FF0000000000000ll ? (long long)0x8000000000000000ull : k;
+}
+
+// ---------------------------------------------------------------- integer FP64 helpers
+constexpr unsigned long long kMant = 0xFFFFFFFFFFFFFull, kHidden = 1ull << 52;
+
+// Bits of the double 1 + x for a float x >= 0.  Exact when x >= 2^-29 (the
+// float's 24 significant bits then fit the double's fraction); smaller x are
+// truncated to 2^-52.  x >= 1 goes through the float sum 1 + x.
+__device__ __forceinline__ long long one_plus(float x) {
+    const uint32_t b = __float_as_uint(x);
+    const int e = (int)((b >> 23) & 0xFF);
+    if (e == 0) return 0x3FF0000000000000ll;  // zero (or subnormal): 1.0
+    if (e < 127) {
+        const unsigned long long m = (b & 0x7FFFFFu) | 0x800000u;
+        const int sh = e - 98;  // m * 2^(e-150) * 2^52
+        const unsigned long long frac = sh >= 0 ? (m << sh) : (sh > -24 ? (m >> -sh) : 0ull);
+        return (long long)(0x3FF0000000000000ull | frac);
+    }
+    const uint32_t f = __float_as_uint(1.0f + x);  // x >= 1: 1 + x in float
+    const unsigned long long fe = (f >> 23) & 0xFF;
+    return (long long)(((fe + 896ull) << 52) | ((unsigned long long)(f & 0x7FFFFFu) << 29));
+}
+
+// a * g for a double a and a positive normal double g, truncated toward zero,
+// from the top 53 bits of the 106-bit mantissa product; other operands, or a
+// result out of the normal range, fall back to the FP64 multiply.
+__device__ __forceinline__ double mul_trunc(double a, long long gb) {
+    const long long ab = __double_as_longlong(a);
+    const int ea = (int)((ab >> 52) & 0x7FF), eg = (int)((gb >> 52) & 0x7FF);
+    int e = ea + eg - 1023;
+    if (gb <= 0 || eg == 0 || eg == 0x7FF || ea == 0 || ea == 0x7FF || e <= 0 || e >= 0x7FE)
+        return a * __longlong_as_double(gb);
+    const unsigned long long ma = ((ab & kMant) | kHidden) << 11, mg = ((gb & kMant) | kHidden) << 11;
+    const unsigned long long hi = __umul64hi(ma, mg);  // = (ma * mg) >> 42, in [2^62, 2^64)
+    unsigned long long m;
+    if (hi >> 63) {
+        m = hi >> 11;
+        e += 1;
+    } else {
+        m = hi >> 10;
+    }
+    return __longlong_as_double((long long)((ab & 0x8000000000000000ll) | ((unsigned long long)e << 52) |
+                                            (m & kMant)));
+}
+
+// ---------------------------------------------------------------- samplers
+// Each returns the link's duration (base + extra) for one sample.
+
+// Exponential with mean lambda_, redrawn above max_scale (_core.cpp:83-89).  The
+// redraw loop is replaced by the inverse CDF of the truncated law, which is the
+// same distribution: X = -lambda_ * log(1 - c u), c = 1 - exp(-max_scale/lambda_).
+__device__ __forceinline__ double draw_exponential(const DistParam &p, double base, uint32_t link, uint64_t seed) {
+    const U4 r = draw_words(seed, link, 0u, 0u);
+    const float w = u01_open0(r.x);       // plays the role of 1 - u
+    const float V = fmaf(p.f1, w, p.f2);  // 1 - c (1 - w), in (1-c, 1]
+    float X = -p.f0 * __logf(V);
+    X = fmaxf(fminf(X, p.f3), 0.0f);
+    return mul_trunc(base, one_plus(X));  // base + X * base
+}
+
+// Gamma(shape, scale) redrawn above max_scale (_core.cpp:98-104), by Marsaglia &
+// Tsang (ACM TOMS 26(3), 2000) in FP32, normals from Box-Muller.  Shapes below 1
+// draw Gamma(shape+1) times U^(1/shape).  Rejection loops are capped; a lane that
+// hits the cap latches ERR_GAMMA_REJECTION and returns the truncation point.
+// Not inlined: it is large, and keeping it out of line keeps the propagation
+// loop's register allocation small.
+static __device__ __noinline__ double draw_gamma(const DistParam &p, double base, uint32_t link, uint64_t seed,
+                                                 int32_t *err) {
+    const float d = p.f0, cc = p.f1;
+    for (uint32_t attempt = 0; attempt < 4096u; ++attempt) {
+        const U4 r = draw_words(seed, link, attempt, 0u);
+        const float rad = __fsqrt_rn(-2.0f * __logf(u01_open0(r.x)));
+        float sn, cs;
+        __sincosf(6.2831853071795865f * ((float)(r.y >> 8) * 5.9604644775390625e-08f), &sn, &cs);
+        float X = -1.0f;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const float z = j == 0 ? rad * cs : rad * sn;
+            const float t = fmaf(cc, z, 1.0f);
+            if (X < 0.0f && t > 0.0f) {
+                const float v = t * t * t;
+                const float u = u01_open0(j == 0 ? r.z : r.w);
+                const float z2 = z * z;
+                if (u < 1.0f - 0.0331f * z2 * z2 || __logf(u) < 0.5f * z2 + d * (1.0f - v + __logf(v))) X = d * v;
+            }
+        }
+        if (X < 0.0f) continue;
+        if (p.boost) {
+            const U4 r2 = draw_words(seed, link, attempt, 1u);
+            X *= exp2f(__log2f(u01_open0(r2.x)) * p.f2);
+        }
+        X *= p.f3;
+        if (X > p.f4) continue;
+        return mul_trunc(base, one_plus(X));
+    }
+    atomicOr(err, ERR_GAMMA_REJECTION);
+    return mul_trunc(base, one_plus(p.f4));
+}
+
+// Empirical tables (_core.cpp:110-141) by Walker/Vose alias sampling: one
+// 32-bit word picks the bin, a second decides bin or alias.  The duration is
+// formed exactly as the reference forms it -- base + value (absolute, :125, 328)
+// or base + factor * base (relative, :140, 328) -- so each bin yields the
+// reference's bit pattern: the values are atoms, and any last-bit difference
+// would separate the two discrete distributions.
+__device__ __forceinline__ double draw_empirical(const DistParam &p, const AliasEntry *alias, double base,
+                                                 bool relative, uint32_t link, uint64_t seed) {
+    const U4 r = draw_words(seed, link, 0u, 0u);
+    const uint32_t j = __umulhi(r.x, (uint32_t)p.tab_n);
+    const AliasEntry &e = alias[p.tab_off + j];
+    const double val = r.y < e.thresh ? e.v_self : e.v_alias;
+    return relative ? __dadd_rn(base, __dmul_rn(val, base)) : __dadd_rn(base, val);
+}
+
+__device__ __forceinline__ double link_duration(int32_t kd, double v, uint32_t link, uint64_t seed,
+                                                const DistParam *dists, const AliasEntry *alias, int32_t *err) {
+    const int kind = kd & KD_KIND_MASK;
+    if (kind == K_FIXED) return v;
+    const DistParam &p = dists[kd >> 8];
+    switch (kind) {
+        case K_EXP: return draw_exponential(p, v, link, seed);
+        case K_GAMMA: return draw_gamma(p, v, link, seed, err);
+        case K_EMP_ABS: return draw_empirical(p, alias, v, false, link, seed);
+        default: return draw_empirical(p, alias, v, true, link, seed);
+    }
+}
+
+// ---------------------------------------------------------------- TMA staging
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Bulk copy global -> shared (16-byte aligned addresses, size a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Issues the copies of one stage's event and predecessor records into a buffer.
+// A stage too large for the buffer (n_ev stored negated) copies nothing; its
+// barrier phase still completes, so the buffers' phases stay in step.
+__device__ __forceinline__ void stage_issue(const KArgs &a, int stage, char *buf, uint64_t *bar) {
+    const int4 m = __ldg(reinterpret_cast<const int4 *>(a.stage_meta) + stage);  // ev_first, n_ev, pred_first, n_pred
+    const bool staged = m.y >= 0;
+    const uint32_t ev_bytes = staged ? (uint32_t)m.y * (uint32_t)sizeof(EvRec) : 0u;
+    const uint32_t pr_bytes = staged ? (uint32_t)m.w * (uint32_t)sizeof(PredRec) : 0u;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(bar, ev_bytes + pr_bytes);
+    if (ev_bytes) bulk_g2s(buf, a.ev + m.x, ev_bytes, bar);
+    if (pr_bytes) bulk_g2s(buf + a.stage_pred_off, a.pred + m.z, pr_bytes, bar);
+}
+
+// Bounded wait for a stage buffer; false (and the error flag latched) if the copy
+// did not land within the limit.
+__device__ __forceinline__ bool stage_wait(uint64_t *bar, uint32_t parity, int32_t *err) {
+    for (uint32_t it = 0; it < (1u << 24); ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    atomicOr(err, ERR_STAGE_TIMEOUT);
+    return false;
+}
+
+// ---------------------------------------------------------------- statistics helpers
+// x * 2^q truncated toward zero, from the bits of a finite double x with
+// |x| * 2^q < 2^62 (the host picks q so that every realized time qualifies).
+__device__ __forceinline__ long long to_ticks(long long b, int q) {
+    const int e = (int)((b >> 52) & 0x7FF);
+    const long long m = (b & 0xFFFFFFFFFFFFFll) | (e ? (1ll << 52) : 0ll);
+    const int sh = (e ? e : 1) - 1075 + q;
+    long long t;
+    if (sh >= 0) t = m << sh;
+    else t = sh > -63 ? (m >> -sh) : 0ll;
+    return b < 0 ? -t : t;
+}
+
+// One event's realized values of the tile into the per-event accumulators:
+// the tile's sum of (realized - earliest) with one 64-bit atomic, and the
+// histogram with one atomic per distinct bin of the warp.
+__device__ __forceinline__ void accumulate_stats(const KArgs &a, const EvRec &ev, long long lbits, bool active,
+                                                 unsigned active_mask) {
+    int bin;
+    if (a.stats_fixed) {
+        const long long te = to_ticks(ev.init_bits, a.tick_q);
+        long long d = active ? to_ticks(lbits, a.tick_q) - te : 0ll;
+        const unsigned long long du = (unsigned long long)(d > 0 ? d : 0ll);
+        bin = (int)__umul64hi(du, a.bin_mul);
+        bin = bin > kHistBins - 1 ? kHistBins - 1 : bin;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xFFFFFFFFu, d, off);
+        if ((threadIdx.x & 31) == 0 && d != 0) atomicAdd(&a.acc[ev.user], (unsigned long long)d);
+    } else {
+        const double dd = active ? __longlong_as_double(lbits) - __longlong_as_double(ev.init_bits) : 0.0;
+        const double x = dd * a.hist_inv_w;
+        bin = x >= (double)(kHistBins - 1) ? kHistBins - 1 : (x > 0.0 ? (int)x : 0);
+        if (active && dd != 0.0) atomicAdd(reinterpret_cast<double *>(&a.acc[ev.user]), dd);
+    }
+    if (lbits == ev.init_bits) bin = kBinLo;
+    else if (lbits == ev.ub_bits) bin = kBinHi;
+    if (active) {
+        const unsigned same = __match_any_sync(active_mask, bin);
+        if ((threadIdx.x & 31) == __ffs(same) - 1)
+            atomicAdd(&a.hist[(int64_t)ev.user * kHistStride + bin], (unsigned)__popc(same));
+    }
+}
+
+// ---------------------------------------------------------------- propagation
+// Walks the compiled DAG for one tile of 32 samples (the tile's sample s is
+// tile * 32 + lane) with all warps of the CTA.
+// GIVEN: durations come from a.dur_in instead of the sampler.
+// WIN_SMEM: predecessor values come from the shared-memory window; otherwise
+// from global realized rows: rows[event * rows_ld + rows_col].
+// STATS: instead of output rows, each event's realized values feed the
+// per-event accumulators (mean, histogram); nothing per sample leaves the chip.
+// POSITIVE: all times non-negative and finite (host-checked): raw bits are keys.
+// reuse: the CTA ran an earlier tile with these barriers (persistent kernels).
+// Returns false when a staged copy never landed (then every thread returns false).
+//
+// Shared memory: [window: window_slots x 32 doubles][stage buffer 0][stage
+// buffer 1][distribution params][alias table][2 mbarriers].
+template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE>
+__device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, double *rows, int64_t rows_ld,
+                                               bool rows_tile_local, unsigned char *smem, bool reuse) {
+    double *win = reinterpret_cast<double *>(smem);
+    char *stage_buf0 = reinterpret_cast<char *>(smem + a.smem_stage_off);
+    DistParam *s_dist = reinterpret_cast<DistParam *>(smem + a.smem_tables_off);
+    AliasEntry *s_alias = reinterpret_cast<AliasEntry *>(smem + a.smem_tables_off + a.n_dist * sizeof(DistParam));
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + a.smem_bar_off);
+    const DistParam *dists = a.tables_in_smem ? s_dist : a.dist;
+    const AliasEntry *alias = a.tables_in_smem ? s_alias : a.alias;
+
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int NW = a.n_warps;
+    const int64_t s = tile * kTile + lane;
+    const int64_t rcol = rows_tile_local ? (int64_t)lane : s;
+    const bool active = s < a.n;
+    const unsigned active_mask = __ballot_sync(0xFFFFFFFFu, active);
+    uint64_t seed = 0;
+    if (!GIVEN && active) seed = a.seeds ? (uint64_t)a.seeds[s] : (uint64_t)(a.seed0 + s);
+
+    // distribution tables into shared memory; fresh barriers for this tile
+    if (a.tables_in_smem) {
+        for (int i = threadIdx.x; i < a.n_dist; i += blockDim.x) s_dist[i] = a.dist[i];
+        for (int i = threadIdx.x; i < a.n_alias; i += blockDim.x) s_alias[i] = a.alias[i];
+    }
+    if (threadIdx.x == 0) {
+        if (reuse) {
+            asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bars[0])) : "memory");
+            asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bars[1])) : "memory");
+        }
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (a.n_stages > 0) stage_issue(a, 0, stage_buf0, &bars[0]);
+        if (a.n_stages > 1) stage_issue(a, 1, stage_buf0 + a.stage_bytes, &bars[1]);
+    }
+
+    for (int l = 0; l < a.n_stages; ++l) {
+        const int b = l & 1;
+        const char *buf = stage_buf0 + b * a.stage_bytes;
+        const bool ok = stage_wait(&bars[b], (uint32_t)((l >> 1) & 1), a.err);
+        if (__syncthreads_or(!ok)) {  // a copy that never landed: drain, then leave together
+            if (threadIdx.x == 0 && l + 1 < a.n_stages)
+                stage_wait(&bars[b ^ 1], (uint32_t)(((l + 1) >> 1) & 1), a.err);
+            __syncthreads();
+            return false;
+        }
+        const int4 meta = __ldg(reinterpret_cast<const int4 *>(a.stage_meta) + l);
+        // a stage whose records exceed the buffer is read from global memory
+        const EvRec *sev = meta.y >= 0 ? reinterpret_cast<const EvRec *>(buf) : a.ev + meta.x;
+        const PredRec *spred = meta.y >= 0 ? reinterpret_cast<const PredRec *>(buf + a.stage_pred_off)
+                                           : a.pred + meta.z;
+        const int ib = __ldg(&a.wk_off[l * NW + warp]) - meta.x;
+        const int ie = __ldg(&a.wk_off[l * NW + warp + 1]) - meta.x;
+        for (int i = ib; i < ie; ++i) {
+            const EvRec ev = sev[i];
+            long long lk = ev.init_key, lbits = ev.init_bits;
+            int32_t cause = -1;
+            for (int p = ev.pred_begin - meta.z; p < ev.pred_end - meta.z; ++p) {
+                const PredRec pr = spred[p];
+                double dur;
+                if (GIVEN) {
+                    dur = (active && pr.link >= 0) ? __ldg(&a.dur_in[(int64_t)pr.link * a.ld_in + s]) : 0.0;
+                } else {
+                    dur = link_duration(pr.kd, pr.v, (uint32_t)pr.link, seed, dists, alias, a.err);
+                    if (!STATS && (pr.kd & KD_WRITE) && a.durations && active)
+                        a.durations[(int64_t)pr.link * a.ld + s] = dur;
+                }
+                double src;
+                if (WIN_SMEM && pr.src_slot >= 0) {
+                    src = win[pr.src_slot * kTile + lane];
+                } else {
+                    src = active ? rows[(int64_t)pr.src_user * rows_ld + rcol] : 0.0;
+                }
+                const double t = src + dur;  // the one FP64 add of the edge (_core.cpp:341)
+                long long tb = __double_as_longlong(t);
+                long long tk = order_key<POSITIVE>(tb);
+                if (ev.ub_key < tk) {  // t = std::min(t, ub)
+                    tk = ev.ub_key;
+                    tb = ev.ub_bits;
+                }
+                if (tk >= lk) {  // if (t >= latest) { latest = t; cause = src; }
+                    lk = tk;
+                    lbits = tb;
+                    cause = pr.src_user;
+                }
+            }
+            if (ev.ub_key < lk) lbits = ev.ub_bits;  // realized = std::min(latest, ub)
+            const double real = __longlong_as_double(lbits);
+            if (WIN_SMEM && ev.slot >= 0) win[ev.slot * kTile + lane] = real;
+            if (STATS) accumulate_stats(a, ev, lbits, active, active_mask);
+            if (active) {
+                if (rows) rows[(int64_t)ev.user * rows_ld + rcol] = real;
+                if (!STATS && a.cause) a.cause[(int64_t)ev.user * a.ld + s] = cause;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && l + 2 < a.n_stages)
+            stage_issue(a, l + 2, stage_buf0 + b * a.stage_bytes, &bars[b]);
+    }
+    // Aux pass: duration rows of fixed links and of links no precedence entry references.
+    if (!STATS && !GIVEN && a.durations) {
+        for (int i = warp; i < a.n_aux; i += NW) {
+            const LinkRec lr = a.aux[i];
+            const double dur = link_duration(lr.kd, lr.v, (uint32_t)lr.link, seed, dists, alias, a.err);
+            if (active) a.durations[(int64_t)lr.link * a.ld + s] = dur;
+        }
+    }
+    return true;
+}
+
+// One CTA per tile of 32 samples.
+template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE>
+__global__ void __launch_bounds__(768) k_propagate(const KArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    double *rows = a.realized ? a.realized : a.scratch;  // global realized rows
+    if (STATS && WIN_SMEM) rows = nullptr;
+    propagate_tile<GIVEN, WIN_SMEM, STATS, POSITIVE>(a, (int64_t)blockIdx.x, rows, a.ld, false, smem, false);
+}
+
+}  // namespace mcd

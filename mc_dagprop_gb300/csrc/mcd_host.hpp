@@ -40,13 +40,25 @@ struct McdError : std::runtime_error {
     McdError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
 };
 
-// Shared memory the propagation window may take per CTA.
-constexpr size_t kMaxWindowBytes = 200 * 1024;
+// Shared memory: the propagation window may take up to kMaxWindowBytes; each of
+// the two record staging buffers up to kMaxStageBytes; the whole CTA kSmemMax.
+constexpr size_t kMaxWindowBytes = 196 * 1024;
+constexpr int32_t kMaxWarps = 24;       // single-DAG kernel: 768 threads per CTA
+constexpr int32_t kMaxBatchWarps = 16;  // persistent batch kernel: 512 threads per CTA
+constexpr size_t kMaxStageBytes = 24 * 1024;
+constexpr size_t kMinStageBytes = 4 * 1024;
+constexpr size_t kMaxTableBytes = 16 * 1024;
+constexpr size_t kSmemMax = 226 * 1024;  // 227 KB per CTA, less room for static shared data
 
 // Output of compile_dag: everything the kernels need, host copies.
 struct HostDag {
     int32_t E = 0, L = 0, n_levels = 0, n_warps = 1, window_slots = 0;
     bool win_smem = true;
+    bool positive = false;        // all times non-negative and finite
+    bool tables_in_smem = true;
+    int32_t n_stages = 0, stage_bytes = 0, stage_pred_off = 0;
+    int32_t smem_stage_off = 0, smem_tables_off = 0, smem_bar_off = 0, smem_total = 0;
+    std::vector<int32_t> stage_meta;  // 4 ints per stage
     std::vector<EvRec> ev;
     std::vector<PredRec> pred;
     std::vector<LinkRec> aux;  // links stored by the aux pass
@@ -75,7 +87,8 @@ struct StatsParams {
 };
 StatsParams stats_params(const HostDag &h, int64_t n);
 
-void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &out);
+// n_warps: warps per CTA the kernels will run with (0: chosen from the DAG's width).
+void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &out, int32_t n_warps);
 int64_t order_key_host(int64_t bits);
 
 }  // namespace mcd

@@ -17,8 +17,8 @@ namespace mcd {
 enum Kind : int32_t { K_FIXED = 0, K_EXP = 1, K_GAMMA = 2, K_EMP_ABS = 3, K_EMP_REL = 4 };
 
 // Packed kind word of a link reference: kind | KD_WRITE | dist << 8.  KD_WRITE
-// marks the one reference of a sampled link that stores its duration row; fixed
-// links and unreferenced links are stored by the kernel's aux-link pass.
+// marks the one reference of a link that stores its duration row; links no
+// precedence entry references are stored by the kernel's aux-link pass.
 constexpr int32_t KD_KIND_MASK = 0x7F;
 constexpr int32_t KD_WRITE = 0x80;
 
@@ -45,9 +45,8 @@ struct alignas(16) PredRec {
     int64_t pad;
 };
 
-// A link whose duration row the aux pass stores: fixed links (one value for all
-// samples) and sampled links no precedence entry references (their durations are
-// still part of SimResult.durations).  16 bytes.
+// A link whose duration row the aux pass stores: a link no precedence entry
+// references (its duration is still part of SimResult.durations).  16 bytes.
 struct alignas(16) LinkRec {
     int32_t link;
     int32_t kd;
@@ -93,11 +92,19 @@ struct KArgs {
     const LinkRec *aux;
     const DistParam *dist;
     const AliasEntry *alias;
-    const int32_t *wk_off;  // [n_levels * n_warps + 1] event chunk per (level, warp)
-    int32_t n_levels;
+    const int32_t *wk_off;    // [n_stages * n_warps + 1] event chunk per (stage, warp), compiled indices
+    const int32_t *stage_meta;  // [n_stages][4] {first event, events (negated: read from global), first pred, preds}
+    int32_t n_stages;
     int32_t n_warps;
     int32_t n_aux;
     int32_t window_slots;
+    int32_t n_dist, n_alias;
+    int32_t tables_in_smem;   // distribution tables copied into shared memory
+    int32_t win_smem;         // window on chip (batch kernel dispatch)
+    int32_t positive;         // every time non-negative and finite: raw bits order like doubles
+    int32_t stage_bytes;      // one staging buffer
+    int32_t stage_pred_off;   // predecessor records' offset inside a staging buffer
+    int32_t smem_stage_off, smem_tables_off, smem_bar_off, smem_total;  // shared-memory layout (bytes)
     const int64_t *seeds;  // [n] per-sample seeds; null: sample s uses seed0 + s
     int64_t seed0;
     int64_t n;
@@ -118,6 +125,16 @@ struct KArgs {
     uint32_t *hist;               // [E][kHistStride]
 };
 
+// Arguments of the persistent batch kernel.
+struct BatchArgs {
+    const KArgs *dags;           // [n_dags] statistics-mode arguments, one per DAG
+    const int32_t *items;        // [n_items][2] (dag, tile), longest first
+    int32_t n_items;
+    unsigned int *counter;       // work-queue head, zero before the launch
+    double *scratch;             // per-CTA realized rows for DAGs whose window is not on chip
+    int64_t scratch_stride;      // doubles per CTA (max events x 32)
+};
+
 // Arguments of the statistics finishing kernel.
 struct FArgs {
     const unsigned long long *acc;
@@ -133,7 +150,7 @@ struct FArgs {
 };
 
 // Device error flags.
-enum : int32_t { ERR_GAMMA_REJECTION = 1 };
+enum : int32_t { ERR_GAMMA_REJECTION = 1, ERR_STAGE_TIMEOUT = 2 };
 
 constexpr int kTile = 32;  // samples per tile: one per lane
 

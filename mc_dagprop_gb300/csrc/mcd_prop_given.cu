@@ -1,0 +1,19 @@
+// mcd_prop_given.cu -- instantiations of k_propagate that read given durations.
+#include "mcd_device.cuh"
+
+namespace mcd {
+
+cudaError_t launch_prop_given(const KArgs &a, bool win_smem, bool stats, dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t st) {
+    void (*fn)(const KArgs);
+    if (stats) fn = win_smem ? k_propagate<true, true, true, false> : k_propagate<true, false, true, false>;
+    else fn = win_smem ? k_propagate<true, true, false, false> : k_propagate<true, false, false, false>;
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    fn<<<grid, block, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace mcd

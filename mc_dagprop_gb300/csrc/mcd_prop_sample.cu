@@ -1,0 +1,80 @@
+// mcd_prop_sample.cu -- instantiations of k_propagate that draw their own delays,
+// and the persistent batch kernel.  (Separate translation units keep the build
+// parallel.)
+#include "mcd_device.cuh"
+
+namespace mcd {
+
+// Persistent statistics kernel over a batch of DAGs: each CTA takes (DAG, tile)
+// items from an atomic work queue (ordered longest first by the host) until the
+// queue is empty.  No CTA waits on another: the queue head is a plain counter.
+// DAGs whose window is not on chip use per-CTA scratch rows (32 samples each).
+__global__ void __launch_bounds__(512) k_batch_stats(const BatchArgs b) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ KArgs s_args;
+    __shared__ int s_item;
+    bool reuse = false;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(b.counter, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= b.n_items) return;
+        const int2 it = __ldg(reinterpret_cast<const int2 *>(b.items) + item);
+        if (threadIdx.x == 0) s_args = b.dags[it.x];
+        __syncthreads();
+        const KArgs &a = s_args;
+        bool ok;
+        if (a.win_smem) {
+            ok = a.positive ? propagate_tile<false, true, true, true>(a, it.y, nullptr, 0, true, smem, reuse)
+                            : propagate_tile<false, true, true, false>(a, it.y, nullptr, 0, true, smem, reuse);
+        } else {
+            double *rows = b.scratch + (int64_t)blockIdx.x * b.scratch_stride;
+            ok = a.positive ? propagate_tile<false, false, true, true>(a, it.y, rows, kTile, true, smem, reuse)
+                            : propagate_tile<false, false, true, false>(a, it.y, rows, kTile, true, smem, reuse);
+        }
+        reuse = true;
+        if (!ok) return;
+        __syncthreads();  // s_args / s_item are rewritten by the next item
+    }
+}
+
+cudaError_t launch_prop_sample(const KArgs &a, bool win_smem, bool stats, bool positive, dim3 grid, dim3 block,
+                               size_t smem, cudaStream_t st) {
+    void (*fn)(const KArgs);
+    if (stats) {
+        if (positive) fn = win_smem ? k_propagate<false, true, true, true> : k_propagate<false, false, true, true>;
+        else fn = win_smem ? k_propagate<false, true, true, false> : k_propagate<false, false, true, false>;
+    } else {
+        if (positive) fn = win_smem ? k_propagate<false, true, false, true> : k_propagate<false, false, false, true>;
+        else fn = win_smem ? k_propagate<false, true, false, false> : k_propagate<false, false, false, false>;
+    }
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    fn<<<grid, block, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+// Persistent batch launch: one CTA per SM slot, `blocks_per_sm` of them per SM.
+cudaError_t launch_batch_stats(const BatchArgs &b, int n_warps, size_t smem, int grid, cudaStream_t st) {
+    if (smem > 48 * 1024) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_batch_stats, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_batch_stats<<<grid, n_warps * 32, smem, st>>>(b);
+    return cudaGetLastError();
+}
+
+// CTAs of the batch kernel that fit on one SM at this block size and shared memory.
+cudaError_t batch_blocks_per_sm(int n_warps, size_t smem, int *out) {
+    if (smem > 48 * 1024) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_batch_stats, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_batch_stats, n_warps * 32, smem);
+}
+
+}  // namespace mcd

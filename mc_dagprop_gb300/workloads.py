@@ -47,8 +47,8 @@ def layered_dag(seed: int, n_layers: int, width: int, back: int, types, max_dela
                 max_preds: int = 4) -> dict:
     """Layered DAG: event j of layer k has earliest = 60 k + U(0,30) s; each event in
     layer k > 0 takes 1..max_preds predecessors (uniform count) drawn without
-    replacement from layers k-back .. k-1; minimal_duration ~ U(30, 300) s; activity
-    types uniform over ``types``."""
+    replacement from layers k-back .. k-1 (a uniform random subset, in random
+    order); minimal_duration ~ U(30, 300) s; activity types uniform over ``types``."""
     rng = np.random.default_rng(seed)
     E = n_layers * width
     layer = np.repeat(np.arange(n_layers), width)
@@ -58,13 +58,17 @@ def layered_dag(seed: int, n_layers: int, width: int, back: int, types, max_dela
     srcs = []
     for k in range(1, n_layers):
         lo = max(0, k - back) * width
-        hi = k * width
-        pool = hi - lo
-        for j in range(width):
-            c = min(int(counts[k * width + j]), pool)
-            counts[k * width + j] = c
-            # without replacement: a random permutation prefix of the pool
-            srcs.append(lo + rng.choice(pool, size=c, replace=False))
+        pool = k * width - lo
+        c = np.minimum(counts[k * width:(k + 1) * width], pool)
+        counts[k * width:(k + 1) * width] = c
+        m = int(min(max_preds, pool))
+        # the m smallest of random keys per row: a uniform random m-subset, in random order
+        keys = rng.random((width, pool))
+        pick = np.argpartition(keys, m - 1, axis=1)[:, :m] if m < pool else np.argsort(keys, axis=1)
+        order = np.take_along_axis(keys, pick, axis=1).argsort(axis=1)
+        pick = np.take_along_axis(pick, order, axis=1)
+        keep = np.arange(pick.shape[1])[None, :] < c[:, None]
+        srcs.append(lo + pick[keep])
     pred_src = np.concatenate(srcs).astype(np.int32) if srcs else np.zeros(0, np.int32)
     P = len(pred_src)
     target = np.arange(width, E, dtype=np.int32)

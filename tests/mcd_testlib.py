@@ -26,7 +26,9 @@ class DagDesc(C.Structure):
 class DagInfo(C.Structure):
     _fields_ = [("n_events", C.c_int32), ("n_links", C.c_int32), ("n_levels", C.c_int32), ("n_warps", C.c_int32),
                 ("n_preds", C.c_int64), ("window_slots", C.c_int32), ("window_in_smem", C.c_int32),
-                ("n_orphan_links", C.c_int32), ("device", C.c_int32), ("device_bytes", C.c_int64)]
+                ("n_orphan_links", C.c_int32), ("device", C.c_int32), ("device_bytes", C.c_int64),
+                ("n_stages", C.c_int32), ("smem_bytes", C.c_int32), ("positive", C.c_int32),
+                ("tables_in_smem", C.c_int32)]
 
 
 def header_functions() -> list[str]:
@@ -58,6 +60,7 @@ def lib():
         L.mcd_dag_node_count.argtypes = [P]
         L.mcd_dag_activity_count.argtypes = [P]
         L.mcd_dag_get_info.argtypes = [P, C.POINTER(DagInfo)]
+        L.mcd_dag_describe.argtypes = [C.POINTER(DagDesc), P, C.POINTER(DagInfo)]
         L.mcd_dag_stream.argtypes = [P]
         L.mcd_dag_stream.restype = P
         L.mcd_run_many_host.argtypes = [P, P, I64, P, P, P]
@@ -121,6 +124,31 @@ def make_desc(flat: dict):
                 ptr(arrs["act_duration"]), ptr(arrs["act_type"]), len(arrs["target"]), ptr(arrs["target"]),
                 ptr(arrs["pred_offsets"]), ptr(arrs["pred_src"]), ptr(arrs["pred_act"]), float(flat["max_delay"]))
     return d, arrs
+
+
+def describe(flat: dict, gen: list, env: dict | None = None):
+    """Host-only compile of a flat DAG: (status, DagInfo, message)."""
+    import os as _os
+
+    old = {}
+    for k, v in (env or {}).items():
+        old[k] = _os.environ.get(k)
+        _os.environ[k] = v
+    try:
+        gh, rc, keep = make_generator(gen)
+        assert rc == MCD_OK
+        d, arrs = make_desc(flat)
+        info = DagInfo()
+        rc = lib().mcd_dag_describe(C.byref(d), gh, C.byref(info))
+        msg = last_error()
+        lib().mcd_generator_destroy(gh)
+        return rc, info, msg
+    finally:
+        for k, v in old.items():
+            if v is None:
+                _os.environ.pop(k, None)
+            else:
+                _os.environ[k] = v
 
 
 def load_golden(name: str):

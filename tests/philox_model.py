@@ -9,12 +9,15 @@ tolerance.
 """
 from __future__ import annotations
 
+import struct
+
 import numpy as np
 
 M0, M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
 W0, W1 = np.uint64(0x9E3779B9), np.uint64(0xBB67AE85)
 MASK = np.uint64(0xFFFFFFFF)
 SALT = 0x6D636470
+KEY0, KEY1 = 0x243F6A88, 0x85A308D3
 
 
 def philox4x32_10(c0, c1, c2, c3, k0, k1):
@@ -35,15 +38,61 @@ def philox4x32_10(c0, c1, c2, c3, k0, k1):
     return tuple(x.astype(np.uint32) for x in (c0, c1, c2, c3))
 
 
-def words(seeds, link, attempt=0, word2=0):
+def words(seeds, link, attempt=0, sel=0):
     s = np.asarray(seeds, dtype=np.int64).view(np.uint64)
-    return philox4x32_10(link, attempt, word2, SALT, s & MASK, s >> np.uint64(32))
+    return philox4x32_10(s & MASK, s >> np.uint64(32), link, SALT ^ ((attempt << 1) | sel), KEY0, KEY1)
 
 
 def u01_open0(r):
     """(r + 1/2) / 2^32 as the kernel rounds it to float32."""
     f = np.asarray(r, dtype=np.uint32).astype(np.float32)
     return (f.astype(np.float64) * 2.0 ** -32 + 2.0 ** -33).astype(np.float32)
+
+
+M52, H52 = (1 << 52) - 1, 1 << 52
+
+
+def _bits(x: float) -> int:
+    return struct.unpack("<q", struct.pack("<d", x))[0]
+
+
+def _from_bits(b: int) -> float:
+    return struct.unpack("<d", struct.pack("<q", b))[0]
+
+
+def mul_trunc(a: float, g: float) -> float:
+    """The kernel's integer product a * g (top 53 bits of the mantissa product,
+    truncated), FP64 multiply for the operands it hands to the FP64 unit."""
+    ab, gb = _bits(a), _bits(g)
+    ea, eg = (ab >> 52) & 0x7FF, (gb >> 52) & 0x7FF
+    e = ea + eg - 1023
+    if gb <= 0 or eg in (0, 0x7FF) or ea in (0, 0x7FF) or e <= 0 or e >= 0x7FE:
+        return a * g
+    ma, mg = ((ab & M52) | H52) << 11, ((gb & M52) | H52) << 11
+    hi = (ma * mg) >> 64
+    if hi >> 63:
+        m, e = hi >> 11, e + 1
+    else:
+        m = hi >> 10
+    sign = ab & (1 << 63) if ab >= 0 else (1 << 63)
+    b = (sign | (e << 52) | (m & M52)) if ab < 0 else ((e << 52) | (m & M52))
+    if ab < 0:
+        b -= 1 << 64
+    return _from_bits(b)
+
+
+def one_plus(x) -> float:
+    """The kernel's double 1 + x for a float32 x >= 0."""
+    b = int(np.asarray(x, np.float32).view(np.uint32))
+    e = (b >> 23) & 0xFF
+    if e == 0:
+        return 1.0
+    if e < 127:
+        m = (b & 0x7FFFFF) | 0x800000
+        sh = e - 98
+        frac = (m << sh) if sh >= 0 else ((m >> -sh) if sh > -24 else 0)
+        return _from_bits(0x3FF0000000000000 | frac)
+    return float(np.float32(1.0) + np.float32(x))
 
 
 def exponential_durations(seeds, link, base, lam, max_scale):
@@ -53,10 +102,11 @@ def exponential_durations(seeds, link, base, lam, max_scale):
     ratio = max_scale / lam
     c = 1.0 if np.isinf(ratio) else -np.expm1(-ratio)
     omc = 0.0 if np.isinf(ratio) else np.exp(-ratio)
-    V = np.float32(c) * w + np.float32(omc)
-    X = np.minimum(-lam * np.log(V), max_scale)
-    X = np.maximum(X, 0.0)
-    return base + X * base
+    V = (np.float32(c) * w.astype(np.float32) + np.float32(omc)).astype(np.float32)
+    # the kernel takes the logarithm with the MUFU approximation (within 2^-21.4
+    # absolute on [0.5, 2], 3 ulp elsewhere); this model takes the exact one
+    X = np.maximum(np.minimum(-np.float32(lam) * np.log(V), np.float32(max_scale)), np.float32(0.0)).astype(np.float32)
+    return np.array([mul_trunc(float(base), one_plus(x)) for x in X])
 
 
 def alias_table(values, weights):
@@ -89,6 +139,13 @@ def alias_table(values, weights):
             th[i] = 0xFFFFFFFF if t >= 4294967295.0 else int(t)
         va[i] = v[i] if th[i] == 0xFFFFFFFF else v[alias[i]]
     return th, v, va
+
+
+def empirical_durations(seeds, link, base, values, weights, relative):
+    """The kernel's duration for each seed (exact): base + value, or
+    base + factor * base, in IEEE double arithmetic as the reference forms them."""
+    v = empirical_values(seeds, link, values, weights)
+    return base + v * base if relative else base + v
 
 
 def empirical_values(seeds, link, values, weights):

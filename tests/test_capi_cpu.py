@@ -151,3 +151,34 @@ def test_reference_and_workload_generators_agree_on_shapes():
     assert len(flat1["earliest"]) == 2000 and len(gen1) == 5
     f6 = six_event_flat()
     assert list(f6["target"]) == [1, 2, 3, 4]
+
+
+def test_compiler_layout_decisions():
+    """Host compile of the benchmark DAG shapes: window on chip, staged records,
+    shared memory within the per-CTA limit, positive-time fast path."""
+    from mc_dagprop_gb300 import workloads as W
+    from mcd_testlib import describe
+
+    for flat, gen in (W.config0(), W.config1(n_layers=200)):
+        rc, info, msg = describe(flat, gen)
+        assert rc == MCD_OK, msg
+        assert info.window_in_smem == 1 and info.positive == 1 and info.tables_in_smem == 1
+        assert info.n_stages >= info.n_levels
+        assert 0 < info.smem_bytes <= 227 * 1024
+        assert info.window_slots * 256 < info.smem_bytes
+        assert info.device == -1
+    # a window too large for shared memory falls back to global rows, staging stays on
+    flat = W.layered_dag(3, 6, 1500, 1, [1], 10.0)
+    rc, info, msg = describe(flat, [("constant", 1, 1.0)])
+    assert rc == MCD_OK and info.window_in_smem == 0 and info.window_slots >= 1500
+    assert info.n_stages > info.n_levels  # wide levels are split into stages
+    # negative times disable the positive fast path
+    f6 = six_event_flat()
+    f6["earliest"] = f6["earliest"] - 50.0
+    rc, info, msg = describe(f6, [("constant", 1, 1.0)])
+    assert rc == MCD_OK and info.positive == 0
+    # an event with more predecessors than a staging buffer holds
+    n = 2000
+    big = flat_from_lists([0.0] * (n + 1), {(i, n): (i, 1.0, 1) for i in range(n)}, [(n, [(i, i) for i in range(n)])], 1e6)
+    rc, info, msg = describe(big, [("constant", 1, 1.0)])
+    assert rc == MCD_OK and info.n_levels == 2

@@ -1,0 +1,53 @@
+"""Batched persistent launch: every DAG of a batch gets exactly the statistics
+the single-DAG path computes for it (the accumulation is exact integer ticks, so
+the tolerance is zero), on the first run and on graph replays."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import mc_dagprop_gb300 as m
+from mc_dagprop_gb300 import workloads as W
+from mcd_testlib import propagator_from_flat
+
+pytestmark = pytest.mark.gpu
+
+
+def _prop(flat, gen, nw):
+    g = W.to_generator(m, gen)
+    return m.MonteCarloPropagator.from_arrays(flat["earliest"], flat["act_idx"], flat["act_duration"],
+                                              flat["act_type"], flat["target"], flat["pred_offsets"],
+                                              flat["pred_src"], flat["pred_act"], flat["max_delay"], g, n_warps=nw)
+
+
+@pytest.mark.parametrize("nw", [4, 16])
+def test_batch_equals_single_dag_statistics(cuda, nw):
+    dags = W.mixed_dags(seed=5, n_dags=10, ev_lo=60, ev_hi=4000, s_lo=40, s_hi=3000, five_types=True)
+    props, seed0, ns = [], [], []
+    for flat, gen, n, sb in dags:
+        props.append(_prop(flat, gen, nw))
+        seed0.append(sb)
+        ns.append(n)
+    # one DAG whose window does not fit in shared memory (global scratch rows)
+    wide = W.layered_dag(3, 6, 1500, 1, [1, 2], 10.0)
+    props.append(_prop(wide, list(W.GEN_TWO_TYPES), nw))
+    seed0.append(10**6)
+    ns.append(100)
+    assert props[-1].info()["window_in_smem"] is False
+    batch = m.Batch(props, seed0, ns)
+    assert batch.items == sum((n + 31) // 32 for n in ns)
+    for rep in range(2):
+        batch.run()
+        for i, p in enumerate(props):
+            got = batch.stats(i, hist=True)
+            ref = p.run_stats(n=ns[i], seed0=seed0[i], hist=True)
+            for k in ("mean", "p50", "p90", "p99", "p_on_time", "hist"):
+                assert np.array_equal(got[k], ref[k]), (rep, i, k)
+
+
+def test_batch_rejects_mixed_warps(cuda):
+    flat, gen = W.config0()
+    a = _prop(flat, gen, 4)
+    b = _prop(flat, gen, 8)
+    with pytest.raises(ValueError, match="same n_warps"):
+        m.Batch([a, b], [0, 0], [64, 64])

@@ -193,9 +193,10 @@ def run_batched(args):
     """Batching workload: 512 DAGs (events log-uniform 100-50,000, layer width
     20-200, two delay kinds), each with its own sample count (log-uniform
     1,000-100,000) and seed range; per-event mean and p50/p90/p99 from 256-bin
-    histograms.  The batched form (one persistent launch per step, CUDA graph,
-    warps per CTA from the autotuner) against the plain form (one
-    mcd_stats_device call per DAG, the same statistics) on the same GPU."""
+    histograms.  The batched form (persistent launches per width class, CUDA
+    graphs, warps per CTA from the autotuner) against the plain form (one
+    mcd_stats_device call per DAG, each DAG compiled with its own automatic
+    warps, the same statistics) on the same GPU."""
     import torch
 
     from mc_dagprop_gb300 import batching
@@ -204,55 +205,46 @@ def run_batched(args):
     t0 = time.perf_counter()
     dags = W.config2(n_dags=args.dags)
     gen_s = time.perf_counter() - t0
-    flats = [d[0] for d in dags]
-    gens = [d[1] for d in dags]
-    ns = [int(d[2]) for d in dags]
-    seed0 = [int(d[3]) for d in dags]
-    units = sum(int(f["act_idx"].max() + 1) * n for f, n in zip(flats, ns))
+    items = [(d[0], d[1], int(d[2]), int(d[3])) for d in dags]
+    units = sum(int(f["act_idx"].max() + 1) * n for f, _, n, _ in items)
     t0 = time.perf_counter()
-    nw = batching.tune_warps(flats, gens, ns, use_cache=False)
-    tune_s = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    props = [batching.compile_dag(f, g, nw) for f, g in zip(flats, gens)]
-    compile_s = time.perf_counter() - t0
+    runner = batching.BatchRunner(items, use_cache=False)
+    setup_s = time.perf_counter() - t0
+    plain_props = [batching.compile_dag(f, g) for f, g, _, _ in items]
     lib = _capi()
     lib.mcd_stats_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.POINTER(_Stats), C.c_void_p]
     dev = torch.device("cuda", 0)
     outs = []
-    for p in props:
+    for p in plain_props:
         t = torch.empty((5, p.node_count()), dtype=torch.float64, device=dev)
         outs.append((t, _Stats(*(t[k].data_ptr() for k in range(5)), None)))
     stream = torch.cuda.Stream(device=dev)
 
     def plain_run():
-        for i, (p, (t, st)) in enumerate(zip(props, outs)):
-            if lib.mcd_stats_device(C.c_void_p(p._handle()), None, seed0[i], ns[i], C.byref(st),
+        for i, (p, (t, st)) in enumerate(zip(plain_props, outs)):
+            if lib.mcd_stats_device(C.c_void_p(p._handle()), None, items[i][3], items[i][2], C.byref(st),
                                     C.c_void_p(stream.cuda_stream)) != 0:
                 raise RuntimeError(lib.mcd_last_error().decode())
 
-    def timed(fn, st, reps):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        a.record(st)
-        for _ in range(reps):
-            fn()
-        b.record(st)
-        torch.cuda.synchronize()
-        return a.elapsed_time(b) / reps
-
     plain_run()  # workspaces allocated here
     torch.cuda.synchronize()
-    plain_ms = timed(plain_run, stream, args.steps)
-    batch = __import__("mc_dagprop_gb300").Batch(props, seed0, ns)
-    bstream = torch.cuda.ExternalStream(batch.stream, device=dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(args.steps):
+        plain_run()
+    b.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = a.elapsed_time(b) / args.steps
     for _ in range(max(1, args.warmup)):
-        batch.run(wait=True)
-    batch_ms = timed(lambda: batch.run(wait=False), bstream, args.steps)
-    batch.sync()
-    # the batch's statistics equal the plain path's, DAG by DAG
+        runner.run()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()  # several streams: host clock around synchronised runs
+    for _ in range(args.steps):
+        runner.run()
+    batch_ms = (time.perf_counter() - t0) * 1e3 / args.steps
     mism = 0
-    for i in range(0, len(props), max(1, len(props) // 16)):
-        got = batch.stats(i)
+    for i in range(0, len(items), max(1, len(items) // 32)):
+        got = runner.stats(i)
         ref = outs[i][0].cpu().numpy()
         mism += int(not np.array_equal(got["mean"], ref[0]) or not np.array_equal(got["p99"], ref[3]))
     print(json.dumps({
@@ -261,12 +253,163 @@ def run_batched(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "512 DAGs, events log-uniform 100-50,000 (width 20-200), samples log-uniform "
                                "1,000-100,000, own seed ranges; per-event mean, p50/p90/p99 (256-bin histograms)",
-                   "dags": len(props), "events_total": int(sum(len(f["earliest"]) for f in flats)),
-                   "sample_edges_per_step": units, "n_warps": nw, "work_items": batch.items, "grid": batch.grid},
+                   "dags": len(items), "events_total": int(sum(len(f["earliest"]) for f, _, _, _ in items)),
+                   "sample_edges_per_step": units,
+                   "classes (warps, dags, items)": runner.classes},
         "plain": {"value": units / (plain_ms * 1e-3), "ms_per_step": plain_ms,
-                  "path": "one mcd_stats_device call per DAG on one stream"},
+                  "path": "one mcd_stats_device call per DAG on one stream, automatic warps per DAG"},
         "batched_over_plain": plain_ms / batch_ms, "check_mismatches": mism,
-        "host_seconds": {"generate": gen_s, "autotune": tune_s, "compile_512": compile_s},
+        "host_seconds": {"generate": gen_s, "classify_autotune_compile": setup_s},
+    }))
+    return 0
+
+
+def run_serving(args):
+    """Serving workload: Poisson arrivals at `--rate` requests/s for `--duration` s.
+    Each request is a DAG from the config-0 generator with events log-uniform in
+    200-20,000, samples log-uniform in 4,096-65,536, the five delay kinds and its
+    own seeds, asking for per-event mean and p50/p90/p99.  DAGs come from a pool
+    of `--pool` generated ones (generation is not part of serving); every request
+    still travels the whole path -- submit, host compile, admission against the
+    64 GB budget, batched launch, statistics back.  Reported: completed
+    sample-edges/s and p50/p99 latency, against the plain per-request path (create
+    the propagator, mcd_stats_host, one request after another) on a sample of the
+    same requests."""
+    import threading
+
+    import mc_dagprop_gb300 as m
+    from mc_dagprop_gb300 import batching
+    from mc_dagprop_gb300 import workloads as W
+
+    pool = W.config4_requests(n_requests=args.pool)
+    gens = [W.to_generator(m, g) for _, g, _, _ in pool]
+    links = [int(f["act_idx"].max()) + 1 for f, _, _, _ in pool]
+    rng = np.random.default_rng(7)
+    n_req = int(args.rate * args.duration)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n_req))
+    which = rng.integers(0, len(pool), n_req)
+    server = m.Server(memory_budget=64 << 30, n_streams=args.streams, n_warps=8, compile_threads=args.compile_threads)
+    # warm the server (kernels loaded, pool grown) with a few requests
+    for i in range(4):
+        f, _, n, s0 = pool[i]
+        t = server.submit(f["earliest"], f["act_idx"], f["act_duration"], f["act_type"], f["target"],
+                          f["pred_offsets"], f["pred_src"], f["pred_act"], f["max_delay"], gens[i], 10**12 + i, 256)
+        server.wait(t, timeout_ms=60_000)
+    tickets = [None] * n_req
+    lat = np.zeros(n_req)
+    done_at = np.zeros(n_req)
+    errors = []
+
+    def collector():
+        for i in range(n_req):
+            while tickets[i] is None:
+                time.sleep(0.0002)
+            try:
+                r = None
+                while r is None:
+                    r = server.wait(tickets[i], timeout_ms=1000.0)
+                lat[i] = r["latency_ms"]
+                done_at[i] = time.perf_counter()
+            except RuntimeError as e:
+                errors.append(str(e))
+
+    th = threading.Thread(target=collector)
+    th.start()
+    t0 = time.perf_counter()
+    for i in range(n_req):
+        now = time.perf_counter() - t0
+        if arrivals[i] > now:
+            time.sleep(arrivals[i] - now)
+        f, _, n, _ = pool[which[i]]
+        tickets[i] = server.submit(f["earliest"], f["act_idx"], f["act_duration"], f["act_type"], f["target"],
+                                   f["pred_offsets"], f["pred_src"], f["pred_act"], f["max_delay"], gens[which[i]],
+                                   1000 * i, n)
+    submit_s = time.perf_counter() - t0
+    th.join()
+    wall = max(done_at.max() - t0, 1e-9)
+    units = sum(links[which[i]] * pool[which[i]][2] for i in range(n_req))
+    counters = server.counters()
+    del server
+    # plain per-request path on a sample of the same requests, one after another
+    k = min(args.plain_requests, n_req)
+    t1 = time.perf_counter()
+    plain_units = 0
+    for i in range(k):
+        f, g, n, _ = pool[which[i]]
+        prop = batching.compile_dag(f, g)
+        prop.run_stats(n=n, seed0=1000 * i)
+        plain_units += links[which[i]] * n
+    plain_s = time.perf_counter() - t1
+    print(json.dumps({
+        "metric": "sample-edges/s (served statistics)", "value": units / wall, "unit": METRIC, "n_gpus": 1,
+        "steps": 1, "warmup": 4, "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "Poisson arrivals; requests: events log-uniform 200-20,000, samples log-uniform "
+                               "4,096-65,536, five delay kinds, own seeds; per-event mean, p50/p90/p99",
+                   "rate_per_s": args.rate, "duration_s": args.duration, "requests": n_req, "dag_pool": len(pool),
+                   "offered_sample_edges_per_s": units / args.duration, "streams": args.streams,
+                   "compile_threads": args.compile_threads, "memory_budget_gb": 64},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "max": float(lat.max())},
+        "completed": int(counters["completed"]), "batches": int(counters["batches"]), "errors": len(errors),
+        "submit_seconds": submit_s,
+        "plain": {"value": plain_units / plain_s, "requests": k,
+                  "path": "per request: create propagator (host compile + upload) + mcd_stats_host, sequential"},
+        "served_over_plain": (units / wall) / (plain_units / plain_s),
+    }))
+    return 0
+
+
+def run_gradient(args):
+    """Differentiation workload: one DAG of 10,000 events (100 layers of 100, five
+    delay kinds), 65,536 samples; objective J = mean over samples of the sum over
+    events of (realized - earliest); gradient with respect to every earliest time
+    and every minimal_duration by the adjoint kernel.  Checked on 200 random
+    coordinates against central finite differences with common random numbers
+    (the same seeds), step 1e-3 s."""
+    from mc_dagprop_gb300 import batching
+    from mc_dagprop_gb300 import workloads as W
+
+    flat, gen = W.config3()
+    n, seed0, h = args.grad_samples, 2024, 1e-3
+    prop = batching.compile_dag(flat, gen)
+    L = prop.activity_count()
+    for _ in range(max(1, args.warmup)):
+        g = prop.gradient(n, seed0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        g = prop.gradient(n, seed0)
+    dt = (time.perf_counter() - t0) / args.steps
+
+    def J(f):
+        st = batching.compile_dag(f, gen).run_stats(n=n, seed0=seed0)
+        return float(np.sum(st["mean"] - f["earliest"]))
+
+    rng = np.random.default_rng(1)
+    errs = []
+    for e in rng.choice(len(flat["earliest"]), args.fd_coords // 2, replace=False):
+        fp, fm = dict(flat), dict(flat)
+        fp["earliest"], fm["earliest"] = flat["earliest"].copy(), flat["earliest"].copy()
+        fp["earliest"][e] += h
+        fm["earliest"][e] -= h
+        fd = (J(fp) - J(fm)) / (2 * h)
+        errs.append(abs(fd - g["grad_earliest"][e]) / (1.0 + abs(fd)))
+    for k in rng.choice(len(flat["act_idx"]), args.fd_coords // 2, replace=False):
+        fp, fm = dict(flat), dict(flat)
+        fp["act_duration"], fm["act_duration"] = flat["act_duration"].copy(), flat["act_duration"].copy()
+        fp["act_duration"][k] += h
+        fm["act_duration"][k] -= h
+        fd = (J(fp) - J(fm)) / (2 * h)
+        errs.append(abs(fd - g["grad_base"][flat["act_idx"][k]]) / (1.0 + abs(fd)))
+    print(json.dumps({
+        "metric": "sample-edges/s (adjoint: forward + backward)", "value": n * L / dt, "unit": METRIC,
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "10,000 events (100 layers x 100), five delay kinds, gradient of "
+                               "mean_s sum_e (realized - earliest) w.r.t. every earliest and minimal_duration",
+                   "samples": n, "links": L, "objective": g["objective"]},
+        "fd_check": {"coordinates": len(errs), "step_s": h, "max_rel_err": float(np.max(errs)),
+                     "median_rel_err": float(np.median(errs)), "metric": "|fd - adjoint| / (1 + |fd|)"},
     }))
     return 0
 
@@ -280,7 +423,15 @@ def main():
     ap.add_argument("--e2e-samples", type=int, default=512)
     ap.add_argument("--layers", type=int, default=2000)
     ap.add_argument("--impl", default="gb300")
-    ap.add_argument("--workload", default="single", choices=["single", "batched"])
+    ap.add_argument("--workload", default="single", choices=["single", "batched", "gradient", "serving"])
+    ap.add_argument("--rate", type=float, default=2000.0)
+    ap.add_argument("--duration", type=float, default=5.0)
+    ap.add_argument("--pool", type=int, default=128)
+    ap.add_argument("--streams", type=int, default=3)
+    ap.add_argument("--compile-threads", type=int, default=8)
+    ap.add_argument("--plain-requests", type=int, default=200)
+    ap.add_argument("--grad-samples", type=int, default=65536)
+    ap.add_argument("--fd-coords", type=int, default=200)
     ap.add_argument("--dags", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -288,6 +439,10 @@ def main():
         return run_reference_arm(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "gradient":
+        return run_gradient(args)
+    if args.workload == "serving":
+        return run_serving(args)
 
     import torch
 

@@ -16,6 +16,8 @@
  *   mcd_run_device            the same, device buffers, sample-minor layout
  *   mcd_propagate_*           the propagation loop alone       _core.cpp:331-350
  *   mcd_batch_*               many DAGs in one persistent launch (no reference counterpart)
+ *   mcd_gradient_host         pathwise gradient of expected tardiness (no reference counterpart)
+ *   mcd_server_*              continuous-batching request server (no reference counterpart)
  *   mcd_stats_*               per-event statistics (no reference counterpart; the
  *                             reference's users stack run_many results in numpy,
  *                             demo/monte_carlo.py:48-49)
@@ -216,6 +218,46 @@ int mcd_batch_download(mcd_batch *batch, int32_t i, const mcd_stats *host);
 void *mcd_batch_stream(const mcd_batch *batch);
 int64_t mcd_batch_items(const mcd_batch *batch);
 int32_t mcd_batch_grid(const mcd_batch *batch);
+
+/* ---- Pathwise gradient (adjoint; no reference counterpart) ----
+ * Objective J = mean over the n samples (seeds seed0 .. seed0+n-1) of
+ * sum over events of (realized - earliest).  Writes J, dJ/d earliest [n_events]
+ * and dJ/d base duration [activity_count] (per link index; Activity.minimal_duration
+ * of the activity with that idx), any may be NULL.  The derivative follows each
+ * sample's winning predecessor chain (the cause_event tie rule): slope 1 along
+ * unclamped chains, d(duration)/d(base) at the winning link.  Needs finite times,
+ * a window that fits in shared memory and at most 16,383 predecessors per event. */
+int mcd_gradient_host(mcd_dag *dag, int64_t seed0, int64_t n, double *objective, double *grad_earliest,
+                      double *grad_base);
+
+/* ---- Serving: continuous batching of statistics requests (no reference counterpart) ----
+ * submit() copies a request (a DAG, its generator, seeds seed0 .. seed0+n-1) and
+ * returns a ticket at once; host threads compile the DAGs; a scheduler thread
+ * admits compiled requests while their device memory fits memory_budget and,
+ * whenever one of n_streams slots is free, runs everything admitted as one
+ * persistent batch.  A request's statistics equal those of the same request run
+ * alone with mcd_stats_*.  Requests whose window does not fit in shared memory
+ * are rejected.  wait() returns done = 1 and the statistics (and the latency
+ * from submit to completion) when the request has finished, done = 0 when it is
+ * still pending after wait_ms, or the request's error. */
+typedef struct mcd_server mcd_server;
+typedef struct mcd_server_options {
+    int64_t memory_budget;    /* device bytes the admitted requests may hold */
+    int32_t n_streams;        /* batches in flight at once, 1..16 */
+    int32_t n_warps;          /* warps per CTA for every request, 1..16 */
+    int32_t max_batch;        /* requests per launch, 0 = no limit */
+    int32_t compile_threads;  /* host threads compiling submitted DAGs */
+} mcd_server_options;
+typedef struct mcd_server_info {
+    int64_t completed, batches, queued, running, bytes_in_use;
+} mcd_server_info;
+int mcd_server_create(const mcd_server_options *opt, mcd_server **out);
+void mcd_server_destroy(mcd_server *server);
+int mcd_server_submit(mcd_server *server, const mcd_dag_desc *desc, const mcd_generator *gen, int64_t seed0,
+                      int64_t n, int64_t *ticket);
+int mcd_server_wait(mcd_server *server, int64_t ticket, double wait_ms, const mcd_stats *host, int32_t *done,
+                    double *latency_ms);
+int mcd_server_counters(mcd_server *server, mcd_server_info *info);
 
 /* ---- Pinned host memory ---- */
 int mcd_host_alloc(size_t bytes, void **out);

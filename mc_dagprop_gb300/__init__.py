@@ -13,6 +13,7 @@ try:
     from .monte_carlo import (
         Activity,
         Batch,
+        Server,
         DagContext,
         Event,
         EventTimestamp,
@@ -29,6 +30,7 @@ except ImportError as exc:  # the compiled module is missing: fail loudly
 
 __all__ = [
     "Batch",
+    "Server",
     "GenericDelayGenerator",
     "DagContext",
     "SimResult",

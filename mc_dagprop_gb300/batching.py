@@ -1,10 +1,13 @@
-"""Batched runs of many DAGs in one persistent launch, with a small autotuner.
+"""Batched runs of many DAGs in persistent launches, with a small autotuner.
 
-A batch compiles every DAG with the same number of warps per CTA (the CTA size
-of the persistent launch) and runs all (DAG, 32-sample tile) work items in one
-CUDA graph (``mc_dagprop_gb300.Batch``).  The warps per CTA trade work per
-stage against barrier and idle time: wide DAGs want many warps, narrow ones few.
-``tune_warps`` times the candidates on a calibration subset of the batch and
+A ``Batch`` compiles every DAG with the same number of warps per CTA (the CTA
+size of its persistent launch) and runs all (DAG, 32-sample tile) work items in
+one CUDA graph.  The warps per CTA trade work per stage against barrier and idle
+time: wide DAGs want many warps, narrow ones few (and more CTAs per SM).
+``BatchRunner`` therefore splits a mixed stream into width classes -- by the
+warps the compiler would pick for each DAG alone -- and runs one batch per class,
+all launched together on their own streams so their CTAs share the SMs.  For each
+class ``tune_warps`` times candidate warp counts on a calibration subset and
 keeps the fastest; results are cached per shape class in a JSON file
 (``$MCD_AUTOTUNE_CACHE``, default ``~/.cache/mc_dagprop_gb300/autotune.json``).
 """
@@ -28,10 +31,12 @@ def _cache_path() -> str:
                           os.path.join(os.path.expanduser("~"), ".cache", "mc_dagprop_gb300", "autotune.json"))
 
 
-def shape_class(flats: list, ns: list) -> str:
+def shape_class(flats: list, ns: list, widths: list | None = None) -> str:
     """Coarse key of a batch: log2 of the mean events, mean level width and mean samples."""
     ev = np.mean([len(f["earliest"]) for f in flats])
-    width = np.mean([len(f["earliest"]) / max(1, _levels(f)) for f in flats])
+    if widths is None:
+        widths = [len(f["earliest"]) / max(1, _levels(f)) for f in flats]
+    width = np.mean(widths)
     return f"E{int(round(math.log2(max(ev, 1))))}-W{int(round(math.log2(max(width, 1))))}-S{int(round(math.log2(max(np.mean(ns), 1))))}"
 
 
@@ -55,6 +60,11 @@ def compile_dag(flat: dict, gen: list, n_warps: int = 0):
         flat["pred_offsets"], flat["pred_src"], flat["pred_act"], flat["max_delay"], g, n_warps=n_warps)
 
 
+def width_class(auto_warps: int) -> int:
+    """Width class of a DAG from the warps the compiler picks for it alone."""
+    return 4 if auto_warps <= 4 else (8 if auto_warps <= 8 else 16)
+
+
 def _time_batch(props, seed0, ns, reps: int = 2) -> float:
     b = _core.Batch(props, seed0, ns)
     b.run()  # records the graph
@@ -65,10 +75,10 @@ def _time_batch(props, seed0, ns, reps: int = 2) -> float:
 
 
 def tune_warps(flats: list, gens: list, ns: list, candidates=CANDIDATE_WARPS, sample_cap: int = 4096,
-               subset: int = 48, use_cache: bool = True) -> int:
+               subset: int = 48, use_cache: bool = True, widths: list | None = None) -> int:
     """Warps per CTA for a batch: the fastest candidate on up to `subset` DAGs of
     the batch (spread over its sizes) with samples capped at `sample_cap`."""
-    key = shape_class(flats, ns)
+    key = "w" + "-".join(str(c) for c in candidates) + ":" + shape_class(flats, ns, widths)
     path = _cache_path()
     cache = {}
     if use_cache and os.path.exists(path):
@@ -99,19 +109,57 @@ def tune_warps(flats: list, gens: list, ns: list, candidates=CANDIDATE_WARPS, sa
 
 class BatchRunner:
     """Compiles a list of (flat DAG, generator, samples, seed0) and runs them as one
-    batch; ``n_warps=None`` asks the autotuner."""
+    batch per width class (``n_warps`` given: a single batch with that many warps;
+    ``tune=True``: each class's warps from the autotuner)."""
 
-    def __init__(self, items: list, n_warps: int | None = None, use_cache: bool = True):
+    def __init__(self, items: list, n_warps: int | None = None, tune: bool = True, use_cache: bool = True):
         flats = [it[0] for it in items]
         gens = [it[1] for it in items]
         self.ns = [int(it[2]) for it in items]
         self.seed0 = [int(it[3]) for it in items]
-        self.n_warps = n_warps or tune_warps(flats, gens, self.ns, use_cache=use_cache)
-        self.props = [compile_dag(f, g, self.n_warps) for f, g in zip(flats, gens)]
-        self.batch = _core.Batch(self.props, self.seed0, self.ns)
+        if n_warps:
+            classes = {n_warps: list(range(len(items)))}
+            warps = {n_warps: n_warps}
+        else:
+            classes = {}
+            widths = []
+            for i, (f, g) in enumerate(zip(flats, gens)):
+                info = compile_dag(f, g).info()
+                widths.append(info["n_events"] / max(1, info["n_levels"]))
+                classes.setdefault(width_class(info["n_warps"]), []).append(i)
+            warps = {}
+            for c, idx in classes.items():
+                cand = tuple(sorted({max(1, c // 2), c, min(16, 2 * c)}))
+                warps[c] = (tune_warps([flats[i] for i in idx], [gens[i] for i in idx], [self.ns[i] for i in idx],
+                                       candidates=cand, use_cache=use_cache, widths=[widths[i] for i in idx])
+                            if tune else c)
+        self.props = [None] * len(items)
+        self.where = {}
+        self.batches = []
+        for c in sorted(classes):
+            idx = classes[c]
+            props = [compile_dag(flats[i], gens[i], warps[c]) for i in idx]
+            for j, i in enumerate(idx):
+                self.props[i] = props[j]
+                self.where[i] = (len(self.batches), j)
+            self.batches.append((warps[c], idx, _core.Batch(props, [self.seed0[i] for i in idx],
+                                                             [self.ns[i] for i in idx])))
+
+    @property
+    def classes(self) -> list:
+        """(warps per CTA, DAG count, work items) of each class batch."""
+        return [(w, len(idx), b.items) for w, idx, b in self.batches]
 
     def run(self, wait: bool = True) -> None:
-        self.batch.run(wait)
+        for _, _, b in self.batches:  # one launch per class, all in flight together
+            b.run(False)
+        if wait:
+            self.sync()
+
+    def sync(self) -> None:
+        for _, _, b in self.batches:
+            b.sync()
 
     def stats(self, i: int, hist: bool = False) -> dict:
-        return self.batch.stats(i, hist)
+        k, j = self.where[i]
+        return self.batches[k][2].stats(j, hist)

@@ -1,0 +1,145 @@
+// mcd_adjoint.cu -- pathwise gradient of the expected total tardiness
+//   J = mean over samples of sum over events of (realized - earliest)
+// with respect to every event's earliest time and every link's base duration.
+//
+// Forward (k_propagate<..., ADJ>, mcd_device.cuh) records for each event and
+// sample which predecessor won the maximum, whether the bound clamped it, and
+// d(duration)/d(base) of that link.  Along the winning chain realized times add
+// up with slope 1, so for one sample
+//   dJ/d realized_e * S = cnt_e = [realized_e > earliest_e] + sum of cnt_c over
+//                         events c whose unclamped winning predecessor is e,
+// an integer.  The backward kernel walks the stages in reverse, keeping cnt of
+// the events still to be visited in a shared-memory window (the forward
+// window's slots: an event's live range is the same in both directions), and
+// accumulates exactly, as integers:
+//   grad_earliest_e * S = sum_s (cnt_e [no predecessor won, or clamped] - [delayed])
+//   grad_base_l * S     = sum_s cnt_e * d(duration_l)/d(base_l)   (l the winning link)
+// the second in fixed point (2^-20).
+#include "mcd_device.cuh"
+
+namespace mcd {
+
+// One CTA per tile of 32 samples; all warps split each stage's events, stages
+// from last to first.  Shared memory: [counts: window_slots x 32 uint32][stage
+// buffer 0][stage buffer 1][tables][2 mbarriers] -- the forward layout, whose
+// window rows are twice the size the counts need.
+__global__ void __launch_bounds__(768) k_adjoint(const KArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint32_t *cnt = reinterpret_cast<uint32_t *>(smem);
+    char *stage_buf0 = reinterpret_cast<char *>(smem + a.smem_stage_off);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + a.smem_bar_off);
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int NW = a.n_warps;
+    const int64_t s = (int64_t)blockIdx.x * kTile + lane;
+    const bool active = s < a.n;
+    for (int i = threadIdx.x; i < a.window_slots * kTile; i += blockDim.x) cnt[i] = 0u;
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const int NS = a.n_stages;
+    if (threadIdx.x == 0) {
+        if (NS > 0) stage_issue(a, NS - 1, stage_buf0, &bars[0]);
+        if (NS > 1) stage_issue(a, NS - 2, stage_buf0 + a.stage_bytes, &bars[1]);
+    }
+    for (int j = 0; j < NS; ++j) {  // j-th stage from the end
+        const int l = NS - 1 - j;
+        const int b = j & 1;
+        const char *buf = stage_buf0 + b * a.stage_bytes;
+        const bool ok = stage_wait(&bars[b], (uint32_t)((j >> 1) & 1), a.err);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0 && j + 1 < NS) stage_wait(&bars[b ^ 1], (uint32_t)(((j + 1) >> 1) & 1), a.err);
+            __syncthreads();
+            return;
+        }
+        const int4 meta = __ldg(reinterpret_cast<const int4 *>(a.stage_meta) + l);
+        const EvRec *sev = meta.y >= 0 ? reinterpret_cast<const EvRec *>(buf) : a.ev + meta.x;
+        const PredRec *spred = meta.y >= 0 ? reinterpret_cast<const PredRec *>(buf + a.stage_pred_off)
+                                           : a.pred + meta.z;
+        const int ib = __ldg(&a.wk_off[l * NW + warp]) - meta.x;
+        const int ie = __ldg(&a.wk_off[l * NW + warp + 1]) - meta.x;
+        for (int i = ib; i < ie; ++i) {
+            const EvRec ev = sev[i];
+            const int64_t o = (int64_t)ev.user * a.ld + s;
+            const uint32_t code = active ? (uint32_t)a.adj_code[o] : kAdjNone;
+            const float dfac = active ? a.adj_dfac[o] : 0.0f;
+            const uint32_t k = code & kAdjNone;
+            const bool clamped = (code & kAdjClamped) != 0u;
+            const bool delayed = (code & kAdjDelayed) != 0u;
+            uint32_t c = delayed ? 1u : 0u;
+            if (ev.slot >= 0) {  // read and clear: the slot's next tenant starts from zero
+                c += cnt[ev.slot * kTile + lane];
+                cnt[ev.slot * kTile + lane] = 0u;
+            }
+            if (!active) c = 0u;
+            long long ge = ((k == kAdjNone || clamped) ? (long long)c : 0ll) - (delayed ? 1ll : 0ll);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) ge += __shfl_xor_sync(0xFFFFFFFFu, ge, off);
+            if (lane == 0 && ge != 0) atomicAdd(reinterpret_cast<unsigned long long *>(&a.grad_e[ev.user]),
+                                                (unsigned long long)ge);
+            if (k != kAdjNone && !clamped && c != 0u) {
+                const PredRec pr = spred[ev.pred_begin - meta.z + (int)k];
+                if (pr.src_slot >= 0) atomicAdd(&cnt[pr.src_slot * kTile + lane], c);
+                if (pr.link >= 0 && dfac != 0.0f) {
+                    const long long gl = __float2ll_rn((float)c * dfac * (float)(1 << kAdjDfacShift));
+                    atomicAdd(reinterpret_cast<unsigned long long *>(&a.grad_l[pr.link]), (unsigned long long)gl);
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && j + 2 < NS) stage_issue(a, l - 2, stage_buf0 + b * a.stage_bytes, &bars[b]);
+    }
+}
+
+template <bool POSITIVE>
+__global__ void __launch_bounds__(768) k_adjoint_forward(const KArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    propagate_tile<false, true, false, POSITIVE, true>(a, (int64_t)blockIdx.x, nullptr, a.ld, false, smem,
+                                                       reinterpret_cast<uint64_t *>(smem + a.smem_bar_off), false);
+}
+
+// grad_earliest[e] = grad_e[e] / n, grad_base[l] = grad_l[l] 2^-20 / n, and the
+// objective sum_e acc[e] 2^-q / n (one thread).
+__global__ void k_adjoint_finish(const long long *grad_e, const long long *grad_l, const unsigned long long *acc,
+                                 int32_t E, int32_t L, int64_t n, int32_t q, double *g_earliest, double *g_base,
+                                 double *objective) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double dn = (double)n;
+    if (i < E && g_earliest) g_earliest[i] = (double)grad_e[i] / dn;
+    if (i < L && g_base) g_base[i] = ldexp((double)grad_l[i], -kAdjDfacShift) / dn;
+    if (i == 0 && objective) {
+        double total = 0.0;
+        for (int e = 0; e < E; ++e) total += ldexp((double)(long long)acc[e], -q);
+        *objective = total / dn;
+    }
+}
+
+cudaError_t launch_adjoint(const KArgs &a, cudaStream_t st) {
+    if (a.n <= 0) return cudaSuccess;
+    const dim3 grid((unsigned)((a.n + kTile - 1) / kTile)), block((unsigned)(a.n_warps * 32));
+    const size_t smem = (size_t)a.smem_total;
+    void (*fwd)(const KArgs) = a.positive ? k_adjoint_forward<true> : k_adjoint_forward<false>;
+    cudaError_t e = raise_smem_limit((const void *)fwd, smem);
+    if (e != cudaSuccess) return e;
+    fwd<<<grid, block, smem, st>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = raise_smem_limit((const void *)k_adjoint, smem);
+    if (e != cudaSuccess) return e;
+    k_adjoint<<<grid, block, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_finish(const long long *grad_e, const long long *grad_l, const unsigned long long *acc,
+                                  int32_t E, int32_t L, int64_t n, int32_t q, double *g_earliest, double *g_base,
+                                  double *objective, cudaStream_t st) {
+    const int m = E > L ? E : L;
+    k_adjoint_finish<<<(unsigned)((m + 255) / 256 + 1), 256, 0, st>>>(grad_e, grad_l, acc, E, L, n, q, g_earliest,
+                                                                       g_base, objective);
+    return cudaGetLastError();
+}
+
+}  // namespace mcd

@@ -169,6 +169,7 @@ int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0,
         B->args.counter = counter;
         B->args.scratch = scratch;
         B->args.scratch_stride = (int64_t)max_E_global * kTile;
+        B->args.smem_bytes = (int32_t)B->smem;
         *out = B;
     });
     if (rc != MCD_OK && B) {

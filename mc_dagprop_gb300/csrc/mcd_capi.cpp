@@ -87,8 +87,12 @@ void check_device_error(mcd_dag *g) {
         cuda_check(cudaMemset(g->d_err, 0, sizeof(int32_t)), "error flag reset");
         if (flags & ERR_GAMMA_REJECTION)
             throw McdError(MCD_ERR_DEVICE,
-                           "gamma sampler: truncation at max_scale rejected 8192 consecutive draws; "
+                           "gamma sampler: truncation at max_scale rejected 4096 consecutive attempts; "
                            "max_scale is too small for this shape/scale");
+        if (flags & ERR_STAGE_TIMEOUT)
+            throw McdError(MCD_ERR_DEVICE, "a staged record copy did not complete within the wait limit");
+        if (flags & ERR_LAYOUT)
+            throw McdError(MCD_ERR_DEVICE, "a DAG's shared-memory layout exceeds its launch's shared memory");
         throw McdError(MCD_ERR_DEVICE, "kernel reported error flags " + std::to_string(flags));
     }
 }

@@ -96,6 +96,101 @@ static void check_table(const DistSpec &d) {
     if (!(sum > 0.0)) throw McdError(MCD_ERR_INVALID, "empirical weights must not all be zero");
 }
 
+// The invariants every kernel access relies on, checked on the compiled DAG:
+// shared-memory regions in order, aligned and within the budget; staged
+// records within their buffer; warp chunks covering each stage; every source in
+// an earlier stage; and window slots reused only after the stage of the last
+// read of the previous tenant.  A violation is a compiler defect and fails the
+// compile rather than a launch.
+static void verify_layout(const HostDag &H) {
+    auto fail = [](const char *what) {
+        throw McdError(MCD_ERR_RUNTIME, std::string("internal layout check failed: ") + what);
+    };
+    const int64_t E = H.E, P = (int64_t)H.pred.size(), NW = H.n_warps, NS = H.n_stages;
+    if ((int64_t)H.ev.size() != E) fail("event records");
+    if ((int64_t)H.stage_meta.size() != NS * 4 || (int64_t)H.wk_off.size() != NS * NW + 1) fail("stage tables");
+    // shared memory: [window][stage buffer 0][stage buffer 1][tables][2 mbarriers]
+    const int64_t win = H.win_smem ? (int64_t)H.window_slots * kTile * (int64_t)sizeof(double) : 0;
+    const int64_t tables = H.tables_in_smem ? (int64_t)(H.dist.size() * sizeof(DistParam) +
+                                                        H.alias.size() * sizeof(AliasEntry))
+                                            : 0;
+    if (H.smem_stage_off < win || H.smem_stage_off % 16) fail("stage buffer offset");
+    if (H.stage_pred_off % 16 || H.stage_bytes % 16 || H.stage_pred_off > H.stage_bytes) fail("stage buffer size");
+    if (H.smem_tables_off < (int64_t)H.smem_stage_off + 2 * (int64_t)H.stage_bytes || H.smem_tables_off % 16)
+        fail("table offset");
+    if (H.smem_bar_off % 8 || H.smem_bar_off < H.smem_tables_off + tables) fail("barrier offset");
+    if (H.smem_total < (int64_t)H.smem_bar_off + 16 || H.smem_total > (int64_t)kSmemMax) fail("shared memory total");
+    // records
+    std::vector<int32_t> stage_of((size_t)E, -1);  // by caller index
+    std::vector<char> seen((size_t)E, 0);
+    int64_t ev_next = 0, pred_next = 0;
+    for (int64_t st = 0; st < NS; ++st) {
+        const int32_t *m = &H.stage_meta[(size_t)st * 4];
+        const int64_t first = m[0], nev = m[1] >= 0 ? m[1] : -(int64_t)m[1], pfirst = m[2], npred = m[3];
+        if (first != ev_next || nev <= 0 || first + nev > E || pfirst != pred_next) fail("stage ranges");
+        if (m[1] >= 0 && (nev * (int64_t)sizeof(EvRec) > H.stage_pred_off ||
+                          H.stage_pred_off + npred * (int64_t)sizeof(PredRec) > H.stage_bytes))
+            fail("staged records exceed the buffer");
+        if (H.wk_off[(size_t)(st * NW)] != first) fail("warp chunk start");
+        for (int64_t w = 0; w < NW; ++w)
+            if (H.wk_off[(size_t)(st * NW + w + 1)] < H.wk_off[(size_t)(st * NW + w)]) fail("warp chunk order");
+        if (H.wk_off[(size_t)((st + 1) * NW)] != first + nev) fail("warp chunk end");
+        int64_t pos = pfirst;
+        for (int64_t i = first; i < first + nev; ++i) {
+            const EvRec &r = H.ev[(size_t)i];
+            if (r.user < 0 || r.user >= E || seen[(size_t)r.user]) fail("event permutation");
+            seen[(size_t)r.user] = 1;
+            stage_of[(size_t)r.user] = (int32_t)st;
+            if (r.pred_begin != pos || r.pred_end < r.pred_begin || r.pred_end > pfirst + npred) fail("pred ranges");
+            pos = r.pred_end;
+        }
+        if (pos != pfirst + npred) fail("stage pred count");
+        ev_next = first + nev;
+        pred_next = pfirst + npred;
+    }
+    if (ev_next != E || pred_next != P) fail("stage coverage");
+    // sources and window slots, in execution order
+    std::vector<int32_t> slot_of((size_t)E, -1), tenant((size_t)std::max(H.window_slots, 1), -1),
+        last_read((size_t)std::max(H.window_slots, 1), -1);
+    for (int64_t i = 0; i < E; ++i) slot_of[(size_t)H.ev[(size_t)i].user] = H.ev[(size_t)i].slot;
+    for (int64_t st = 0, i = 0; st < NS; ++st) {
+        const int64_t end = H.wk_off[(size_t)((st + 1) * NW)];
+        for (; i < end; ++i) {
+            const EvRec &r = H.ev[(size_t)i];
+            for (int64_t k = r.pred_begin; k < r.pred_end; ++k) {
+                const PredRec &p = H.pred[(size_t)k];
+                if (p.src_user < 0 || p.src_user >= E || stage_of[(size_t)p.src_user] >= st) fail("source order");
+                if (p.link < -1 || p.link >= H.L) fail("link index");
+                const int kind = p.kd & KD_KIND_MASK;
+                if (kind < K_FIXED || kind > K_EMP_REL) fail("delay kind");
+                if (kind != K_FIXED) {
+                    const int64_t di = (int64_t)(p.kd >> 8);
+                    if (di < 0 || di >= (int64_t)H.dist.size()) fail("distribution index");
+                    const DistParam &dp = H.dist[(size_t)di];
+                    if ((kind == K_EMP_ABS || kind == K_EMP_REL) &&
+                        (dp.tab_n <= 0 || dp.tab_off < 0 || (int64_t)dp.tab_off + dp.tab_n > (int64_t)H.alias.size()))
+                        fail("alias table range");
+                }
+                if (!H.win_smem) {
+                    if (p.src_slot != -1) fail("window slot without a window");
+                    continue;
+                }
+                if (p.src_slot < 0 || p.src_slot >= H.window_slots || p.src_slot != slot_of[(size_t)p.src_user] ||
+                    tenant[(size_t)p.src_slot] != p.src_user)
+                    fail("window slot of a source");
+                last_read[(size_t)p.src_slot] = std::max(last_read[(size_t)p.src_slot], (int32_t)st);
+            }
+            if (r.slot >= 0) {
+                if (!H.win_smem || r.slot >= H.window_slots || last_read[(size_t)r.slot] >= st)
+                    fail("window slot reuse");
+                tenant[(size_t)r.slot] = r.user;
+            } else if (r.slot != -1) {
+                fail("window slot");
+            }
+        }
+    }
+}
+
 void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int32_t n_warps) {
     // ---- 1) distributions: the last add_* per type wins (README semantics of dist_map_)
     std::unordered_map<int32_t, size_t> type_spec;
@@ -214,6 +309,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
     H.L = L;
     H.link_kd.assign((size_t)L, K_FIXED);
     H.link_v.assign((size_t)L, 0.0);  // gaps: duration 0, no delay
+    H.link_dv.assign((size_t)L, 0.0f);
     for (int32_t k = 0; k < d.n_activities; ++k) {
         const int32_t l = d.act_idx[k];
         const double base = d.act_duration[k];
@@ -221,6 +317,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         if (it == form.end()) {
             H.link_kd[l] = K_FIXED;
             H.link_v[l] = base;
+            H.link_dv[l] = 1.0f;
             continue;
         }
         const TypeForm &f = it->second;
@@ -230,6 +327,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
             else extra = f.relative ? f.factor * base : f.factor;  // _core.cpp:125, 140
             H.link_kd[l] = K_FIXED;
             H.link_v[l] = base + extra;                           // _core.cpp:328
+            H.link_dv[l] = (float)(f.fixed == 1 ? 1.0 + f.factor : (f.relative ? 1.0 + f.factor : 1.0));
         } else {
             H.link_kd[l] = f.kind | (f.dist << 8);
             H.link_v[l] = base;
@@ -289,6 +387,9 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
     for (int32_t e = 0; e < E; ++e) n_levels = std::max(n_levels, level[e] + 1);
     H.n_levels = n_levels;
 
+    H.max_preds = 0;
+    for (int32_t e = 0; e < E; ++e) H.max_preds = std::max<int64_t>(H.max_preds, tlen[e]);
+
     // ---- 5) last level at which each event is read
     std::vector<int32_t> last_use((size_t)E, -1);
     for (int32_t e = 0; e < E; ++e)
@@ -343,16 +444,18 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
     if (n_warps > 0) nw = n_warps;
     nw = std::max(1, std::min(kMaxWarps, nw));
     H.n_warps = nw;
+    // relative cost of an edge by delay kind (kernel time per edge, fixed = 1)
+    // and of an event's own work
     auto kind_cost = [&](int32_t l) -> double {
         if (l >= L) return 1.0;
         switch (H.link_kd[l] & KD_KIND_MASK) {
             case K_FIXED: return 1.0;
-            case K_EXP: return 5.0;
-            case K_GAMMA: return 12.0;
-            default: return 4.0;
+            case K_EXP: return 2.4;
+            case K_GAMMA: return 3.5;
+            default: return 2.0;
         }
     };
-    std::vector<double> cost((size_t)E, 2.0);
+    std::vector<double> cost((size_t)E, 1.0);
     for (int32_t e = 0; e < E; ++e)
         for (int64_t k = 0; k < tlen[e]; ++k) cost[e] += kind_cost(d.pred_act[tstart[e] + k]);
 
@@ -500,10 +603,12 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
                 p.link = -1;
                 p.kd = K_FIXED;
                 p.v = 0.0;
+                p.dv = 0.0f;
             } else {
                 p.link = l;
                 p.kd = H.link_kd[l];
                 p.v = H.link_v[l];
+                p.dv = H.link_dv[l];
                 if (!written[l]) {  // the first reference stores the link's duration row
                     p.kd |= KD_WRITE;
                     written[l] = 1;
@@ -532,6 +637,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         if (!referenced[l]) ++H.n_orphan;
         if (!written[l]) H.aux.push_back(LinkRec{l, H.link_kd[l], H.link_v[l]});
     }
+    verify_layout(H);
 }
 
 // Ticks of 2^-q seconds: every |time| * 2^q must stay below 2^62, and the sum

@@ -19,6 +19,7 @@
 #include <cstdint>
 #include <limits>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <unordered_map>
 #include <utility>
@@ -308,6 +309,22 @@ class Propagator {
         d["n"] = n;
         return d;
     }
+    py::dict gradient(int64_t n, int64_t seed0) {
+        py::array_t<double> ge(E_), gb(L_);
+        double obj = 0.0;
+        double *gp = ge.mutable_data(), *bp = gb.mutable_data();
+        int rc;
+        {
+            py::gil_scoped_release release;
+            rc = mcd_gradient_host(dag_.get(), seed0, n, &obj, gp, bp);
+        }
+        raise_status(rc);
+        py::dict d;
+        d["objective"] = obj;
+        d["grad_earliest"] = ge;
+        d["grad_base"] = gb;
+        return d;
+    }
     py::dict info() const {
         mcd_dag_info i{};
         raise_status(mcd_dag_get_info(dag_.get(), &i));
@@ -408,6 +425,95 @@ class Batch {
     std::vector<Propagator *> props_;
     std::vector<py::object> keep_;  // the propagators outlive the batch
     std::shared_ptr<mcd_batch> b_;
+};
+
+// The continuous-batching server: submit requests, wait for their statistics.
+class Server {
+   public:
+    Server(int64_t budget, int n_streams, int n_warps, int max_batch, int compile_threads) {
+        mcd_server_options o{budget, n_streams, n_warps, max_batch, compile_threads};
+        mcd_server *p = nullptr;
+        raise_status(mcd_server_create(&o, &p));
+        s_.reset(p, mcd_server_destroy);
+    }
+    int64_t submit(py::handle earliest, py::handle act_idx, py::handle act_duration, py::handle act_type,
+                   py::handle target, py::handle pred_offsets, py::handle pred_src, py::handle pred_act,
+                   double max_delay, const Generator &g, int64_t seed0, int64_t n) {
+        FlatDag f;
+        f.earliest = to_vec<double>(earliest);
+        f.act_idx = to_vec<int32_t>(act_idx);
+        f.act_duration = to_vec<double>(act_duration);
+        f.act_type = to_vec<int32_t>(act_type);
+        f.target = to_vec<int32_t>(target);
+        f.pred_offsets = to_vec<int64_t>(pred_offsets);
+        f.pred_src = to_vec<int32_t>(pred_src);
+        f.pred_act = to_vec<int32_t>(pred_act);
+        f.max_delay = max_delay;
+        if (f.act_duration.size() != f.act_idx.size() || f.act_type.size() != f.act_idx.size() ||
+            f.pred_offsets.size() != f.target.size() + 1 || f.pred_offsets.front() != 0 ||
+            f.pred_offsets.back() != (int64_t)f.pred_src.size() || f.pred_src.size() != f.pred_act.size())
+            throw py::value_error("inconsistent DAG arrays");
+        const mcd_dag_desc d = f.desc();
+        int64_t t = 0;
+        int rc;
+        {
+            py::gil_scoped_release release;
+            rc = mcd_server_submit(s_.get(), &d, g.g.get(), seed0, n, &t);
+        }
+        raise_status(rc);
+        std::lock_guard<std::mutex> lk(mu_);
+        sizes_[t] = (int64_t)f.earliest.size();
+        return t;
+    }
+    py::object wait(int64_t ticket, double timeout_ms) {
+        int64_t E;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            auto it = sizes_.find(ticket);
+            if (it == sizes_.end()) throw py::value_error("unknown ticket");
+            E = it->second;
+        }
+        py::array_t<double> mean(E), p50(E), p90(E), p99(E), pot(E);
+        mcd_stats st{mean.mutable_data(), p50.mutable_data(), p90.mutable_data(), p99.mutable_data(),
+                     pot.mutable_data(), nullptr};
+        int32_t done = 0;
+        double lat = 0.0;
+        int rc;
+        {
+            py::gil_scoped_release release;
+            rc = mcd_server_wait(s_.get(), ticket, timeout_ms, &st, &done, &lat);
+        }
+        if (rc != MCD_OK || done) {
+            std::lock_guard<std::mutex> lk(mu_);
+            sizes_.erase(ticket);
+        }
+        if (rc != MCD_OK) throw std::runtime_error(mcd_last_error());
+        if (!done) return py::none();
+        py::dict d;
+        d["mean"] = mean;
+        d["p50"] = p50;
+        d["p90"] = p90;
+        d["p99"] = p99;
+        d["p_on_time"] = pot;
+        d["latency_ms"] = lat;
+        return std::move(d);
+    }
+    py::dict counters() {
+        mcd_server_info i{};
+        raise_status(mcd_server_counters(s_.get(), &i));
+        py::dict d;
+        d["completed"] = i.completed;
+        d["batches"] = i.batches;
+        d["queued"] = i.queued;
+        d["running"] = i.running;
+        d["bytes_in_use"] = i.bytes_in_use;
+        return d;
+    }
+
+   private:
+    std::shared_ptr<mcd_server> s_;
+    std::mutex mu_;
+    std::unordered_map<int64_t, int64_t> sizes_;
 };
 
 }  // namespace mcd_py
@@ -594,6 +700,9 @@ PYBIND11_MODULE(_core, m) {
              py::arg("seed0") = 0, py::arg("hist") = false,
              "Per-event statistics over samples (seeds, or seed0..seed0+n-1) computed on the GPU: "
              "dict of mean, p50, p90, p99, p_on_time (and the raw histogram when hist=True)")
+        .def("gradient", &Propagator::gradient, py::arg("n"), py::arg("seed0") = 0,
+             "Pathwise gradient of J = mean_s sum_e (realized - earliest) over seeds seed0..seed0+n-1: "
+             "dict of objective, grad_earliest (per event), grad_base (per link index)")
         .def("info", &Propagator::info, "Compiled-DAG facts")
         .def("_handle", [](const Propagator &p) { return (uintptr_t)p.handle(); });
 
@@ -609,4 +718,17 @@ PYBIND11_MODULE(_core, m) {
         .def_property_readonly("items", &Batch::items, "Work items (DAG, 32-sample tile)")
         .def_property_readonly("grid", &Batch::grid, "CTAs of the persistent launch")
         .def_property_readonly("stream", &Batch::stream, "The batch's CUDA stream");
+
+    py::class_<Server>(m, "Server")
+        .def(py::init<int64_t, int, int, int, int>(), py::arg("memory_budget") = (int64_t)64 << 30,
+             py::arg("n_streams") = 2, py::arg("n_warps") = 8, py::arg("max_batch") = 0,
+             py::arg("compile_threads") = 4,
+             "Continuous-batching statistics server on the current GPU")
+        .def("submit", &Server::submit, py::arg("earliest"), py::arg("act_idx"), py::arg("act_duration"),
+             py::arg("act_type"), py::arg("target"), py::arg("pred_offsets"), py::arg("pred_src"),
+             py::arg("pred_act"), py::arg("max_delay"), py::arg("generator"), py::arg("seed0"), py::arg("n"),
+             "Submit a request (flat DAG, generator, seeds seed0..seed0+n-1); returns a ticket")
+        .def("wait", &Server::wait, py::arg("ticket"), py::arg("timeout_ms") = 0.0,
+             "Statistics of a finished request (dict with latency_ms), None while pending")
+        .def("counters", &Server::counters, "completed, batches, queued, running, bytes_in_use");
 }

@@ -30,6 +30,11 @@
 
 namespace mcd {
 
+// Raises a kernel's dynamic shared-memory limit to at least `smem` bytes and
+// never lowers it: kernels captured in graphs and launches from other threads
+// keep the limit they were recorded with.
+cudaError_t raise_smem_limit(const void *fn, size_t smem);
+
 // ---------------------------------------------------------------- Philox4x32-10
 // Counter mode under one fixed key: the 128-bit counter is (seed low, seed high,
 // link, salt ^ attempt), so a draw depends only on (sample seed, link, attempt)
@@ -133,12 +138,14 @@ __device__ __forceinline__ double mul_trunc(double a, long long gb) {
 // Exponential with mean lambda_, redrawn above max_scale (_core.cpp:83-89).  The
 // redraw loop is replaced by the inverse CDF of the truncated law, which is the
 // same distribution: X = -lambda_ * log(1 - c u), c = 1 - exp(-max_scale/lambda_).
-__device__ __forceinline__ double draw_exponential(const DistParam &p, double base, uint32_t link, uint64_t seed) {
+__device__ __forceinline__ double draw_exponential(const DistParam &p, double base, uint32_t link, uint64_t seed,
+                                                   float &dfac) {
     const U4 r = draw_words(seed, link, 0u, 0u);
     const float w = u01_open0(r.x);       // plays the role of 1 - u
     const float V = fmaf(p.f1, w, p.f2);  // 1 - c (1 - w), in (1-c, 1]
     float X = -p.f0 * __logf(V);
     X = fmaxf(fminf(X, p.f3), 0.0f);
+    dfac = 1.0f + X;
     return mul_trunc(base, one_plus(X));  // base + X * base
 }
 
@@ -149,7 +156,7 @@ __device__ __forceinline__ double draw_exponential(const DistParam &p, double ba
 // Not inlined: it is large, and keeping it out of line keeps the propagation
 // loop's register allocation small.
 static __device__ __noinline__ double draw_gamma(const DistParam &p, double base, uint32_t link, uint64_t seed,
-                                                 int32_t *err) {
+                                                 int32_t *err, float *dfac) {
     const float d = p.f0, cc = p.f1;
     for (uint32_t attempt = 0; attempt < 4096u; ++attempt) {
         const U4 r = draw_words(seed, link, attempt, 0u);
@@ -175,9 +182,11 @@ static __device__ __noinline__ double draw_gamma(const DistParam &p, double base
         }
         X *= p.f3;
         if (X > p.f4) continue;
+        *dfac = 1.0f + X;
         return mul_trunc(base, one_plus(X));
     }
     atomicOr(err, ERR_GAMMA_REJECTION);
+    *dfac = 1.0f + p.f4;
     return mul_trunc(base, one_plus(p.f4));
 }
 
@@ -188,24 +197,32 @@ static __device__ __noinline__ double draw_gamma(const DistParam &p, double base
 // reference's bit pattern: the values are atoms, and any last-bit difference
 // would separate the two discrete distributions.
 __device__ __forceinline__ double draw_empirical(const DistParam &p, const AliasEntry *alias, double base,
-                                                 bool relative, uint32_t link, uint64_t seed) {
+                                                 bool relative, uint32_t link, uint64_t seed, float &dfac) {
     const U4 r = draw_words(seed, link, 0u, 0u);
     const uint32_t j = __umulhi(r.x, (uint32_t)p.tab_n);
     const AliasEntry &e = alias[p.tab_off + j];
     const double val = r.y < e.thresh ? e.v_self : e.v_alias;
+    dfac = relative ? 1.0f + (float)val : 1.0f;
     return relative ? __dadd_rn(base, __dmul_rn(val, base)) : __dadd_rn(base, val);
 }
 
-__device__ __forceinline__ double link_duration(int32_t kd, double v, uint32_t link, uint64_t seed,
-                                                const DistParam *dists, const AliasEntry *alias, int32_t *err) {
+// The link's duration for one sample, and (dfac) its derivative with respect to
+// the base duration: 1 + X for the multiplicative kinds, 1 for absolute tables,
+// the host-computed value (dv) for fixed links.
+__device__ __forceinline__ double link_duration(int32_t kd, double v, float dv, uint32_t link, uint64_t seed,
+                                                const DistParam *dists, const AliasEntry *alias, int32_t *err,
+                                                float &dfac) {
     const int kind = kd & KD_KIND_MASK;
-    if (kind == K_FIXED) return v;
+    if (kind == K_FIXED) {
+        dfac = dv;
+        return v;
+    }
     const DistParam &p = dists[kd >> 8];
     switch (kind) {
-        case K_EXP: return draw_exponential(p, v, link, seed);
-        case K_GAMMA: return draw_gamma(p, v, link, seed, err);
-        case K_EMP_ABS: return draw_empirical(p, alias, v, false, link, seed);
-        default: return draw_empirical(p, alias, v, true, link, seed);
+        case K_EXP: return draw_exponential(p, v, link, seed, dfac);
+        case K_GAMMA: return draw_gamma(p, v, link, seed, err, &dfac);
+        case K_EMP_ABS: return draw_empirical(p, alias, v, false, link, seed, dfac);
+        default: return draw_empirical(p, alias, v, true, link, seed, dfac);
     }
 }
 
@@ -306,6 +323,15 @@ __device__ __forceinline__ void accumulate_stats(const KArgs &a, const EvRec &ev
     }
 }
 
+// The tile's sum of (realized - earliest) ticks into a.acc (objective of the
+// adjoint; the same integer accumulation as the statistics mean).
+__device__ __forceinline__ void accumulate_sum(const KArgs &a, const EvRec &ev, long long lbits, bool active) {
+    long long d = active ? to_ticks(lbits, a.tick_q) - to_ticks(ev.init_bits, a.tick_q) : 0ll;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xFFFFFFFFu, d, off);
+    if ((threadIdx.x & 31) == 0 && d != 0) atomicAdd(&a.acc[ev.user], (unsigned long long)d);
+}
+
 // ---------------------------------------------------------------- propagation
 // Walks the compiled DAG for one tile of 32 samples (the tile's sample s is
 // tile * 32 + lane) with all warps of the CTA.
@@ -319,15 +345,21 @@ __device__ __forceinline__ void accumulate_stats(const KArgs &a, const EvRec &ev
 // Returns false when a staged copy never landed (then every thread returns false).
 //
 // Shared memory: [window: window_slots x 32 doubles][stage buffer 0][stage
-// buffer 1][distribution params][alias table][2 mbarriers].
-template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE>
+// buffer 1][distribution params][alias table][2 mbarriers]; `bars` is that
+// layout's barrier pair, or one fixed pair for every tile of a persistent CTA
+// (a barrier stays where it was initialised: only the same address is
+// invalidated and initialised again between tiles).
+// ADJ: the forward half of the adjoint: per event and sample, the winning
+// predecessor's position, clamp and delay flags and d(duration)/d(base) go to
+// a.adj_code / a.adj_dfac, and (realized - earliest) to the objective sum.
+template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ = false>
 __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, double *rows, int64_t rows_ld,
-                                               bool rows_tile_local, unsigned char *smem, bool reuse) {
+                                               bool rows_tile_local, unsigned char *smem, uint64_t *bars,
+                                               bool reuse) {
     double *win = reinterpret_cast<double *>(smem);
     char *stage_buf0 = reinterpret_cast<char *>(smem + a.smem_stage_off);
     DistParam *s_dist = reinterpret_cast<DistParam *>(smem + a.smem_tables_off);
     AliasEntry *s_alias = reinterpret_cast<AliasEntry *>(smem + a.smem_tables_off + a.n_dist * sizeof(DistParam));
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + a.smem_bar_off);
     const DistParam *dists = a.tables_in_smem ? s_dist : a.dist;
     const AliasEntry *alias = a.tables_in_smem ? s_alias : a.alias;
 
@@ -355,6 +387,10 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
         mbar_init(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    // A persistent CTA's previous tile may have had another layout: its window
+    // stores (generic proxy) can lie where this tile's staged copies (async
+    // proxy) land, so every thread orders its stores before the copies.
+    if (reuse) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (threadIdx.x == 0) {
         if (a.n_stages > 0) stage_issue(a, 0, stage_buf0, &bars[0]);
@@ -382,14 +418,17 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
             const EvRec ev = sev[i];
             long long lk = ev.init_key, lbits = ev.init_bits;
             int32_t cause = -1;
+            uint32_t win_code = kAdjNone;  // ADJ: winner position | clamp flag
+            float win_dfac = 0.0f;
             for (int p = ev.pred_begin - meta.z; p < ev.pred_end - meta.z; ++p) {
                 const PredRec pr = spred[p];
                 double dur;
+                float dfac = 0.0f;
                 if (GIVEN) {
                     dur = (active && pr.link >= 0) ? __ldg(&a.dur_in[(int64_t)pr.link * a.ld_in + s]) : 0.0;
                 } else {
-                    dur = link_duration(pr.kd, pr.v, (uint32_t)pr.link, seed, dists, alias, a.err);
-                    if (!STATS && (pr.kd & KD_WRITE) && a.durations && active)
+                    dur = link_duration(pr.kd, pr.v, pr.dv, (uint32_t)pr.link, seed, dists, alias, a.err, dfac);
+                    if (!STATS && !ADJ && (pr.kd & KD_WRITE) && a.durations && active)
                         a.durations[(int64_t)pr.link * a.ld + s] = dur;
                 }
                 double src;
@@ -401,7 +440,8 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
                 const double t = src + dur;  // the one FP64 add of the edge (_core.cpp:341)
                 long long tb = __double_as_longlong(t);
                 long long tk = order_key<POSITIVE>(tb);
-                if (ev.ub_key < tk) {  // t = std::min(t, ub)
+                const bool clamp = ev.ub_key < tk;
+                if (clamp) {  // t = std::min(t, ub)
                     tk = ev.ub_key;
                     tb = ev.ub_bits;
                 }
@@ -409,26 +449,40 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
                     lk = tk;
                     lbits = tb;
                     cause = pr.src_user;
+                    if (ADJ) {
+                        win_code = (uint32_t)(p - (ev.pred_begin - meta.z)) | (clamp ? kAdjClamped : 0u);
+                        win_dfac = dfac;
+                    }
                 }
             }
             if (ev.ub_key < lk) lbits = ev.ub_bits;  // realized = std::min(latest, ub)
             const double real = __longlong_as_double(lbits);
             if (WIN_SMEM && ev.slot >= 0) win[ev.slot * kTile + lane] = real;
             if (STATS) accumulate_stats(a, ev, lbits, active, active_mask);
+            if (ADJ) {
+                const bool delayed = lk > ev.init_key;  // realized > earliest
+                accumulate_sum(a, ev, lbits, active);
+                if (active) {
+                    const int64_t o = (int64_t)ev.user * a.ld + s;
+                    a.adj_code[o] = (uint16_t)(win_code | (delayed ? kAdjDelayed : 0u));
+                    a.adj_dfac[o] = win_dfac;
+                }
+            }
             if (active) {
                 if (rows) rows[(int64_t)ev.user * rows_ld + rcol] = real;
-                if (!STATS && a.cause) a.cause[(int64_t)ev.user * a.ld + s] = cause;
+                if (!STATS && !ADJ && a.cause) a.cause[(int64_t)ev.user * a.ld + s] = cause;
             }
         }
         __syncthreads();
         if (threadIdx.x == 0 && l + 2 < a.n_stages)
             stage_issue(a, l + 2, stage_buf0 + b * a.stage_bytes, &bars[b]);
     }
-    // Aux pass: duration rows of fixed links and of links no precedence entry references.
-    if (!STATS && !GIVEN && a.durations) {
+    // Aux pass: duration rows of links no precedence entry references.
+    if (!STATS && !ADJ && !GIVEN && a.durations) {
         for (int i = warp; i < a.n_aux; i += NW) {
             const LinkRec lr = a.aux[i];
-            const double dur = link_duration(lr.kd, lr.v, (uint32_t)lr.link, seed, dists, alias, a.err);
+            float dfac;
+            const double dur = link_duration(lr.kd, lr.v, 0.0f, (uint32_t)lr.link, seed, dists, alias, a.err, dfac);
             if (active) a.durations[(int64_t)lr.link * a.ld + s] = dur;
         }
     }
@@ -441,7 +495,8 @@ __global__ void __launch_bounds__(768) k_propagate(const KArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     double *rows = a.realized ? a.realized : a.scratch;  // global realized rows
     if (STATS && WIN_SMEM) rows = nullptr;
-    propagate_tile<GIVEN, WIN_SMEM, STATS, POSITIVE>(a, (int64_t)blockIdx.x, rows, a.ld, false, smem, false);
+    propagate_tile<GIVEN, WIN_SMEM, STATS, POSITIVE>(a, (int64_t)blockIdx.x, rows, a.ld, false, smem,
+                                                     reinterpret_cast<uint64_t *>(smem + a.smem_bar_off), false);
 }
 
 }  // namespace mcd

@@ -55,6 +55,7 @@ struct HostDag {
     int32_t E = 0, L = 0, n_levels = 0, n_warps = 1, window_slots = 0;
     bool win_smem = true;
     bool positive = false;        // all times non-negative and finite
+    int64_t max_preds = 0;        // largest predecessor list
     bool tables_in_smem = true;
     int32_t n_stages = 0, stage_bytes = 0, stage_pred_off = 0;
     int32_t smem_stage_off = 0, smem_tables_off = 0, smem_bar_off = 0, smem_total = 0;
@@ -68,6 +69,7 @@ struct HostDag {
     std::vector<int32_t> wk_off;
     std::vector<int32_t> link_kd;
     std::vector<double> link_v;
+    std::vector<float> link_dv;    // FIXED links: d(duration)/d(base)
     std::vector<double> earliest;  // caller order
     std::vector<double> ub;        // earliest + max_delay, caller order
     double max_delay = 0.0;

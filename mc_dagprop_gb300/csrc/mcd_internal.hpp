@@ -42,7 +42,8 @@ struct alignas(16) PredRec {
                        // past the last link, which has duration 0 (see the compiler)
     int32_t kd;        // kind | KD_WRITE | dist << 8
     double v;          // FIXED: the duration; otherwise the base (minimal_duration)
-    int64_t pad;
+    float dv;          // FIXED: d(duration)/d(base) (1 + factor, 1, or 0 for gaps)
+    int32_t pad;
 };
 
 // A link whose duration row the aux pass stores: a link no precedence entry
@@ -76,6 +77,15 @@ struct alignas(16) AliasEntry {
     uint32_t thresh;
     uint32_t pad[3];
 };
+
+// Adjoint forward record per (event, sample): the winning predecessor's position
+// in the event's list (kAdjNone: no predecessor won, realized = earliest), and
+// flags for "clamped at earliest + max_delay" and "realized > earliest".
+constexpr uint32_t kAdjNone = 0x3FFFu;
+constexpr uint32_t kAdjClamped = 0x4000u;
+constexpr uint32_t kAdjDelayed = 0x8000u;
+constexpr int32_t kAdjMaxPreds = 0x3FFF;     // events with more predecessors are rejected
+constexpr int kAdjDfacShift = 20;            // link gradients accumulate cnt * dfac * 2^20
 
 // Per-event statistics layout: 256 equal bins over [earliest, earliest +
 // max_delay] plus two exact atoms -- realized == earliest (not delayed) and
@@ -123,6 +133,11 @@ struct KArgs {
     double hist_inv_w;            // FP64 fallback: 256 / max_delay, 0 when not finite
     unsigned long long *acc;      // [E] sum of delta ticks (fixed) or FP64 sum bits (fallback)
     uint32_t *hist;               // [E][kHistStride]
+    // adjoint
+    uint16_t *adj_code;           // [E][ld] winner position and flags (forward), read backward
+    float *adj_dfac;              // [E][ld] d(duration)/d(base) of the winning link
+    long long *grad_e;            // [E] sum over samples of the earliest-time derivative (counts)
+    long long *grad_l;            // [L] sum over samples of cnt * dfac * 2^20 per link
 };
 
 // Arguments of the persistent batch kernel.
@@ -133,6 +148,7 @@ struct BatchArgs {
     unsigned int *counter;       // work-queue head, zero before the launch
     double *scratch;             // per-CTA realized rows for DAGs whose window is not on chip
     int64_t scratch_stride;      // doubles per CTA (max events x 32)
+    int32_t smem_bytes;          // dynamic shared memory of the launch (>= every DAG's layout)
 };
 
 // Arguments of the statistics finishing kernel.
@@ -150,7 +166,7 @@ struct FArgs {
 };
 
 // Device error flags.
-enum : int32_t { ERR_GAMMA_REJECTION = 1, ERR_STAGE_TIMEOUT = 2 };
+enum : int32_t { ERR_GAMMA_REJECTION = 1, ERR_STAGE_TIMEOUT = 2, ERR_LAYOUT = 4 };
 
 constexpr int kTile = 32;  // samples per tile: one per lane
 

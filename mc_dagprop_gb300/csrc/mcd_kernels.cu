@@ -5,7 +5,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <mutex>
+#include <utility>
 
 #include "mcd_internal.hpp"
 
@@ -53,10 +55,12 @@ __global__ void k_stats_finish(const FArgs f) {
 }
 
 // The finish of every DAG of a batch in one launch: blockIdx.y selects the DAG.
-__global__ void k_batch_finish(const FArgs *__restrict__ fs) {
-    const FArgs &f = fs[blockIdx.y];
+__global__ void k_batch_finish(const FArgs *__restrict__ fs, int32_t n_dags) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < f.E) finish_event(f, e);
+    for (int32_t d = (int32_t)blockIdx.y; d < n_dags; d += (int32_t)gridDim.y) {
+        const FArgs &f = fs[d];
+        if (e < f.E) finish_event(f, e);
+    }
 }
 
 // ---------------------------------------------------------------- layout change
@@ -78,6 +82,21 @@ __global__ void k_transpose(const T *__restrict__ in, int64_t ld_in, T *__restri
 }
 
 // ---------------------------------------------------------------- launchers
+cudaError_t raise_smem_limit(const void *fn, size_t smem) {
+    if (smem <= 48 * 1024) return cudaSuccess;
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, size_t> limit;  // (kernel, device) -> bytes set
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &cur = limit[{fn, dev}];
+    if (smem <= cur) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) cur = smem;
+    return e;
+}
+
 cudaError_t launch_prop_sample(const KArgs &a, bool win_smem, bool stats, bool positive, dim3 grid, dim3 block,
                                size_t smem, cudaStream_t st);
 cudaError_t launch_prop_given(const KArgs &a, bool win_smem, bool stats, dim3 grid, dim3 block, size_t smem,
@@ -127,7 +146,8 @@ cudaError_t noalloc_scratch(void **ptr, size_t *bytes) {
 
 cudaError_t launch_batch_finish(const FArgs *fs, int32_t n_dags, int32_t max_events, cudaStream_t st) {
     if (n_dags <= 0 || max_events <= 0) return cudaSuccess;
-    k_batch_finish<<<dim3((unsigned)((max_events + 255) / 256), (unsigned)n_dags), 256, 0, st>>>(fs);
+    const unsigned gy = (unsigned)(n_dags < 65535 ? n_dags : 65535);  // grid y limit; the kernel strides
+    k_batch_finish<<<dim3((unsigned)((max_events + 255) / 256), gy), 256, 0, st>>>(fs, n_dags);
     return cudaGetLastError();
 }
 

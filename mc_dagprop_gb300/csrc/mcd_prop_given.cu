@@ -8,10 +8,8 @@ cudaError_t launch_prop_given(const KArgs &a, bool win_smem, bool stats, dim3 gr
     void (*fn)(const KArgs);
     if (stats) fn = win_smem ? k_propagate<true, true, true, false> : k_propagate<true, false, true, false>;
     else fn = win_smem ? k_propagate<true, true, false, false> : k_propagate<true, false, false, false>;
-    if (smem > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
+    const cudaError_t e = raise_smem_limit((const void *)fn, smem);
+    if (e != cudaSuccess) return e;
     fn<<<grid, block, smem, st>>>(a);
     return cudaGetLastError();
 }

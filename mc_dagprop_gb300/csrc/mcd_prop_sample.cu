@@ -9,9 +9,12 @@ namespace mcd {
 // items from an atomic work queue (ordered longest first by the host) until the
 // queue is empty.  No CTA waits on another: the queue head is a plain counter.
 // DAGs whose window is not on chip use per-CTA scratch rows (32 samples each).
+// Each DAG has its own shared-memory layout; the barrier pair lives outside
+// all of them, in static shared memory, so it never moves between items.
 __global__ void __launch_bounds__(512) k_batch_stats(const BatchArgs b) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ KArgs s_args;
+    __shared__ __align__(8) uint64_t s_bars[2];
     __shared__ int s_item;
     bool reuse = false;
     for (;;) {
@@ -23,14 +26,21 @@ __global__ void __launch_bounds__(512) k_batch_stats(const BatchArgs b) {
         if (threadIdx.x == 0) s_args = b.dags[it.x];
         __syncthreads();
         const KArgs &a = s_args;
+        if (a.smem_total > b.smem_bytes) {  // a layout larger than the launch's shared memory: never touch it
+            if (threadIdx.x == 0) atomicOr(a.err, ERR_LAYOUT);
+            __syncthreads();
+            continue;
+        }
         bool ok;
         if (a.win_smem) {
-            ok = a.positive ? propagate_tile<false, true, true, true>(a, it.y, nullptr, 0, true, smem, reuse)
-                            : propagate_tile<false, true, true, false>(a, it.y, nullptr, 0, true, smem, reuse);
+            ok = a.positive
+                     ? propagate_tile<false, true, true, true>(a, it.y, nullptr, 0, true, smem, s_bars, reuse)
+                     : propagate_tile<false, true, true, false>(a, it.y, nullptr, 0, true, smem, s_bars, reuse);
         } else {
             double *rows = b.scratch + (int64_t)blockIdx.x * b.scratch_stride;
-            ok = a.positive ? propagate_tile<false, false, true, true>(a, it.y, rows, kTile, true, smem, reuse)
-                            : propagate_tile<false, false, true, false>(a, it.y, rows, kTile, true, smem, reuse);
+            ok = a.positive
+                     ? propagate_tile<false, false, true, true>(a, it.y, rows, kTile, true, smem, s_bars, reuse)
+                     : propagate_tile<false, false, true, false>(a, it.y, rows, kTile, true, smem, s_bars, reuse);
         }
         reuse = true;
         if (!ok) return;
@@ -48,32 +58,24 @@ cudaError_t launch_prop_sample(const KArgs &a, bool win_smem, bool stats, bool p
         if (positive) fn = win_smem ? k_propagate<false, true, false, true> : k_propagate<false, false, false, true>;
         else fn = win_smem ? k_propagate<false, true, false, false> : k_propagate<false, false, false, false>;
     }
-    if (smem > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
+    const cudaError_t e = raise_smem_limit((const void *)fn, smem);
+    if (e != cudaSuccess) return e;
     fn<<<grid, block, smem, st>>>(a);
     return cudaGetLastError();
 }
 
 // Persistent batch launch: one CTA per SM slot, `blocks_per_sm` of them per SM.
 cudaError_t launch_batch_stats(const BatchArgs &b, int n_warps, size_t smem, int grid, cudaStream_t st) {
-    if (smem > 48 * 1024) {
-        const cudaError_t e =
-            cudaFuncSetAttribute(k_batch_stats, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
+    const cudaError_t e = raise_smem_limit((const void *)k_batch_stats, smem);
+    if (e != cudaSuccess) return e;
     k_batch_stats<<<grid, n_warps * 32, smem, st>>>(b);
     return cudaGetLastError();
 }
 
 // CTAs of the batch kernel that fit on one SM at this block size and shared memory.
 cudaError_t batch_blocks_per_sm(int n_warps, size_t smem, int *out) {
-    if (smem > 48 * 1024) {
-        const cudaError_t e =
-            cudaFuncSetAttribute(k_batch_stats, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
+    const cudaError_t e = raise_smem_limit((const void *)k_batch_stats, smem);
+    if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_batch_stats, n_warps * 32, smem);
 }
 

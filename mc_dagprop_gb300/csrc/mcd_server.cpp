@@ -1,0 +1,544 @@
+// mcd_server.cpp -- continuous-batching request server (no reference counterpart).
+//
+// Requests are (DAG, generator, seed0, n samples) asking for per-event
+// statistics.  submit() copies the inputs and returns a ticket at once; a pool
+// of host threads compiles the DAGs (mcd_compile.cpp); one scheduler thread
+//   - admits compiled requests while the device-memory budget allows, taking
+//     each request's block (compiled records, accumulators, outputs) from the
+//     stream-ordered allocator (cudaMallocAsync: no device-wide synchronisation);
+//   - whenever one of its stream slots is free, launches everything admitted as
+//     one batch (the persistent k_batch_stats over (request, tile) items, then
+//     the batched finish and the copy of the statistics to pinned host memory),
+//     so requests that arrive while earlier batches run are batched as soon as a
+//     slot frees up, and batches on different slots overlap on the GPU;
+//   - polls the slots' events, completes tickets and returns memory.
+// A request's statistics are the same alone and in any mix: every request has
+// its own accumulators and the accumulation is exact integer arithmetic.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "mcd_handle.hpp"
+
+namespace mcd {
+cudaError_t launch_batch_stats(const BatchArgs &b, int n_warps, size_t smem, int grid, cudaStream_t st);
+cudaError_t batch_blocks_per_sm(int n_warps, size_t smem, int *out);
+cudaError_t launch_batch_finish(const FArgs *fs, int32_t n_dags, int32_t max_events, cudaStream_t st);
+}  // namespace mcd
+
+using namespace mcd;
+using Clock = std::chrono::steady_clock;
+
+namespace {
+
+enum State : int { Q_COMPILE = 0, Q_READY = 1, Q_RUNNING = 2, Q_DONE = 3, Q_FAILED = 4 };
+
+struct Request {
+    int64_t ticket = 0;
+    // inputs (copied at submit)
+    std::vector<double> earliest, act_duration;
+    std::vector<int32_t> act_idx, act_type, target, pred_src, pred_act;
+    std::vector<int64_t> pred_offsets;
+    double max_delay = 0.0;
+    mcd_generator gen;
+    int64_t seed0 = 0, n = 0;
+    // compiled
+    HostDag h;
+    size_t bytes = 0;  // device block
+    std::string error;
+    // device (while running)
+    char *dblock = nullptr;
+    // results
+    std::vector<double> out;  // 5 x E: mean, p50, p90, p99, p_on_time
+    std::atomic<int> state{Q_COMPILE};
+    Clock::time_point t_submit, t_done;
+};
+
+// Offsets of one request's device block.
+struct Layout {
+    size_t ev, pred, aux, dist, alias, wk, meta, earliest, ub, err, acc, hist, out, total;
+};
+
+Layout layout_of(const HostDag &h) {
+    Layout L{};
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o += align_up(std::max<size_t>(bytes, 1), 256);
+        return at;
+    };
+    L.ev = take(h.ev.size() * sizeof(EvRec));
+    L.pred = take(h.pred.size() * sizeof(PredRec));
+    L.aux = take(h.aux.size() * sizeof(LinkRec));
+    L.dist = take(h.dist.size() * sizeof(DistParam));
+    L.alias = take(h.alias.size() * sizeof(AliasEntry));
+    L.wk = take(h.wk_off.size() * 4);
+    L.meta = take(h.stage_meta.size() * 4);
+    L.earliest = take((size_t)h.E * 8);
+    L.ub = take((size_t)h.E * 8);
+    L.err = take(4);
+    L.acc = take((size_t)h.E * 8);
+    L.hist = take((size_t)h.E * kHistStride * 4);
+    L.out = take((size_t)h.E * 5 * 8);
+    L.total = o;
+    return L;
+}
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    bool busy = false;
+    std::vector<Request *> batch;
+    char *meta_dev = nullptr;  // KArgs[], FArgs[], items, queue head
+    size_t meta_bytes = 0;
+    double *pinned = nullptr;  // statistics of the batch, host side
+    size_t pinned_elems = 0;
+    std::vector<char> meta_host;
+};
+
+}  // namespace
+
+struct mcd_server {
+    mcd_server_options opt{};
+    int device = 0, sms = 1;
+    cudaMemPool_t pool = nullptr;
+    std::mutex mu;
+    std::condition_variable cv_compile, cv_sched, cv_done;
+    std::deque<Request *> to_compile, ready;
+    std::unordered_map<int64_t, std::unique_ptr<Request>> all;
+    std::vector<Slot> slots;
+    std::vector<std::thread> compilers;
+    std::thread scheduler;
+    std::atomic<bool> stop{false};
+    int64_t next_ticket = 1;
+    int64_t bytes_in_use = 0;
+    int64_t completed = 0, launched_batches = 0, running = 0;
+    std::string fatal;  // a CUDA failure of the scheduler: every later call reports it
+};
+
+namespace {
+
+void compile_loop(mcd_server *S) {
+    for (;;) {
+        Request *r = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            S->cv_compile.wait(lk, [&] { return S->stop || !S->to_compile.empty(); });
+            if (S->stop) return;
+            r = S->to_compile.front();
+            S->to_compile.pop_front();
+        }
+        try {
+            mcd_dag_desc d{};
+            d.n_events = (int32_t)r->earliest.size();
+            d.earliest = r->earliest.data();
+            d.n_activities = (int32_t)r->act_idx.size();
+            d.act_idx = r->act_idx.data();
+            d.act_duration = r->act_duration.data();
+            d.act_type = r->act_type.data();
+            d.n_targets = (int32_t)r->target.size();
+            d.target = r->target.data();
+            d.pred_offsets = r->pred_offsets.data();
+            d.pred_src = r->pred_src.data();
+            d.pred_act = r->pred_act.data();
+            d.max_delay = r->max_delay;
+            compile_dag(d, r->gen, r->h, S->opt.n_warps);
+            r->bytes = layout_of(r->h).total;
+            if ((int64_t)r->bytes > S->opt.memory_budget)
+                throw McdError(MCD_ERR_INVALID, "request needs more device memory than the server's budget");
+            std::lock_guard<std::mutex> lk(S->mu);
+            r->state = Q_READY;
+            S->ready.push_back(r);
+        } catch (const std::exception &e) {
+            std::lock_guard<std::mutex> lk(S->mu);
+            r->error = e.what();
+            r->state = Q_FAILED;
+            r->t_done = Clock::now();
+            S->cv_done.notify_all();
+        }
+        S->cv_sched.notify_one();
+    }
+}
+
+// Uploads one request's compiled records into its block; returns its kernel
+// and finish arguments.
+void stage_request(mcd_server *S, Request *r, cudaStream_t st, KArgs &a, FArgs &f) {
+    const HostDag &h = r->h;
+    const Layout L = layout_of(h);
+    char *b = r->dblock;
+    auto up = [&](size_t off, const void *src, size_t bytes) {
+        if (bytes) cuda_check(cudaMemcpyAsync(b + off, src, bytes, cudaMemcpyHostToDevice, st), "request upload");
+    };
+    up(L.ev, h.ev.data(), h.ev.size() * sizeof(EvRec));
+    up(L.pred, h.pred.data(), h.pred.size() * sizeof(PredRec));
+    up(L.aux, h.aux.data(), h.aux.size() * sizeof(LinkRec));
+    up(L.dist, h.dist.data(), h.dist.size() * sizeof(DistParam));
+    up(L.alias, h.alias.data(), h.alias.size() * sizeof(AliasEntry));
+    up(L.wk, h.wk_off.data(), h.wk_off.size() * 4);
+    up(L.meta, h.stage_meta.data(), h.stage_meta.size() * 4);
+    up(L.earliest, h.earliest.data(), (size_t)h.E * 8);
+    up(L.ub, h.ub.data(), (size_t)h.E * 8);
+    cuda_check(cudaMemsetAsync(b + L.err, 0, L.out - L.err, st), "request reset");  // flags + accumulators
+    const StatsParams sp = stats_params(h, r->n);
+    a = KArgs{};
+    a.ev = reinterpret_cast<const EvRec *>(b + L.ev);
+    a.pred = reinterpret_cast<const PredRec *>(b + L.pred);
+    a.aux = reinterpret_cast<const LinkRec *>(b + L.aux);
+    a.dist = reinterpret_cast<const DistParam *>(b + L.dist);
+    a.alias = reinterpret_cast<const AliasEntry *>(b + L.alias);
+    a.wk_off = reinterpret_cast<const int32_t *>(b + L.wk);
+    a.stage_meta = reinterpret_cast<const int32_t *>(b + L.meta);
+    a.n_stages = h.n_stages;
+    a.n_warps = h.n_warps;
+    a.n_aux = (int32_t)h.aux.size();
+    a.window_slots = h.window_slots;
+    a.n_dist = (int32_t)h.dist.size();
+    a.n_alias = (int32_t)h.alias.size();
+    a.tables_in_smem = h.tables_in_smem ? 1 : 0;
+    a.win_smem = h.win_smem ? 1 : 0;
+    a.positive = h.positive ? 1 : 0;
+    a.stage_bytes = h.stage_bytes;
+    a.stage_pred_off = h.stage_pred_off;
+    a.smem_stage_off = h.smem_stage_off;
+    a.smem_tables_off = h.smem_tables_off;
+    a.smem_bar_off = h.smem_bar_off;
+    a.smem_total = h.smem_total;
+    a.err = reinterpret_cast<int32_t *>(b + L.err);
+    a.seeds = nullptr;
+    a.seed0 = r->seed0;
+    a.n = r->n;
+    a.stats_fixed = sp.fixed;
+    a.tick_q = sp.q;
+    a.bin_mul = sp.bin_mul;
+    a.hist_inv_w = sp.inv_w;
+    a.acc = reinterpret_cast<unsigned long long *>(b + L.acc);
+    a.hist = reinterpret_cast<uint32_t *>(b + L.hist);
+    f = FArgs{};
+    f.acc = a.acc;
+    f.hist = a.hist;
+    f.earliest = reinterpret_cast<const double *>(b + L.earliest);
+    f.ub = reinterpret_cast<const double *>(b + L.ub);
+    f.E = h.E;
+    f.stats_fixed = sp.fixed;
+    f.tick_q = sp.q;
+    f.bin_w = sp.bin_w;
+    f.n = r->n;
+    double *o = reinterpret_cast<double *>(b + L.out);
+    f.mean = o;
+    f.p50 = o + h.E;
+    f.p90 = o + 2 * (size_t)h.E;
+    f.p99 = o + 3 * (size_t)h.E;
+    f.p_on_time = o + 4 * (size_t)h.E;
+}
+
+// Launches one batch on a free slot (scheduler thread; the lock is not held).
+void launch_batch(mcd_server *S, Slot &slot, std::vector<Request *> &batch) {
+    cudaStream_t st = slot.stream;
+    const size_t nb = batch.size();
+    std::vector<KArgs> ka(nb);
+    std::vector<FArgs> fa(nb);
+    std::vector<int32_t> items;
+    size_t smem = 0, out_elems = 0;
+    int32_t max_E = 0;
+    for (size_t i = 0; i < nb; ++i) {
+        Request *r = batch[i];
+        cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&r->dblock), r->bytes, st), "request allocation");
+        stage_request(S, r, st, ka[i], fa[i]);
+        smem = std::max(smem, (size_t)r->h.smem_total);
+        max_E = std::max(max_E, r->h.E);
+        out_elems += (size_t)r->h.E * 5;
+        const int64_t tiles = (r->n + kTile - 1) / kTile;
+        for (int64_t t = 0; t < tiles; ++t) {
+            items.push_back((int32_t)i);
+            items.push_back((int32_t)t);
+        }
+    }
+    // longest first: requests by cost per tile, descending
+    {
+        std::vector<int32_t> order(nb);
+        for (size_t i = 0; i < nb; ++i) order[i] = (int32_t)i;
+        std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+            return batch[x]->h.pred.size() + 2 * (size_t)batch[x]->h.E > batch[y]->h.pred.size() + 2 * (size_t)batch[y]->h.E;
+        });
+        std::vector<int32_t> sorted;
+        sorted.reserve(items.size());
+        for (int32_t i : order) {
+            const int64_t tiles = (batch[i]->n + kTile - 1) / kTile;
+            for (int64_t t = 0; t < tiles; ++t) {
+                sorted.push_back(i);
+                sorted.push_back((int32_t)t);
+            }
+        }
+        items.swap(sorted);
+    }
+    const size_t s_ka = align_up(nb * sizeof(KArgs), 256), s_fa = align_up(nb * sizeof(FArgs), 256),
+                 s_items = align_up(items.size() * 4, 256), s_ctr = 256;
+    const size_t need = s_ka + s_fa + s_items + s_ctr;
+    if (need > slot.meta_bytes) {
+        if (slot.meta_dev) cuda_check(cudaFreeAsync(slot.meta_dev, st), "slot metadata free");
+        slot.meta_bytes = need * 2;
+        cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&slot.meta_dev), slot.meta_bytes, st), "slot metadata");
+    }
+    if (out_elems > slot.pinned_elems) {
+        cuda_check(cudaStreamSynchronize(st), "slot sync");
+        if (slot.pinned) cudaFreeHost(slot.pinned);
+        slot.pinned_elems = out_elems * 2;
+        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&slot.pinned), slot.pinned_elems * 8, cudaHostAllocDefault),
+                   "pinned results");
+    }
+    // metadata in one host buffer, one upload (the buffer stays alive until the slot completes)
+    slot.meta_host.assign(need, 0);
+    std::memcpy(slot.meta_host.data(), ka.data(), nb * sizeof(KArgs));
+    std::memcpy(slot.meta_host.data() + s_ka, fa.data(), nb * sizeof(FArgs));
+    std::memcpy(slot.meta_host.data() + s_ka + s_fa, items.data(), items.size() * 4);
+    cuda_check(cudaMemcpyAsync(slot.meta_dev, slot.meta_host.data(), need, cudaMemcpyHostToDevice, st), "batch upload");
+    BatchArgs ba{};
+    ba.dags = reinterpret_cast<const KArgs *>(slot.meta_dev);
+    ba.items = reinterpret_cast<const int32_t *>(slot.meta_dev + s_ka + s_fa);
+    ba.n_items = (int32_t)(items.size() / 2);
+    ba.counter = reinterpret_cast<unsigned int *>(slot.meta_dev + s_ka + s_fa + s_items);
+    ba.scratch = nullptr;  // requests need their window in shared memory (checked at admission)
+    ba.scratch_stride = 0;
+    ba.smem_bytes = (int32_t)smem;
+    int per_sm = 1;
+    cuda_check(batch_blocks_per_sm(S->opt.n_warps, smem, &per_sm), "occupancy");
+    const int grid = std::max(1, per_sm) * S->sms;
+    cuda_check(launch_batch_stats(ba, S->opt.n_warps, smem, grid, st), "batch launch");
+    cuda_check(launch_batch_finish(reinterpret_cast<const FArgs *>(slot.meta_dev + s_ka), (int32_t)nb, max_E, st),
+               "batch finish");
+    size_t pos = 0;
+    for (Request *r : batch) {
+        const size_t e5 = (size_t)r->h.E * 5;
+        cuda_check(cudaMemcpyAsync(slot.pinned + pos, r->dblock + layout_of(r->h).out, e5 * 8, cudaMemcpyDeviceToHost,
+                                   st),
+                   "results download");
+        cuda_check(cudaFreeAsync(r->dblock, st), "request free");
+        pos += e5;
+    }
+    cuda_check(cudaEventRecord(slot.done, st), "event record");
+    slot.batch = batch;
+    slot.busy = true;
+}
+
+void complete_slot(mcd_server *S, Slot &slot) {
+    size_t pos = 0;
+    std::vector<Request *> done = slot.batch;
+    for (Request *r : done) {
+        const size_t e5 = (size_t)r->h.E * 5;
+        r->out.assign(slot.pinned + pos, slot.pinned + pos + e5);
+        pos += e5;
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (Request *r : done) {
+        r->dblock = nullptr;
+        r->t_done = Clock::now();
+        r->state = Q_DONE;
+        S->bytes_in_use -= (int64_t)r->bytes;
+        S->completed += 1;
+        S->running -= 1;
+    }
+    slot.batch.clear();
+    slot.busy = false;
+    S->cv_done.notify_all();
+}
+
+void schedule_loop(mcd_server *S) {
+    cudaSetDevice(S->device);
+    while (!S->stop) {
+        try {
+            bool progressed = false;
+            for (Slot &slot : S->slots) {
+                if (slot.busy && cudaEventQuery(slot.done) == cudaSuccess) {
+                    complete_slot(S, slot);
+                    progressed = true;
+                }
+            }
+            for (Slot &slot : S->slots) {
+                if (slot.busy) continue;
+                std::vector<Request *> batch;
+                {
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    while (!S->ready.empty() && (S->opt.max_batch <= 0 || (int32_t)batch.size() < S->opt.max_batch)) {
+                        Request *r = S->ready.front();
+                        if (S->bytes_in_use + (int64_t)r->bytes > S->opt.memory_budget) break;
+                        S->ready.pop_front();
+                        if (!r->h.win_smem) {  // the served kernel keeps every window on chip
+                            r->error = "request DAG's window does not fit in shared memory";
+                            r->state = Q_FAILED;
+                            r->t_done = Clock::now();
+                            S->cv_done.notify_all();
+                            continue;
+                        }
+                        S->bytes_in_use += (int64_t)r->bytes;
+                        S->running += 1;
+                        r->state = Q_RUNNING;
+                        batch.push_back(r);
+                    }
+                }
+                if (batch.empty()) break;
+                launch_batch(S, slot, batch);
+                {
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    S->launched_batches += 1;
+                }
+                progressed = true;
+            }
+            if (!progressed) {
+                std::unique_lock<std::mutex> lk(S->mu);
+                S->cv_sched.wait_for(lk, std::chrono::microseconds(50));
+            }
+        } catch (const std::exception &e) {
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->fatal = e.what();
+            S->stop = true;
+            S->cv_done.notify_all();
+            return;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int mcd_server_create(const mcd_server_options *opt, mcd_server **out) {
+    return guarded([&] {
+        if (!opt || !out) throw McdError(MCD_ERR_INVALID, "null argument");
+        if (opt->memory_budget <= 0 || opt->n_streams < 1 || opt->n_streams > 16 || opt->n_warps < 1 ||
+            opt->n_warps > kMaxBatchWarps || opt->compile_threads < 1 || opt->compile_threads > 256)
+            throw McdError(MCD_ERR_INVALID, "bad server options");
+        auto S = std::make_unique<mcd_server>();
+        S->opt = *opt;
+        cuda_check(cudaGetDevice(&S->device), "cudaGetDevice");
+        cuda_check(cudaDeviceGetAttribute(&S->sms, cudaDevAttrMultiProcessorCount, S->device), "SM count");
+        cuda_check(cudaDeviceGetDefaultMemPool(&S->pool, S->device), "memory pool");
+        uint64_t keep = (uint64_t)opt->memory_budget;  // freed blocks stay in the pool for reuse
+        cuda_check(cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep), "pool threshold");
+        S->slots.resize((size_t)opt->n_streams);
+        for (Slot &s : S->slots) {
+            cuda_check(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "stream create");
+            cuda_check(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming), "event create");
+        }
+        mcd_server *raw = S.get();
+        for (int i = 0; i < opt->compile_threads; ++i) S->compilers.emplace_back(compile_loop, raw);
+        S->scheduler = std::thread(schedule_loop, raw);
+        *out = S.release();
+    });
+}
+
+void mcd_server_destroy(mcd_server *S) {
+    if (!S) return;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->stop = true;
+    }
+    S->cv_compile.notify_all();
+    S->cv_sched.notify_all();
+    if (S->scheduler.joinable()) S->scheduler.join();
+    for (std::thread &t : S->compilers)
+        if (t.joinable()) t.join();
+    cudaSetDevice(S->device);
+    for (Slot &s : S->slots) {
+        if (s.stream) cudaStreamSynchronize(s.stream);
+        if (s.meta_dev) cudaFreeAsync(s.meta_dev, s.stream);
+        if (s.stream) cudaStreamSynchronize(s.stream);
+        if (s.pinned) cudaFreeHost(s.pinned);
+        if (s.done) cudaEventDestroy(s.done);
+        if (s.stream) cudaStreamDestroy(s.stream);
+    }
+    delete S;
+}
+
+int mcd_server_submit(mcd_server *S, const mcd_dag_desc *d, const mcd_generator *gen, int64_t seed0, int64_t n,
+                      int64_t *ticket) {
+    return guarded([&] {
+        if (!S || !d || !gen || !ticket) throw McdError(MCD_ERR_INVALID, "null argument");
+        if (n <= 0 || n > (int64_t)1 << 31) throw McdError(MCD_ERR_INVALID, "need 0 < n <= 2^31 samples");
+        if (d->n_events < 0 || d->n_activities < 0 || d->n_targets < 0)
+            throw McdError(MCD_ERR_INVALID, "negative array length in DAG description");
+        auto r = std::make_unique<Request>();
+        r->earliest.assign(d->earliest, d->earliest + d->n_events);
+        r->act_idx.assign(d->act_idx, d->act_idx + d->n_activities);
+        r->act_duration.assign(d->act_duration, d->act_duration + d->n_activities);
+        r->act_type.assign(d->act_type, d->act_type + d->n_activities);
+        r->target.assign(d->target, d->target + d->n_targets);
+        r->pred_offsets.assign(d->pred_offsets, d->pred_offsets + d->n_targets + 1);
+        const int64_t P = d->n_targets > 0 ? d->pred_offsets[d->n_targets] : 0;
+        r->pred_src.assign(d->pred_src, d->pred_src + P);
+        r->pred_act.assign(d->pred_act, d->pred_act + P);
+        r->max_delay = d->max_delay;
+        r->gen = *gen;
+        r->seed0 = seed0;
+        r->n = n;
+        r->t_submit = Clock::now();
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (!S->fatal.empty()) throw McdError(MCD_ERR_CUDA, "server stopped: " + S->fatal);
+        r->ticket = S->next_ticket++;
+        *ticket = r->ticket;
+        S->to_compile.push_back(r.get());
+        S->all[r->ticket] = std::move(r);
+        S->cv_compile.notify_one();
+    });
+}
+
+// Copies the statistics of a finished request and forgets it.  status: 1 done,
+// 0 still pending (wait_ms elapsed); an error status for a failed request.
+int mcd_server_wait(mcd_server *S, int64_t ticket, double wait_ms, const mcd_stats *host, int32_t *done,
+                    double *latency_ms) {
+    return guarded([&] {
+        if (!S || !done) throw McdError(MCD_ERR_INVALID, "null argument");
+        std::unique_lock<std::mutex> lk(S->mu);
+        auto it = S->all.find(ticket);
+        if (it == S->all.end()) throw McdError(MCD_ERR_INVALID, "unknown ticket");
+        Request *r = it->second.get();
+        auto finished = [&] { return r->state == Q_DONE || r->state == Q_FAILED || !S->fatal.empty(); };
+        if (!finished()) {
+            if (wait_ms > 0)
+                S->cv_done.wait_for(lk, std::chrono::duration<double, std::milli>(wait_ms), finished);
+        }
+        if (!S->fatal.empty() && r->state != Q_DONE) throw McdError(MCD_ERR_CUDA, "server stopped: " + S->fatal);
+        if (r->state == Q_FAILED) {
+            const std::string msg = r->error;
+            S->all.erase(it);
+            throw McdError(MCD_ERR_INVALID, msg);
+        }
+        if (r->state != Q_DONE) {
+            *done = 0;
+            return;
+        }
+        *done = 1;
+        const size_t E = (size_t)r->h.E;
+        double *dst[5] = {host ? host->mean : nullptr, host ? host->p50 : nullptr, host ? host->p90 : nullptr,
+                          host ? host->p99 : nullptr, host ? host->p_on_time : nullptr};
+        for (int k = 0; k < 5; ++k)
+            if (dst[k]) std::memcpy(dst[k], r->out.data() + k * E, E * 8);
+        if (latency_ms)
+            *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+        S->all.erase(it);
+    });
+}
+
+int mcd_server_counters(mcd_server *S, mcd_server_info *info) {
+    return guarded([&] {
+        if (!S || !info) throw McdError(MCD_ERR_INVALID, "null argument");
+        std::lock_guard<std::mutex> lk(S->mu);
+        info->completed = S->completed;
+        info->batches = S->launched_batches;
+        info->queued = (int64_t)(S->to_compile.size() + S->ready.size());
+        info->bytes_in_use = S->bytes_in_use;
+        info->running = S->running;
+    });
+}
+
+}  // extern "C"

@@ -51,3 +51,27 @@ def test_batch_rejects_mixed_warps(cuda):
     b = _prop(flat, gen, 8)
     with pytest.raises(ValueError, match="same n_warps"):
         m.Batch([a, b], [0, 0], [64, 64])
+
+
+@pytest.mark.parametrize("nw", [2, 8])
+def test_batch_many_layouts_per_cta(cuda, nw):
+    """Persistent CTAs that run tiles of many DAGs in turn, each with its own
+    shared-memory layout (window, staging buffers and tables at different
+    offsets): every DAG still gets exactly its single-DAG statistics."""
+    dags = W.mixed_dags(seed=2, n_dags=40, ev_lo=100, ev_hi=20000, s_lo=300, s_hi=2500, five_types=True)
+    props, seed0, ns = [], [], []
+    for flat, gen, n, sb in dags:
+        props.append(_prop(flat, gen, nw))
+        seed0.append(sb)
+        ns.append(n)
+    offsets = {p.info()["smem_bytes"] for p in props}
+    assert len(offsets) > 10
+    batch = m.Batch(props, seed0, ns)
+    assert batch.items > 4 * batch.grid  # most CTAs take several items
+    for rep in range(2):
+        batch.run()
+        for i, p in enumerate(props):
+            got = batch.stats(i)
+            ref = p.run_stats(n=ns[i], seed0=seed0[i])
+            for k in ("mean", "p50", "p90", "p99", "p_on_time"):
+                assert np.array_equal(got[k], ref[k]), (rep, i, k)

@@ -1,0 +1,54 @@
+"""Continuous-batching server: every request's statistics equal those of the
+same request run alone (exact: per-request accumulators, integer accumulation),
+whatever mix it was batched with; failures are per request; the memory budget
+admits work in pieces."""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+import pytest
+
+import mc_dagprop_gb300 as m
+from mc_dagprop_gb300 import batching
+from mc_dagprop_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _submit(server, flat, gen, seed0, n):
+    return server.submit(flat["earliest"], flat["act_idx"], flat["act_duration"], flat["act_type"], flat["target"],
+                         flat["pred_offsets"], flat["pred_src"], flat["pred_act"], flat["max_delay"],
+                         W.to_generator(m, gen), seed0, n)
+
+
+@pytest.mark.parametrize("n_streams,budget", [(2, 8 << 30), (3, 64 << 20)])
+def test_served_results_equal_alone(cuda, n_streams, budget):
+    reqs = W.mixed_dags(seed=9, n_dags=24, ev_lo=50, ev_hi=3000, s_lo=64, s_hi=4000, five_types=True)
+    server = m.Server(memory_budget=budget, n_streams=n_streams, n_warps=8, compile_threads=4)
+    tickets = []
+    for i, (flat, gen, n, s0) in enumerate(reqs):
+        tickets.append(_submit(server, flat, gen, s0, n))
+        if i % 5 == 0:
+            time.sleep(0.002)  # let some batches start while others arrive
+    results = [server.wait(t, timeout_ms=60_000) for t in tickets]
+    c = server.counters()
+    assert c["completed"] == len(reqs) and c["queued"] == 0
+    assert c["batches"] >= 2
+    for (flat, gen, n, s0), got in zip(reqs, results):
+        assert got is not None
+        alone = batching.compile_dag(flat, gen, 8).run_stats(n=n, seed0=s0)
+        for k in ("mean", "p50", "p90", "p99", "p_on_time"):
+            assert np.array_equal(got[k], alone[k]), k
+        assert got["latency_ms"] > 0
+
+
+def test_server_rejects_bad_request_and_keeps_serving(cuda):
+    server = m.Server(memory_budget=1 << 30, n_streams=2, n_warps=8, compile_threads=2)
+    flat, gen = W.config0()
+    bad = dict(flat, max_delay=-1.0)
+    t_bad = _submit(server, bad, gen, 0, 64)
+    t_ok = _submit(server, flat, gen, 0, 64)
+    with pytest.raises(RuntimeError, match="max_delay"):
+        server.wait(t_bad, timeout_ms=30_000)
+    assert server.wait(t_ok, timeout_ms=30_000) is not None

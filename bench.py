@@ -255,7 +255,7 @@ def run_batched(args):
                                "1,000-100,000, own seed ranges; per-event mean, p50/p90/p99 (256-bin histograms)",
                    "dags": len(items), "events_total": int(sum(len(f["earliest"]) for f, _, _, _ in items)),
                    "sample_edges_per_step": units,
-                   "classes (warps, dags, items)": runner.classes},
+                   "classes (warps, ctas_per_sm, dags, items)": runner.classes},
         "plain": {"value": units / (plain_ms * 1e-3), "ms_per_step": plain_ms,
                   "path": "one mcd_stats_device call per DAG on one stream, automatic warps per DAG"},
         "batched_over_plain": plain_ms / batch_ms, "check_mismatches": mism,
@@ -288,7 +288,7 @@ def run_serving(args):
     n_req = int(args.rate * args.duration)
     arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n_req))
     which = rng.integers(0, len(pool), n_req)
-    server = m.Server(memory_budget=64 << 30, n_streams=args.streams, n_warps=8, compile_threads=args.compile_threads)
+    server = m.Server(memory_budget=64 << 30, n_streams=args.streams, n_warps=0, compile_threads=args.compile_threads)
     # warm the server (kernels loaded, pool grown) with a few requests
     for i in range(4):
         f, _, n, s0 = pool[i]
@@ -352,6 +352,8 @@ def run_serving(args):
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "max": float(lat.max())},
         "completed": int(counters["completed"]), "batches": int(counters["batches"]), "errors": len(errors),
+        "server_seconds": {k: round(float(counters[k]), 3) for k in ("compile_seconds", "upload_seconds",
+                                                                      "launch_seconds")},
         "submit_seconds": submit_s,
         "plain": {"value": plain_units / plain_s, "requests": k,
                   "path": "per request: create propagator (host compile + upload) + mcd_stats_host, sequential"},
@@ -427,7 +429,7 @@ def main():
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--duration", type=float, default=5.0)
     ap.add_argument("--pool", type=int, default=128)
-    ap.add_argument("--streams", type=int, default=3)
+    ap.add_argument("--streams", type=int, default=4)
     ap.add_argument("--compile-threads", type=int, default=8)
     ap.add_argument("--plain-requests", type=int, default=200)
     ap.add_argument("--grad-samples", type=int, default=65536)

@@ -120,8 +120,10 @@ typedef struct mcd_dag_info {
  * separate handles run concurrently. */
 int mcd_dag_create(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag **out);
 /* Compile options (the same call with explicit choices). */
+#define MCD_WARPS_BATCH_CLASS (-1)
 typedef struct mcd_dag_options {
-    int32_t n_warps; /* warps per CTA, 1..16; 0 = chosen from the DAG's level width */
+    int32_t n_warps; /* warps per CTA, 1..24; 0 = chosen from the DAG's level width;
+                        MCD_WARPS_BATCH_CLASS = chosen, then rounded up to 2, 4, 8, 12 or 24 */
 } mcd_dag_options;
 int mcd_dag_create_ex(const mcd_dag_desc *desc, const mcd_generator *gen, const mcd_dag_options *opts,
                       mcd_dag **out);
@@ -202,8 +204,8 @@ int mcd_stats_bin_width(const mcd_dag *dag, int64_t n, double *out);
  * (no reference counterpart: the reference runs one DAG per run_many call).
  * DAG i runs samples with seeds seed0[i] .. seed0[i]+n_samples[i]-1 and produces
  * the same statistics as mcd_stats_* would for it alone.  All DAGs must share a
- * device and be compiled with the same n_warps (mcd_dag_create_ex); they must
- * outlive the batch.  A run is one CUDA graph (recorded on the first run,
+ * device and be compiled with the same n_warps (1..24, mcd_dag_create_ex); they
+ * must outlive the batch.  A run is one CUDA graph (recorded on the first run,
  * replayed after): accumulator reset, the persistent kernel over (DAG, tile)
  * work items in longest-first order, the batched finish.  mcd_batch_run is
  * asynchronous on the batch's own stream; mcd_batch_sync waits and reports
@@ -218,6 +220,11 @@ int mcd_batch_download(mcd_batch *batch, int32_t i, const mcd_stats *host);
 void *mcd_batch_stream(const mcd_batch *batch);
 int64_t mcd_batch_items(const mcd_batch *batch);
 int32_t mcd_batch_grid(const mcd_batch *batch);
+/* CTAs of the persistent batch kernel one SM holds at n_warps warps per CTA and
+ * smem_bytes of dynamic shared memory (the largest mcd_dag_info.smem_bytes of the
+ * batch): DAGs with equal values share a launch without lowering each other's
+ * occupancy.  (Every variant of the kernel runs at the same register count.) */
+int mcd_batch_occupancy(int32_t n_warps, int64_t smem_bytes, int32_t *blocks_per_sm);
 
 /* ---- Pathwise gradient (adjoint; no reference counterpart) ----
  * Objective J = mean over the n samples (seeds seed0 .. seed0+n-1) of
@@ -232,9 +239,10 @@ int mcd_gradient_host(mcd_dag *dag, int64_t seed0, int64_t n, double *objective,
 
 /* ---- Serving: continuous batching of statistics requests (no reference counterpart) ----
  * submit() copies a request (a DAG, its generator, seeds seed0 .. seed0+n-1) and
- * returns a ticket at once; host threads compile the DAGs; a scheduler thread
- * admits compiled requests while their device memory fits memory_budget and,
- * whenever one of n_streams slots is free, runs everything admitted as one
+ * returns a ticket at once; host threads compile the DAGs and upload them while
+ * their device memory fits memory_budget; a scheduler thread, whenever one of
+ * n_streams slots is free, runs the uploaded requests of one class -- equal warps
+ * per CTA and CTAs per SM, the class of the oldest waiting request -- as one
  * persistent batch.  A request's statistics equal those of the same request run
  * alone with mcd_stats_*.  Requests whose window does not fit in shared memory
  * are rejected.  wait() returns done = 1 and the statistics (and the latency
@@ -244,12 +252,16 @@ typedef struct mcd_server mcd_server;
 typedef struct mcd_server_options {
     int64_t memory_budget;    /* device bytes the admitted requests may hold */
     int32_t n_streams;        /* batches in flight at once, 1..16 */
-    int32_t n_warps;          /* warps per CTA for every request, 1..16 */
+    int32_t n_warps;          /* warps per CTA for every request, 1..24; 0 = per request
+                                 (MCD_WARPS_BATCH_CLASS), batched by (warps, CTAs per SM) */
     int32_t max_batch;        /* requests per launch, 0 = no limit */
-    int32_t compile_threads;  /* host threads compiling submitted DAGs */
+    int32_t compile_threads;  /* host threads compiling and uploading submitted DAGs */
 } mcd_server_options;
 typedef struct mcd_server_info {
     int64_t completed, batches, queued, running, bytes_in_use;
+    double compile_seconds;   /* host compile time summed over requests */
+    double upload_seconds;    /* allocation + upload time summed over requests */
+    double launch_seconds;    /* scheduler time spent forming and launching batches */
 } mcd_server_info;
 int mcd_server_create(const mcd_server_options *opt, mcd_server **out);
 void mcd_server_destroy(mcd_server *server);

@@ -5,8 +5,11 @@ size of its persistent launch) and runs all (DAG, 32-sample tile) work items in
 one CUDA graph.  The warps per CTA trade work per stage against barrier and idle
 time: wide DAGs want many warps, narrow ones few (and more CTAs per SM).
 ``BatchRunner`` therefore splits a mixed stream into width classes -- by the
-warps the compiler would pick for each DAG alone -- and runs one batch per class,
-all launched together on their own streams so their CTAs share the SMs.  For each
+warps the compiler would pick for each DAG alone -- and each width class by the
+CTAs per SM its DAGs' shared-memory layouts allow (a launch runs at the
+occupancy of its largest layout, so one wide window would otherwise throttle
+every narrow DAG of the batch).  It runs one batch per class, all launched
+together on their own streams so their CTAs share the SMs.  For each width
 class ``tune_warps`` times candidate warp counts on a calibration subset and
 keeps the fastest; results are cached per shape class in a JSON file
 (``$MCD_AUTOTUNE_CACHE``, default ``~/.cache/mc_dagprop_gb300/autotune.json``).
@@ -23,7 +26,10 @@ import numpy as np
 from . import _core
 from . import workloads as W
 
-CANDIDATE_WARPS = (4, 8, 16)
+CANDIDATE_WARPS = (4, 8, 12, 24)
+# warps per CTA tried for each width class: block sizes that divide the 24 warps
+# an SM holds at the batch kernel's register count
+CLASS_CANDIDATES = {4: (2, 4, 8), 8: (4, 8, 12), 12: (6, 12, 24), 24: (12, 24)}
 
 
 def _cache_path() -> str:
@@ -62,7 +68,7 @@ def compile_dag(flat: dict, gen: list, n_warps: int = 0):
 
 def width_class(auto_warps: int) -> int:
     """Width class of a DAG from the warps the compiler picks for it alone."""
-    return 4 if auto_warps <= 4 else (8 if auto_warps <= 8 else 16)
+    return 4 if auto_warps <= 4 else 8 if auto_warps <= 8 else 12 if auto_warps <= 12 else 24
 
 
 def _time_batch(props, seed0, ns, reps: int = 2) -> float:
@@ -129,7 +135,7 @@ class BatchRunner:
                 classes.setdefault(width_class(info["n_warps"]), []).append(i)
             warps = {}
             for c, idx in classes.items():
-                cand = tuple(sorted({max(1, c // 2), c, min(16, 2 * c)}))
+                cand = CLASS_CANDIDATES[c]
                 warps[c] = (tune_warps([flats[i] for i in idx], [gens[i] for i in idx], [self.ns[i] for i in idx],
                                        candidates=cand, use_cache=use_cache, widths=[widths[i] for i in idx])
                             if tune else c)
@@ -137,29 +143,35 @@ class BatchRunner:
         self.where = {}
         self.batches = []
         for c in sorted(classes):
-            idx = classes[c]
-            props = [compile_dag(flats[i], gens[i], warps[c]) for i in idx]
-            for j, i in enumerate(idx):
-                self.props[i] = props[j]
-                self.where[i] = (len(self.batches), j)
-            self.batches.append((warps[c], idx, _core.Batch(props, [self.seed0[i] for i in idx],
-                                                             [self.ns[i] for i in idx])))
+            nw = warps[c]
+            groups = {}
+            for i in classes[c]:
+                p = compile_dag(flats[i], gens[i], nw)
+                self.props[i] = p
+                groups.setdefault(_core.Batch.occupancy(nw, p.info()["smem_bytes"]), []).append(i)
+            for per_sm in sorted(groups, reverse=True):
+                idx = groups[per_sm]
+                for j, i in enumerate(idx):
+                    self.where[i] = (len(self.batches), j)
+                self.batches.append((nw, per_sm, idx, _core.Batch([self.props[i] for i in idx],
+                                                                  [self.seed0[i] for i in idx],
+                                                                  [self.ns[i] for i in idx])))
 
     @property
     def classes(self) -> list:
-        """(warps per CTA, DAG count, work items) of each class batch."""
-        return [(w, len(idx), b.items) for w, idx, b in self.batches]
+        """(warps per CTA, CTAs per SM, DAG count, work items) of each class batch."""
+        return [(w, per_sm, len(idx), b.items) for w, per_sm, idx, b in self.batches]
 
     def run(self, wait: bool = True) -> None:
-        for _, _, b in self.batches:  # one launch per class, all in flight together
+        for *_, b in self.batches:  # one launch per class, all in flight together
             b.run(False)
         if wait:
             self.sync()
 
     def sync(self) -> None:
-        for _, _, b in self.batches:
+        for *_, b in self.batches:
             b.sync()
 
     def stats(self, i: int, hist: bool = False) -> dict:
         k, j = self.where[i]
-        return self.batches[k][2].stats(j, hist)
+        return self.batches[k][3].stats(j, hist)

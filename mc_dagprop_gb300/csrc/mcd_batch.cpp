@@ -4,9 +4,11 @@
 // (longest-processing-time order), consumed by a persistent grid of CTAs that
 // fills every SM whatever the DAGs' sizes -- a plain per-DAG launch of a DAG
 // with 1,000 samples keeps 32 CTAs busy and leaves the rest of the GPU idle.
-// Each run is one CUDA graph: reset the accumulators and the queue head, the
-// persistent statistics kernel, the batched finish.  The graph is recorded on
-// the first run and replayed afterwards.
+// DAGs are grouped by kernel variant (window on chip or not, positive times or
+// not); each group is one launch with its own queue.  Each run is one CUDA
+// graph: reset the accumulators and the queue heads, the persistent statistics
+// launches, the batched finish.  The graph is recorded on the first run and
+// replayed afterwards.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -17,12 +19,24 @@
 #include "mcd_handle.hpp"
 
 namespace mcd {
-cudaError_t launch_batch_stats(const BatchArgs &b, int n_warps, size_t smem, int grid, cudaStream_t st);
-cudaError_t batch_blocks_per_sm(int n_warps, size_t smem, int *out);
+cudaError_t launch_batch_stats(const BatchArgs &b, bool win_smem, bool positive, int n_warps, size_t smem, int grid,
+                               cudaStream_t st);
+cudaError_t batch_blocks_per_sm(bool win_smem, bool positive, int n_warps, size_t smem, int *out);
 cudaError_t launch_batch_finish(const FArgs *fs, int32_t n_dags, int32_t max_events, cudaStream_t st);
 }  // namespace mcd
 
 using namespace mcd;
+
+namespace {
+// One persistent launch: the DAGs of one kernel variant.
+struct Launch {
+    bool win_smem = true, positive = true;
+    std::vector<int32_t> dags;
+    size_t smem = 0;
+    int grid = 1;
+    BatchArgs args{};
+};
+}  // namespace
 
 struct mcd_batch {
     int device = 0;
@@ -30,15 +44,14 @@ struct mcd_batch {
     std::vector<mcd_dag *> dags;
     std::vector<int64_t> n, ev_off;
     int n_warps = 1, grid = 1;
-    size_t smem = 0;
     int32_t max_E = 0;
     int64_t total_E = 0, n_items = 0;
     char *dmem = nullptr;
-    size_t zero_bytes = 0;  // accumulators + queue head, cleared every run
+    size_t zero_bytes = 0;  // accumulators + queue heads, cleared every run
     double *out = nullptr;  // [5][total_E]: mean, p50, p90, p99, p_on_time
     uint32_t *hist = nullptr;
     FArgs *d_fargs = nullptr;
-    BatchArgs args{};
+    std::vector<Launch> launches;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -55,7 +68,7 @@ int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0,
         B->device = dags[0]->device;
         B->n_warps = dags[0]->h.n_warps;
         if (B->n_warps > kMaxBatchWarps)
-            throw McdError(MCD_ERR_INVALID, "DAGs of a batch must be compiled with n_warps <= 16");
+            throw McdError(MCD_ERR_INVALID, "DAGs of a batch must be compiled with n_warps <= 24");
         for (int32_t i = 0; i < n_dags; ++i) {
             const mcd_dag *g = dags[i];
             if (!g) throw McdError(MCD_ERR_INVALID, "null DAG handle");
@@ -69,37 +82,51 @@ int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0,
         }
         cuda_check(cudaSetDevice(B->device), "cudaSetDevice");
         cuda_check(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking), "stream create");
-        // layout of the batch's device memory
-        bool any_global = false;
-        int32_t max_E_global = 0;
+        // layout of the batch's device memory; launches by kernel variant
         B->ev_off.resize((size_t)n_dags + 1, 0);
         for (int32_t i = 0; i < n_dags; ++i) {
             const HostDag &h = B->dags[i]->h;
-            B->smem = std::max(B->smem, (size_t)h.smem_total);
             B->max_E = std::max(B->max_E, h.E);
-            if (!h.win_smem) {
-                any_global = true;
-                max_E_global = std::max(max_E_global, h.E);
-            }
             B->ev_off[i + 1] = B->ev_off[i] + h.E;
+            Launch *L = nullptr;
+            for (Launch &x : B->launches)
+                if (x.win_smem == h.win_smem && x.positive == h.positive) L = &x;
+            if (!L) {
+                B->launches.emplace_back();
+                L = &B->launches.back();
+                L->win_smem = h.win_smem;
+                L->positive = h.positive;
+            }
+            L->dags.push_back(i);
+            L->smem = std::max(L->smem, (size_t)h.smem_total);
         }
         B->total_E = B->ev_off[n_dags];
-        int per_sm = 0, sms = 0;
-        cuda_check(batch_blocks_per_sm(B->n_warps, B->smem, &per_sm), "occupancy query");
+        int sms = 0;
         cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->device), "SM count");
-        B->grid = std::max(1, per_sm) * std::max(1, sms);
-        // items: DAGs by cost per tile, most expensive first; every tile of a DAG
-        std::vector<int32_t> order((size_t)n_dags);
-        std::iota(order.begin(), order.end(), 0);
+        // items: within each launch, DAGs by cost per tile, most expensive first; every tile of a DAG
         auto cost = [&](int32_t i) { return (double)B->dags[i]->h.pred.size() + 2.0 * B->dags[i]->h.E; };
-        std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return cost(x) > cost(y); });
         std::vector<int32_t> items;
-        for (int32_t i : order) {
-            const int64_t tiles = (B->n[i] + kTile - 1) / kTile;
-            for (int64_t t = 0; t < tiles; ++t) {
-                items.push_back(i);
-                items.push_back((int32_t)t);
+        std::vector<size_t> item_off;  // first item of each launch
+        int32_t max_E_global = 0;
+        int grid_global = 0;
+        B->grid = 0;
+        for (Launch &L : B->launches) {
+            int per_sm = 0;
+            cuda_check(batch_blocks_per_sm(L.win_smem, L.positive, B->n_warps, L.smem, &per_sm), "occupancy query");
+            L.grid = std::max(1, per_sm) * std::max(1, sms);
+            B->grid += L.grid;
+            std::stable_sort(L.dags.begin(), L.dags.end(), [&](int32_t x, int32_t y) { return cost(x) > cost(y); });
+            item_off.push_back(items.size() / 2);
+            for (int32_t i : L.dags) {
+                if (!L.win_smem) max_E_global = std::max(max_E_global, B->dags[i]->h.E);
+                const int64_t tiles = (B->n[i] + kTile - 1) / kTile;
+                for (int64_t t = 0; t < tiles; ++t) {
+                    items.push_back(i);
+                    items.push_back((int32_t)t);
+                }
             }
+            L.args.n_items = (int32_t)(items.size() / 2 - item_off.back());
+            if (!L.win_smem) grid_global = std::max(grid_global, L.grid);  // launches run one after another
         }
         B->n_items = (int64_t)items.size() / 2;
         if (B->n_items > (int64_t)INT32_MAX) throw McdError(MCD_ERR_INVALID, "too many work items");
@@ -108,7 +135,7 @@ int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0,
                      s_out = align_up(5 * E * 8, 256), s_args = align_up((size_t)n_dags * sizeof(KArgs), 256),
                      s_fargs = align_up((size_t)n_dags * sizeof(FArgs), 256),
                      s_items = align_up(items.size() * 4, 256),
-                     s_scr = any_global ? align_up((size_t)B->grid * max_E_global * kTile * 8, 256) : 0;
+                     s_scr = align_up((size_t)grid_global * max_E_global * kTile * 8, 256);
         B->zero_bytes = s_acc + s_hist + s_ctr;
         cuda_check(cudaMalloc(&B->dmem, B->zero_bytes + s_out + s_args + s_fargs + s_items + s_scr),
                    "batch allocation");
@@ -163,13 +190,15 @@ int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0,
         cuda_check(cudaMemcpy(d_args, ka.data(), ka.size() * sizeof(KArgs), cudaMemcpyHostToDevice), "upload");
         cuda_check(cudaMemcpy(B->d_fargs, fa.data(), fa.size() * sizeof(FArgs), cudaMemcpyHostToDevice), "upload");
         cuda_check(cudaMemcpy(d_items, items.data(), items.size() * 4, cudaMemcpyHostToDevice), "upload");
-        B->args.dags = d_args;
-        B->args.items = d_items;
-        B->args.n_items = (int32_t)B->n_items;
-        B->args.counter = counter;
-        B->args.scratch = scratch;
-        B->args.scratch_stride = (int64_t)max_E_global * kTile;
-        B->args.smem_bytes = (int32_t)B->smem;
+        for (size_t k = 0; k < B->launches.size(); ++k) {
+            Launch &L = B->launches[k];
+            L.args.dags = d_args;
+            L.args.items = d_items + 2 * item_off[k];
+            L.args.counter = counter + 16 * k;  // one queue head per launch, 64 bytes apart
+            L.args.scratch = L.win_smem ? nullptr : scratch;
+            L.args.scratch_stride = L.win_smem ? 0 : (int64_t)max_E_global * kTile;
+            L.args.smem_bytes = (int32_t)L.smem;
+        }
         *out = B;
     });
     if (rc != MCD_OK && B) {
@@ -198,7 +227,9 @@ int mcd_batch_run(mcd_batch *B) {
         if (!B->exec) {
             cuda_check(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
             cudaError_t e = cudaMemsetAsync(B->dmem, 0, B->zero_bytes, B->stream);
-            if (e == cudaSuccess) e = launch_batch_stats(B->args, B->n_warps, B->smem, B->grid, B->stream);
+            for (const Launch &L : B->launches)
+                if (e == cudaSuccess)
+                    e = launch_batch_stats(L.args, L.win_smem, L.positive, B->n_warps, L.smem, L.grid, B->stream);
             if (e == cudaSuccess)
                 e = launch_batch_finish(B->d_fargs, (int32_t)B->dags.size(), B->max_E, B->stream);
             cudaGraph_t graph = nullptr;
@@ -218,6 +249,17 @@ int mcd_batch_sync(mcd_batch *B) {
         cuda_check(cudaSetDevice(B->device), "cudaSetDevice");
         cuda_check(cudaStreamSynchronize(B->stream), "batch sync");
         for (mcd_dag *g : B->dags) check_device_error(g);
+    });
+}
+
+int mcd_batch_occupancy(int32_t n_warps, int64_t smem_bytes, int32_t *blocks_per_sm) {
+    return guarded([&] {
+        if (!blocks_per_sm || n_warps < 1 || n_warps > kMaxBatchWarps || smem_bytes < 0 ||
+            smem_bytes > (int64_t)kSmemMax)
+            throw McdError(MCD_ERR_INVALID, "bad arguments");
+        int per_sm = 0;
+        cuda_check(batch_blocks_per_sm(true, true, n_warps, (size_t)smem_bytes, &per_sm), "occupancy query");
+        *blocks_per_sm = per_sm;
     });
 }
 

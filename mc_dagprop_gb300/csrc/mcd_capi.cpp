@@ -216,7 +216,8 @@ int mcd_dag_create_ex(const mcd_dag_desc *desc, const mcd_generator *gen, const 
         if (!desc || !gen || !out) throw McdError(MCD_ERR_INVALID, "null argument");
         *out = nullptr;
         const int32_t nw = opts ? opts->n_warps : 0;
-        if (nw < 0 || nw > kMaxWarps) throw McdError(MCD_ERR_INVALID, "n_warps must be 0 (automatic) or 1..24");
+        if (nw < kBatchClassWarps || nw > kMaxWarps)
+            throw McdError(MCD_ERR_INVALID, "n_warps must be -1 (batch class), 0 (automatic) or 1..24");
         g = new mcd_dag();
         compile_dag(*desc, *gen, g->h, nw);
         cuda_check(cudaGetDevice(&g->device), "cudaGetDevice");

@@ -442,6 +442,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
     }
     if (const char *env = std::getenv("MCD_WARPS")) nw = std::atoi(env);
     if (n_warps > 0) nw = n_warps;
+    if (n_warps == kBatchClassWarps) nw = nw <= 2 ? 2 : nw <= 4 ? 4 : nw <= 8 ? 8 : nw <= 12 ? 12 : 24;
     nw = std::max(1, std::min(kMaxWarps, nw));
     H.n_warps = nw;
     // relative cost of an edge by delay kind (kernel time per edge, fixed = 1)

@@ -507,6 +507,9 @@ class Server {
         d["queued"] = i.queued;
         d["running"] = i.running;
         d["bytes_in_use"] = i.bytes_in_use;
+        d["compile_seconds"] = i.compile_seconds;
+        d["upload_seconds"] = i.upload_seconds;
+        d["launch_seconds"] = i.launch_seconds;
         return d;
     }
 
@@ -717,18 +720,29 @@ PYBIND11_MODULE(_core, m) {
         .def("stats", &Batch::stats, py::arg("i"), py::arg("hist") = false, "Statistics of propagator i")
         .def_property_readonly("items", &Batch::items, "Work items (DAG, 32-sample tile)")
         .def_property_readonly("grid", &Batch::grid, "CTAs of the persistent launch")
+        .def_static(
+            "occupancy",
+            [](int32_t n_warps, int64_t smem_bytes) {
+                int32_t per_sm = 0;
+                raise_status(mcd_batch_occupancy(n_warps, smem_bytes, &per_sm));
+                return per_sm;
+            },
+            py::arg("n_warps"), py::arg("smem_bytes"),
+            "CTAs per SM of the batch kernel at this block size and shared memory")
         .def_property_readonly("stream", &Batch::stream, "The batch's CUDA stream");
 
     py::class_<Server>(m, "Server")
         .def(py::init<int64_t, int, int, int, int>(), py::arg("memory_budget") = (int64_t)64 << 30,
-             py::arg("n_streams") = 2, py::arg("n_warps") = 8, py::arg("max_batch") = 0,
-             py::arg("compile_threads") = 4,
-             "Continuous-batching statistics server on the current GPU")
+             py::arg("n_streams") = 4, py::arg("n_warps") = 0, py::arg("max_batch") = 0,
+             py::arg("compile_threads") = 8,
+             "Continuous-batching statistics server on the current GPU (n_warps 0: per request, "
+             "batched by warps per CTA and CTAs per SM)")
         .def("submit", &Server::submit, py::arg("earliest"), py::arg("act_idx"), py::arg("act_duration"),
              py::arg("act_type"), py::arg("target"), py::arg("pred_offsets"), py::arg("pred_src"),
              py::arg("pred_act"), py::arg("max_delay"), py::arg("generator"), py::arg("seed0"), py::arg("n"),
              "Submit a request (flat DAG, generator, seeds seed0..seed0+n-1); returns a ticket")
         .def("wait", &Server::wait, py::arg("ticket"), py::arg("timeout_ms") = 0.0,
              "Statistics of a finished request (dict with latency_ms), None while pending")
-        .def("counters", &Server::counters, "completed, batches, queued, running, bytes_in_use");
+        .def("counters", &Server::counters,
+             "completed, batches, queued, running, bytes_in_use, and compile/upload/launch seconds");
 }

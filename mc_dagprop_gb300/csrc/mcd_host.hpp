@@ -44,7 +44,10 @@ struct McdError : std::runtime_error {
 // the two record staging buffers up to kMaxStageBytes; the whole CTA kSmemMax.
 constexpr size_t kMaxWindowBytes = 196 * 1024;
 constexpr int32_t kMaxWarps = 24;       // single-DAG kernel: 768 threads per CTA
-constexpr int32_t kMaxBatchWarps = 16;  // persistent batch kernel: 512 threads per CTA
+constexpr int32_t kMaxBatchWarps = 24;  // persistent batch kernel: 768 threads per CTA
+// n_warps request: automatic, rounded up to 2, 4, 8, 12 or 24 warps -- block
+// sizes whose CTAs fill an SM's 24 warps at the batch kernel's 80 registers
+constexpr int32_t kBatchClassWarps = -1;
 constexpr size_t kMaxStageBytes = 24 * 1024;
 constexpr size_t kMinStageBytes = 4 * 1024;
 constexpr size_t kMaxTableBytes = 16 * 1024;

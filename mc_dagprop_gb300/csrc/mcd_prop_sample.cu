@@ -8,10 +8,13 @@ namespace mcd {
 // Persistent statistics kernel over a batch of DAGs: each CTA takes (DAG, tile)
 // items from an atomic work queue (ordered longest first by the host) until the
 // queue is empty.  No CTA waits on another: the queue head is a plain counter.
+// One instantiation per (window on chip, positive times): every DAG of a launch
+// shares both, so only one propagation variant is inlined (fewer registers).
 // DAGs whose window is not on chip use per-CTA scratch rows (32 samples each).
 // Each DAG has its own shared-memory layout; the barrier pair lives outside
 // all of them, in static shared memory, so it never moves between items.
-__global__ void __launch_bounds__(512) k_batch_stats(const BatchArgs b) {
+template <bool WIN_SMEM, bool POSITIVE>
+__global__ void __launch_bounds__(768, 1) k_batch_stats(const BatchArgs b) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ KArgs s_args;
     __shared__ __align__(8) uint64_t s_bars[2];
@@ -26,26 +29,25 @@ __global__ void __launch_bounds__(512) k_batch_stats(const BatchArgs b) {
         if (threadIdx.x == 0) s_args = b.dags[it.x];
         __syncthreads();
         const KArgs &a = s_args;
-        if (a.smem_total > b.smem_bytes) {  // a layout larger than the launch's shared memory: never touch it
+        // a layout larger than the launch's shared memory, or of another variant: never touch it
+        if (a.smem_total > b.smem_bytes || (a.win_smem != 0) != WIN_SMEM || (a.positive != 0) != POSITIVE ||
+            a.n_warps * 32 != (int)blockDim.x) {
             if (threadIdx.x == 0) atomicOr(a.err, ERR_LAYOUT);
             __syncthreads();
             continue;
         }
-        bool ok;
-        if (a.win_smem) {
-            ok = a.positive
-                     ? propagate_tile<false, true, true, true>(a, it.y, nullptr, 0, true, smem, s_bars, reuse)
-                     : propagate_tile<false, true, true, false>(a, it.y, nullptr, 0, true, smem, s_bars, reuse);
-        } else {
-            double *rows = b.scratch + (int64_t)blockIdx.x * b.scratch_stride;
-            ok = a.positive
-                     ? propagate_tile<false, false, true, true>(a, it.y, rows, kTile, true, smem, s_bars, reuse)
-                     : propagate_tile<false, false, true, false>(a, it.y, rows, kTile, true, smem, s_bars, reuse);
-        }
+        double *rows = WIN_SMEM ? nullptr : b.scratch + (int64_t)blockIdx.x * b.scratch_stride;
+        const bool ok = propagate_tile<false, WIN_SMEM, true, POSITIVE>(a, it.y, rows, WIN_SMEM ? 0 : kTile, true,
+                                                                         smem, s_bars, reuse);
         reuse = true;
         if (!ok) return;
         __syncthreads();  // s_args / s_item are rewritten by the next item
     }
+}
+
+static void (*batch_kernel(bool win_smem, bool positive))(const BatchArgs) {
+    if (win_smem) return positive ? k_batch_stats<true, true> : k_batch_stats<true, false>;
+    return positive ? k_batch_stats<false, true> : k_batch_stats<false, false>;
 }
 
 cudaError_t launch_prop_sample(const KArgs &a, bool win_smem, bool stats, bool positive, dim3 grid, dim3 block,
@@ -65,18 +67,21 @@ cudaError_t launch_prop_sample(const KArgs &a, bool win_smem, bool stats, bool p
 }
 
 // Persistent batch launch: one CTA per SM slot, `blocks_per_sm` of them per SM.
-cudaError_t launch_batch_stats(const BatchArgs &b, int n_warps, size_t smem, int grid, cudaStream_t st) {
-    const cudaError_t e = raise_smem_limit((const void *)k_batch_stats, smem);
+cudaError_t launch_batch_stats(const BatchArgs &b, bool win_smem, bool positive, int n_warps, size_t smem, int grid,
+                               cudaStream_t st) {
+    void (*fn)(const BatchArgs) = batch_kernel(win_smem, positive);
+    const cudaError_t e = raise_smem_limit((const void *)fn, smem);
     if (e != cudaSuccess) return e;
-    k_batch_stats<<<grid, n_warps * 32, smem, st>>>(b);
+    fn<<<grid, n_warps * 32, smem, st>>>(b);
     return cudaGetLastError();
 }
 
 // CTAs of the batch kernel that fit on one SM at this block size and shared memory.
-cudaError_t batch_blocks_per_sm(int n_warps, size_t smem, int *out) {
-    const cudaError_t e = raise_smem_limit((const void *)k_batch_stats, smem);
+cudaError_t batch_blocks_per_sm(bool win_smem, bool positive, int n_warps, size_t smem, int *out) {
+    void (*fn)(const BatchArgs) = batch_kernel(win_smem, positive);
+    const cudaError_t e = raise_smem_limit((const void *)fn, smem);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k_batch_stats, n_warps * 32, smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, fn, n_warps * 32, smem);
 }
 
 }  // namespace mcd

@@ -1,17 +1,21 @@
 // mcd_server.cpp -- continuous-batching request server (no reference counterpart).
 //
 // Requests are (DAG, generator, seed0, n samples) asking for per-event
-// statistics.  submit() copies the inputs and returns a ticket at once; a pool
-// of host threads compiles the DAGs (mcd_compile.cpp); one scheduler thread
-//   - admits compiled requests while the device-memory budget allows, taking
-//     each request's block (compiled records, accumulators, outputs) from the
-//     stream-ordered allocator (cudaMallocAsync: no device-wide synchronisation);
-//   - whenever one of its stream slots is free, launches everything admitted as
-//     one batch (the persistent k_batch_stats over (request, tile) items, then
-//     the batched finish and the copy of the statistics to pinned host memory),
-//     so requests that arrive while earlier batches run are batched as soon as a
-//     slot frees up, and batches on different slots overlap on the GPU;
-//   - polls the slots' events, completes tickets and returns memory.
+// statistics.  submit() copies the inputs and returns a ticket at once.
+//   - A pool of host threads compiles the DAGs (mcd_compile.cpp) with warps per
+//     CTA from each DAG's width (rounded to 2, 4, 8 or 16), waits until the
+//     request's device block fits the memory budget, takes the block from the
+//     stream-ordered allocator and uploads the compiled records on its own
+//     stream: uploads run in parallel, off the scheduler.
+//   - Requests are batched by class: equal warps per CTA, equal CTAs per SM for
+//     their shared-memory layout (so no request lowers another's occupancy) and
+//     the same kernel variant (positive times or not).
+//   - One scheduler thread, whenever one of its stream slots is free, launches
+//     the uploaded requests of the class of the oldest waiting request as one
+//     batch (the persistent k_batch_stats over (request, tile) items, then the
+//     batched finish and the copy of the statistics to pinned host memory);
+//     batches on different slots overlap on the GPU.  It polls the slots'
+//     events, completes tickets and returns memory.
 // A request's statistics are the same alone and in any mix: every request has
 // its own accumulators and the accumulation is exact integer arithmetic.
 #include <cuda_runtime.h>
@@ -32,8 +36,9 @@
 #include "mcd_handle.hpp"
 
 namespace mcd {
-cudaError_t launch_batch_stats(const BatchArgs &b, int n_warps, size_t smem, int grid, cudaStream_t st);
-cudaError_t batch_blocks_per_sm(int n_warps, size_t smem, int *out);
+cudaError_t launch_batch_stats(const BatchArgs &b, bool win_smem, bool positive, int n_warps, size_t smem, int grid,
+                               cudaStream_t st);
+cudaError_t batch_blocks_per_sm(bool win_smem, bool positive, int n_warps, size_t smem, int *out);
 cudaError_t launch_batch_finish(const FArgs *fs, int32_t n_dags, int32_t max_events, cudaStream_t st);
 }  // namespace mcd
 
@@ -44,28 +49,8 @@ namespace {
 
 enum State : int { Q_COMPILE = 0, Q_READY = 1, Q_RUNNING = 2, Q_DONE = 3, Q_FAILED = 4 };
 
-struct Request {
-    int64_t ticket = 0;
-    // inputs (copied at submit)
-    std::vector<double> earliest, act_duration;
-    std::vector<int32_t> act_idx, act_type, target, pred_src, pred_act;
-    std::vector<int64_t> pred_offsets;
-    double max_delay = 0.0;
-    mcd_generator gen;
-    int64_t seed0 = 0, n = 0;
-    // compiled
-    HostDag h;
-    size_t bytes = 0;  // device block
-    std::string error;
-    // device (while running)
-    char *dblock = nullptr;
-    // results
-    std::vector<double> out;  // 5 x E: mean, p50, p90, p99, p_on_time
-    std::atomic<int> state{Q_COMPILE};
-    Clock::time_point t_submit, t_done;
-};
-
-// Offsets of one request's device block.
+// Offsets of one request's device block: compiled records, then the
+// accumulators (zeroed at upload), then the statistics.
 struct Layout {
     size_t ev, pred, aux, dist, alias, wk, meta, earliest, ub, err, acc, hist, out, total;
 };
@@ -95,16 +80,42 @@ Layout layout_of(const HostDag &h) {
     return L;
 }
 
+struct Request {
+    int64_t ticket = 0;
+    // inputs (copied at submit, dropped after compile)
+    std::vector<double> earliest, act_duration;
+    std::vector<int32_t> act_idx, act_type, target, pred_src, pred_act;
+    std::vector<int64_t> pred_offsets;
+    double max_delay = 0.0;
+    mcd_generator gen;
+    int64_t seed0 = 0, n = 0;
+    // compiled (records dropped after upload)
+    HostDag h;
+    Layout lay{};
+    size_t bytes = 0;       // device block
+    int32_t per_sm = 1;     // batch class: (h.n_warps, per_sm)
+    double tile_cost = 0;   // work per 32-sample tile, for longest-first ordering
+    std::string error;
+    // device (uploaded until the batch completes)
+    char *dblock = nullptr;
+    KArgs ka{};
+    FArgs fa{};
+    // results
+    std::vector<double> out;  // 5 x E: mean, p50, p90, p99, p_on_time
+    std::atomic<int> state{Q_COMPILE};
+    Clock::time_point t_submit, t_done;
+};
+
 struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     bool busy = false;
     std::vector<Request *> batch;
-    char *meta_dev = nullptr;  // KArgs[], FArgs[], items, queue head
+    char *meta_dev = nullptr;   // KArgs[], FArgs[], items, queue head
+    char *meta_pinned = nullptr;
     size_t meta_bytes = 0;
-    double *pinned = nullptr;  // statistics of the batch, host side
+    double *pinned = nullptr;   // statistics of the batch, host side
     size_t pinned_elems = 0;
-    std::vector<char> meta_host;
 };
 
 }  // namespace
@@ -114,7 +125,7 @@ struct mcd_server {
     int device = 0, sms = 1;
     cudaMemPool_t pool = nullptr;
     std::mutex mu;
-    std::condition_variable cv_compile, cv_sched, cv_done;
+    std::condition_variable cv_compile, cv_sched, cv_done, cv_budget;
     std::deque<Request *> to_compile, ready;
     std::unordered_map<int64_t, std::unique_ptr<Request>> all;
     std::vector<Slot> slots;
@@ -123,74 +134,27 @@ struct mcd_server {
     std::atomic<bool> stop{false};
     int64_t next_ticket = 1;
     int64_t bytes_in_use = 0;
-    int64_t completed = 0, launched_batches = 0, running = 0;
-    std::string fatal;  // a CUDA failure of the scheduler: every later call reports it
+    int64_t completed = 0, launched_batches = 0, running = 0, pending = 0;
+    double compile_s = 0.0, upload_s = 0.0, launch_s = 0.0;
+    char *zeros = nullptr;  // pinned zero bytes: accumulators are cleared by the copy engines
+    std::string fatal;      // a CUDA failure of the scheduler: every later call reports it
 };
 
 namespace {
+constexpr size_t kZeroBytes = 8u << 20;
+}  // namespace
 
-void compile_loop(mcd_server *S) {
-    for (;;) {
-        Request *r = nullptr;
-        {
-            std::unique_lock<std::mutex> lk(S->mu);
-            S->cv_compile.wait(lk, [&] { return S->stop || !S->to_compile.empty(); });
-            if (S->stop) return;
-            r = S->to_compile.front();
-            S->to_compile.pop_front();
-        }
-        try {
-            mcd_dag_desc d{};
-            d.n_events = (int32_t)r->earliest.size();
-            d.earliest = r->earliest.data();
-            d.n_activities = (int32_t)r->act_idx.size();
-            d.act_idx = r->act_idx.data();
-            d.act_duration = r->act_duration.data();
-            d.act_type = r->act_type.data();
-            d.n_targets = (int32_t)r->target.size();
-            d.target = r->target.data();
-            d.pred_offsets = r->pred_offsets.data();
-            d.pred_src = r->pred_src.data();
-            d.pred_act = r->pred_act.data();
-            d.max_delay = r->max_delay;
-            compile_dag(d, r->gen, r->h, S->opt.n_warps);
-            r->bytes = layout_of(r->h).total;
-            if ((int64_t)r->bytes > S->opt.memory_budget)
-                throw McdError(MCD_ERR_INVALID, "request needs more device memory than the server's budget");
-            std::lock_guard<std::mutex> lk(S->mu);
-            r->state = Q_READY;
-            S->ready.push_back(r);
-        } catch (const std::exception &e) {
-            std::lock_guard<std::mutex> lk(S->mu);
-            r->error = e.what();
-            r->state = Q_FAILED;
-            r->t_done = Clock::now();
-            S->cv_done.notify_all();
-        }
-        S->cv_sched.notify_one();
-    }
-}
+namespace {
 
-// Uploads one request's compiled records into its block; returns its kernel
-// and finish arguments.
-void stage_request(mcd_server *S, Request *r, cudaStream_t st, KArgs &a, FArgs &f) {
+double seconds_since(Clock::time_point t0) { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+
+// Kernel and finish arguments of an uploaded request.
+void request_args(Request *r) {
     const HostDag &h = r->h;
-    const Layout L = layout_of(h);
+    const Layout &L = r->lay;
     char *b = r->dblock;
-    auto up = [&](size_t off, const void *src, size_t bytes) {
-        if (bytes) cuda_check(cudaMemcpyAsync(b + off, src, bytes, cudaMemcpyHostToDevice, st), "request upload");
-    };
-    up(L.ev, h.ev.data(), h.ev.size() * sizeof(EvRec));
-    up(L.pred, h.pred.data(), h.pred.size() * sizeof(PredRec));
-    up(L.aux, h.aux.data(), h.aux.size() * sizeof(LinkRec));
-    up(L.dist, h.dist.data(), h.dist.size() * sizeof(DistParam));
-    up(L.alias, h.alias.data(), h.alias.size() * sizeof(AliasEntry));
-    up(L.wk, h.wk_off.data(), h.wk_off.size() * 4);
-    up(L.meta, h.stage_meta.data(), h.stage_meta.size() * 4);
-    up(L.earliest, h.earliest.data(), (size_t)h.E * 8);
-    up(L.ub, h.ub.data(), (size_t)h.E * 8);
-    cuda_check(cudaMemsetAsync(b + L.err, 0, L.out - L.err, st), "request reset");  // flags + accumulators
     const StatsParams sp = stats_params(h, r->n);
+    KArgs &a = r->ka;
     a = KArgs{};
     a.ev = reinterpret_cast<const EvRec *>(b + L.ev);
     a.pred = reinterpret_cast<const PredRec *>(b + L.pred);
@@ -224,6 +188,7 @@ void stage_request(mcd_server *S, Request *r, cudaStream_t st, KArgs &a, FArgs &
     a.hist_inv_w = sp.inv_w;
     a.acc = reinterpret_cast<unsigned long long *>(b + L.acc);
     a.hist = reinterpret_cast<uint32_t *>(b + L.hist);
+    FArgs &f = r->fa;
     f = FArgs{};
     f.acc = a.acc;
     f.hist = a.hist;
@@ -242,86 +207,220 @@ void stage_request(mcd_server *S, Request *r, cudaStream_t st, KArgs &a, FArgs &
     f.p_on_time = o + 4 * (size_t)h.E;
 }
 
-// Launches one batch on a free slot (scheduler thread; the lock is not held).
+// Uploads the compiled records into the request's block and zeroes its
+// accumulators; returns when the copies have landed.  Only copies: a kernel
+// (such as a memset) would queue behind the persistent batch launches that
+// hold every SM, while the copy engines are free.
+void upload_request(const mcd_server *S, Request *r, cudaStream_t st) {
+    const HostDag &h = r->h;
+    const Layout &L = r->lay;
+    cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&r->dblock), r->bytes, st), "request allocation");
+    char *b = r->dblock;
+    auto up = [&](size_t off, const void *src, size_t bytes) {
+        if (bytes) cuda_check(cudaMemcpyAsync(b + off, src, bytes, cudaMemcpyHostToDevice, st), "request upload");
+    };
+    up(L.ev, h.ev.data(), h.ev.size() * sizeof(EvRec));
+    up(L.pred, h.pred.data(), h.pred.size() * sizeof(PredRec));
+    up(L.aux, h.aux.data(), h.aux.size() * sizeof(LinkRec));
+    up(L.dist, h.dist.data(), h.dist.size() * sizeof(DistParam));
+    up(L.alias, h.alias.data(), h.alias.size() * sizeof(AliasEntry));
+    up(L.wk, h.wk_off.data(), h.wk_off.size() * 4);
+    up(L.meta, h.stage_meta.data(), h.stage_meta.size() * 4);
+    up(L.earliest, h.earliest.data(), (size_t)h.E * 8);
+    up(L.ub, h.ub.data(), (size_t)h.E * 8);
+    for (size_t off = L.err; off < L.out; off += kZeroBytes)  // flags + accumulators
+        up(off, S->zeros, std::min(kZeroBytes, L.out - off));
+    cuda_check(cudaStreamSynchronize(st), "request upload sync");
+}
+
+template <typename T>
+void drop(std::vector<T> &v) {
+    std::vector<T>().swap(v);
+}
+
+void compile_loop(mcd_server *S) {
+    cudaStream_t st = nullptr;
+    if (cudaSetDevice(S->device) != cudaSuccess || cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (S->fatal.empty()) S->fatal = "compile thread: no CUDA stream";
+        S->cv_done.notify_all();
+        return;
+    }
+    for (;;) {
+        Request *r = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            S->cv_compile.wait(lk, [&] { return S->stop || !S->to_compile.empty(); });
+            if (S->stop) break;
+            r = S->to_compile.front();
+            S->to_compile.pop_front();
+        }
+        bool holds_budget = false;
+        try {
+            const Clock::time_point t0 = Clock::now();
+            mcd_dag_desc d{};
+            d.n_events = (int32_t)r->earliest.size();
+            d.earliest = r->earliest.data();
+            d.n_activities = (int32_t)r->act_idx.size();
+            d.act_idx = r->act_idx.data();
+            d.act_duration = r->act_duration.data();
+            d.act_type = r->act_type.data();
+            d.n_targets = (int32_t)r->target.size();
+            d.target = r->target.data();
+            d.pred_offsets = r->pred_offsets.data();
+            d.pred_src = r->pred_src.data();
+            d.pred_act = r->pred_act.data();
+            d.max_delay = r->max_delay;
+            compile_dag(d, r->gen, r->h, S->opt.n_warps > 0 ? S->opt.n_warps : kBatchClassWarps);
+            drop(r->earliest);
+            drop(r->act_duration);
+            drop(r->act_idx);
+            drop(r->act_type);
+            drop(r->target);
+            drop(r->pred_src);
+            drop(r->pred_act);
+            drop(r->pred_offsets);
+            if (!r->h.win_smem)  // the served kernel keeps every window on chip
+                throw McdError(MCD_ERR_INVALID, "request DAG's window does not fit in shared memory");
+            r->lay = layout_of(r->h);
+            r->bytes = r->lay.total;
+            if ((int64_t)r->bytes > S->opt.memory_budget)
+                throw McdError(MCD_ERR_INVALID, "request needs more device memory than the server's budget");
+            int per_sm = 0;
+            cuda_check(batch_blocks_per_sm(true, r->h.positive, r->h.n_warps, (size_t)r->h.smem_total, &per_sm),
+                       "occupancy query");
+            r->per_sm = std::max(1, per_sm);
+            r->tile_cost = (double)r->h.pred.size() + 2.0 * r->h.E;
+            const double t_compile = seconds_since(t0);
+            {  // admission: wait until the block fits the budget
+                std::unique_lock<std::mutex> lk(S->mu);
+                S->compile_s += t_compile;
+                S->cv_budget.wait(lk, [&] {
+                    return S->stop || S->bytes_in_use + (int64_t)r->bytes <= S->opt.memory_budget;
+                });
+                if (S->stop) break;
+                S->bytes_in_use += (int64_t)r->bytes;
+                holds_budget = true;
+            }
+            const Clock::time_point t1 = Clock::now();
+            upload_request(S, r, st);
+            request_args(r);
+            HostDag &h = r->h;  // only the scalars stay
+            drop(h.ev);
+            drop(h.pred);
+            drop(h.aux);
+            drop(h.dist);
+            drop(h.alias);
+            drop(h.wk_off);
+            drop(h.stage_meta);
+            drop(h.link_kd);
+            drop(h.link_v);
+            drop(h.link_dv);
+            drop(h.earliest);
+            drop(h.ub);
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->upload_s += seconds_since(t1);
+            r->state = Q_READY;
+            S->ready.push_back(r);
+        } catch (const std::exception &e) {
+            if (r->dblock) {
+                cudaFreeAsync(r->dblock, st);
+                cudaStreamSynchronize(st);
+                r->dblock = nullptr;
+            }
+            std::lock_guard<std::mutex> lk(S->mu);
+            if (holds_budget) {
+                S->bytes_in_use -= (int64_t)r->bytes;
+                S->cv_budget.notify_all();
+            }
+            r->error = e.what();
+            r->state = Q_FAILED;
+            r->t_done = Clock::now();
+            S->pending -= 1;
+            S->cv_done.notify_all();
+        }
+        S->cv_sched.notify_one();
+    }
+    cudaStreamDestroy(st);
+}
+
+// Launches one batch of uploaded requests of one class on a free slot
+// (scheduler thread; the lock is not held).
 void launch_batch(mcd_server *S, Slot &slot, std::vector<Request *> &batch) {
+    const Clock::time_point t0 = Clock::now();
     cudaStream_t st = slot.stream;
     const size_t nb = batch.size();
-    std::vector<KArgs> ka(nb);
-    std::vector<FArgs> fa(nb);
-    std::vector<int32_t> items;
-    size_t smem = 0, out_elems = 0;
+    // longest first: requests by cost per tile, descending
+    std::vector<int32_t> order(nb);
+    for (size_t i = 0; i < nb; ++i) order[i] = (int32_t)i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int32_t x, int32_t y) { return batch[x]->tile_cost > batch[y]->tile_cost; });
+    size_t smem = 0, out_elems = 0, n_items = 0;
     int32_t max_E = 0;
-    for (size_t i = 0; i < nb; ++i) {
-        Request *r = batch[i];
-        cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&r->dblock), r->bytes, st), "request allocation");
-        stage_request(S, r, st, ka[i], fa[i]);
+    for (Request *r : batch) {
         smem = std::max(smem, (size_t)r->h.smem_total);
         max_E = std::max(max_E, r->h.E);
         out_elems += (size_t)r->h.E * 5;
-        const int64_t tiles = (r->n + kTile - 1) / kTile;
-        for (int64_t t = 0; t < tiles; ++t) {
-            items.push_back((int32_t)i);
-            items.push_back((int32_t)t);
-        }
-    }
-    // longest first: requests by cost per tile, descending
-    {
-        std::vector<int32_t> order(nb);
-        for (size_t i = 0; i < nb; ++i) order[i] = (int32_t)i;
-        std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
-            return batch[x]->h.pred.size() + 2 * (size_t)batch[x]->h.E > batch[y]->h.pred.size() + 2 * (size_t)batch[y]->h.E;
-        });
-        std::vector<int32_t> sorted;
-        sorted.reserve(items.size());
-        for (int32_t i : order) {
-            const int64_t tiles = (batch[i]->n + kTile - 1) / kTile;
-            for (int64_t t = 0; t < tiles; ++t) {
-                sorted.push_back(i);
-                sorted.push_back((int32_t)t);
-            }
-        }
-        items.swap(sorted);
+        n_items += (size_t)((r->n + kTile - 1) / kTile);
     }
     const size_t s_ka = align_up(nb * sizeof(KArgs), 256), s_fa = align_up(nb * sizeof(FArgs), 256),
-                 s_items = align_up(items.size() * 4, 256), s_ctr = 256;
+                 s_items = align_up(n_items * 8, 256), s_ctr = 256;
     const size_t need = s_ka + s_fa + s_items + s_ctr;
-    if (need > slot.meta_bytes) {
-        if (slot.meta_dev) cuda_check(cudaFreeAsync(slot.meta_dev, st), "slot metadata free");
+    if (need > slot.meta_bytes) {  // the slot is idle: its stream has nothing in flight
+        if (slot.meta_dev) cuda_check(cudaFree(slot.meta_dev), "slot metadata free");
+        if (slot.meta_pinned) cuda_check(cudaFreeHost(slot.meta_pinned), "slot metadata free");
+        slot.meta_dev = nullptr;
+        slot.meta_pinned = nullptr;
+        slot.meta_bytes = 0;
+        cuda_check(cudaMalloc(reinterpret_cast<void **>(&slot.meta_dev), need * 2), "slot metadata");
+        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&slot.meta_pinned), need * 2, cudaHostAllocDefault),
+                   "slot metadata");
         slot.meta_bytes = need * 2;
-        cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&slot.meta_dev), slot.meta_bytes, st), "slot metadata");
     }
     if (out_elems > slot.pinned_elems) {
-        cuda_check(cudaStreamSynchronize(st), "slot sync");
-        if (slot.pinned) cudaFreeHost(slot.pinned);
-        slot.pinned_elems = out_elems * 2;
-        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&slot.pinned), slot.pinned_elems * 8, cudaHostAllocDefault),
+        if (slot.pinned) cuda_check(cudaFreeHost(slot.pinned), "pinned results free");
+        slot.pinned = nullptr;
+        slot.pinned_elems = 0;
+        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&slot.pinned), out_elems * 2 * 8, cudaHostAllocDefault),
                    "pinned results");
+        slot.pinned_elems = out_elems * 2;
     }
-    // metadata in one host buffer, one upload (the buffer stays alive until the slot completes)
-    slot.meta_host.assign(need, 0);
-    std::memcpy(slot.meta_host.data(), ka.data(), nb * sizeof(KArgs));
-    std::memcpy(slot.meta_host.data() + s_ka, fa.data(), nb * sizeof(FArgs));
-    std::memcpy(slot.meta_host.data() + s_ka + s_fa, items.data(), items.size() * 4);
-    cuda_check(cudaMemcpyAsync(slot.meta_dev, slot.meta_host.data(), need, cudaMemcpyHostToDevice, st), "batch upload");
+    // metadata straight into pinned memory, one upload
+    char *mh = slot.meta_pinned;
+    auto *ka = reinterpret_cast<KArgs *>(mh);
+    auto *fa = reinterpret_cast<FArgs *>(mh + s_ka);
+    auto *items = reinterpret_cast<int32_t *>(mh + s_ka + s_fa);
+    for (size_t i = 0; i < nb; ++i) {
+        ka[i] = batch[i]->ka;
+        fa[i] = batch[i]->fa;
+    }
+    size_t k = 0;
+    for (int32_t i : order) {
+        const int64_t tiles = (batch[i]->n + kTile - 1) / kTile;
+        for (int64_t t = 0; t < tiles; ++t) {
+            items[k++] = i;
+            items[k++] = (int32_t)t;
+        }
+    }
+    std::memset(mh + s_ka + s_fa + s_items, 0, s_ctr);  // queue head
+    cuda_check(cudaMemcpyAsync(slot.meta_dev, mh, need, cudaMemcpyHostToDevice, st), "batch upload");
     BatchArgs ba{};
     ba.dags = reinterpret_cast<const KArgs *>(slot.meta_dev);
     ba.items = reinterpret_cast<const int32_t *>(slot.meta_dev + s_ka + s_fa);
-    ba.n_items = (int32_t)(items.size() / 2);
+    ba.n_items = (int32_t)n_items;
     ba.counter = reinterpret_cast<unsigned int *>(slot.meta_dev + s_ka + s_fa + s_items);
-    ba.scratch = nullptr;  // requests need their window in shared memory (checked at admission)
+    ba.scratch = nullptr;  // requests keep their window in shared memory (checked at compile)
     ba.scratch_stride = 0;
     ba.smem_bytes = (int32_t)smem;
-    int per_sm = 1;
-    cuda_check(batch_blocks_per_sm(S->opt.n_warps, smem, &per_sm), "occupancy");
-    const int grid = std::max(1, per_sm) * S->sms;
-    cuda_check(launch_batch_stats(ba, S->opt.n_warps, smem, grid, st), "batch launch");
+    const int32_t nw = batch[0]->h.n_warps;
+    const int grid = batch[0]->per_sm * S->sms;  // the class's CTAs per SM, on every SM
+    cuda_check(launch_batch_stats(ba, true, batch[0]->h.positive, nw, smem, grid, st), "batch launch");
     cuda_check(launch_batch_finish(reinterpret_cast<const FArgs *>(slot.meta_dev + s_ka), (int32_t)nb, max_E, st),
                "batch finish");
     size_t pos = 0;
     for (Request *r : batch) {
         const size_t e5 = (size_t)r->h.E * 5;
-        cuda_check(cudaMemcpyAsync(slot.pinned + pos, r->dblock + layout_of(r->h).out, e5 * 8, cudaMemcpyDeviceToHost,
-                                   st),
+        cuda_check(cudaMemcpyAsync(slot.pinned + pos, r->dblock + r->lay.out, e5 * 8, cudaMemcpyDeviceToHost, st),
                    "results download");
         cuda_check(cudaFreeAsync(r->dblock, st), "request free");
         pos += e5;
@@ -329,6 +428,8 @@ void launch_batch(mcd_server *S, Slot &slot, std::vector<Request *> &batch) {
     cuda_check(cudaEventRecord(slot.done, st), "event record");
     slot.batch = batch;
     slot.busy = true;
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->launch_s += seconds_since(t0);
 }
 
 void complete_slot(mcd_server *S, Slot &slot) {
@@ -350,7 +451,33 @@ void complete_slot(mcd_server *S, Slot &slot) {
     }
     slot.batch.clear();
     slot.busy = false;
+    S->cv_budget.notify_all();
     S->cv_done.notify_all();
+}
+
+// The uploaded requests of the oldest waiting request's class, oldest first
+// (caller holds the lock).
+std::vector<Request *> take_class(mcd_server *S) {
+    std::vector<Request *> batch;
+    if (S->ready.empty()) return batch;
+    const Request *first = S->ready.front();
+    const int32_t nw = first->h.n_warps, per_sm = first->per_sm;
+    const bool positive = first->h.positive;
+    std::deque<Request *> rest;
+    for (Request *r : S->ready) {
+        if (r->h.n_warps == nw && r->per_sm == per_sm && r->h.positive == positive &&
+            (S->opt.max_batch <= 0 || (int32_t)batch.size() < S->opt.max_batch))
+            batch.push_back(r);
+        else
+            rest.push_back(r);
+    }
+    S->ready.swap(rest);
+    for (Request *r : batch) {
+        r->state = Q_RUNNING;
+        S->running += 1;
+        S->pending -= 1;
+    }
+    return batch;
 }
 
 void schedule_loop(mcd_server *S) {
@@ -369,22 +496,7 @@ void schedule_loop(mcd_server *S) {
                 std::vector<Request *> batch;
                 {
                     std::lock_guard<std::mutex> lk(S->mu);
-                    while (!S->ready.empty() && (S->opt.max_batch <= 0 || (int32_t)batch.size() < S->opt.max_batch)) {
-                        Request *r = S->ready.front();
-                        if (S->bytes_in_use + (int64_t)r->bytes > S->opt.memory_budget) break;
-                        S->ready.pop_front();
-                        if (!r->h.win_smem) {  // the served kernel keeps every window on chip
-                            r->error = "request DAG's window does not fit in shared memory";
-                            r->state = Q_FAILED;
-                            r->t_done = Clock::now();
-                            S->cv_done.notify_all();
-                            continue;
-                        }
-                        S->bytes_in_use += (int64_t)r->bytes;
-                        S->running += 1;
-                        r->state = Q_RUNNING;
-                        batch.push_back(r);
-                    }
+                    batch = take_class(S);
                 }
                 if (batch.empty()) break;
                 launch_batch(S, slot, batch);
@@ -403,6 +515,8 @@ void schedule_loop(mcd_server *S) {
             S->fatal = e.what();
             S->stop = true;
             S->cv_done.notify_all();
+            S->cv_budget.notify_all();
+            S->cv_compile.notify_all();
             return;
         }
     }
@@ -415,7 +529,7 @@ extern "C" {
 int mcd_server_create(const mcd_server_options *opt, mcd_server **out) {
     return guarded([&] {
         if (!opt || !out) throw McdError(MCD_ERR_INVALID, "null argument");
-        if (opt->memory_budget <= 0 || opt->n_streams < 1 || opt->n_streams > 16 || opt->n_warps < 1 ||
+        if (opt->memory_budget <= 0 || opt->n_streams < 1 || opt->n_streams > 16 || opt->n_warps < 0 ||
             opt->n_warps > kMaxBatchWarps || opt->compile_threads < 1 || opt->compile_threads > 256)
             throw McdError(MCD_ERR_INVALID, "bad server options");
         auto S = std::make_unique<mcd_server>();
@@ -425,6 +539,9 @@ int mcd_server_create(const mcd_server_options *opt, mcd_server **out) {
         cuda_check(cudaDeviceGetDefaultMemPool(&S->pool, S->device), "memory pool");
         uint64_t keep = (uint64_t)opt->memory_budget;  // freed blocks stay in the pool for reuse
         cuda_check(cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep), "pool threshold");
+        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&S->zeros), kZeroBytes, cudaHostAllocDefault),
+                   "pinned zeros");
+        std::memset(S->zeros, 0, kZeroBytes);
         S->slots.resize((size_t)opt->n_streams);
         for (Slot &s : S->slots) {
             cuda_check(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "stream create");
@@ -445,18 +562,22 @@ void mcd_server_destroy(mcd_server *S) {
     }
     S->cv_compile.notify_all();
     S->cv_sched.notify_all();
+    S->cv_budget.notify_all();
     if (S->scheduler.joinable()) S->scheduler.join();
     for (std::thread &t : S->compilers)
         if (t.joinable()) t.join();
     cudaSetDevice(S->device);
     for (Slot &s : S->slots) {
         if (s.stream) cudaStreamSynchronize(s.stream);
-        if (s.meta_dev) cudaFreeAsync(s.meta_dev, s.stream);
-        if (s.stream) cudaStreamSynchronize(s.stream);
+        if (s.meta_dev) cudaFree(s.meta_dev);
+        if (s.meta_pinned) cudaFreeHost(s.meta_pinned);
         if (s.pinned) cudaFreeHost(s.pinned);
         if (s.done) cudaEventDestroy(s.done);
         if (s.stream) cudaStreamDestroy(s.stream);
     }
+    for (auto &kv : S->all)  // uploaded requests that never ran
+        if (kv.second->dblock && kv.second->state != Q_RUNNING) cudaFree(kv.second->dblock);
+    if (S->zeros) cudaFreeHost(S->zeros);
     delete S;
 }
 
@@ -488,6 +609,7 @@ int mcd_server_submit(mcd_server *S, const mcd_dag_desc *d, const mcd_generator 
         *ticket = r->ticket;
         S->to_compile.push_back(r.get());
         S->all[r->ticket] = std::move(r);
+        S->pending += 1;
         S->cv_compile.notify_one();
     });
 }
@@ -535,9 +657,12 @@ int mcd_server_counters(mcd_server *S, mcd_server_info *info) {
         std::lock_guard<std::mutex> lk(S->mu);
         info->completed = S->completed;
         info->batches = S->launched_batches;
-        info->queued = (int64_t)(S->to_compile.size() + S->ready.size());
+        info->queued = S->pending;
         info->bytes_in_use = S->bytes_in_use;
         info->running = S->running;
+        info->compile_seconds = S->compile_s;
+        info->upload_seconds = S->upload_s;
+        info->launch_seconds = S->launch_s;
     });
 }
 

@@ -20,7 +20,7 @@ def _prop(flat, gen, nw):
                                               flat["pred_src"], flat["pred_act"], flat["max_delay"], g, n_warps=nw)
 
 
-@pytest.mark.parametrize("nw", [4, 16])
+@pytest.mark.parametrize("nw", [4, 16, 24])
 def test_batch_equals_single_dag_statistics(cuda, nw):
     dags = W.mixed_dags(seed=5, n_dags=10, ev_lo=60, ev_hi=4000, s_lo=40, s_hi=3000, five_types=True)
     props, seed0, ns = [], [], []
@@ -34,6 +34,11 @@ def test_batch_equals_single_dag_statistics(cuda, nw):
     seed0.append(10**6)
     ns.append(100)
     assert props[-1].info()["window_in_smem"] is False
+    # one DAG with negative times (the general-key kernel variant: a launch of its own)
+    neg = dict(dags[0][0], earliest=dags[0][0]["earliest"] - 500.0)
+    props.append(_prop(neg, dags[0][1], nw))
+    seed0.append(2 * 10**6)
+    ns.append(200)
     batch = m.Batch(props, seed0, ns)
     assert batch.items == sum((n + 31) // 32 for n in ns)
     for rep in range(2):

@@ -22,10 +22,11 @@ def _submit(server, flat, gen, seed0, n):
                          W.to_generator(m, gen), seed0, n)
 
 
-@pytest.mark.parametrize("n_streams,budget", [(2, 8 << 30), (3, 64 << 20)])
-def test_served_results_equal_alone(cuda, n_streams, budget):
+@pytest.mark.parametrize("n_streams,budget,n_warps", [(2, 8 << 30, 8), (3, 64 << 20, 0), (4, 8 << 30, 0)])
+def test_served_results_equal_alone(cuda, n_streams, budget, n_warps):
+    """n_warps 0: each request with its own warps per CTA, batched by class."""
     reqs = W.mixed_dags(seed=9, n_dags=24, ev_lo=50, ev_hi=3000, s_lo=64, s_hi=4000, five_types=True)
-    server = m.Server(memory_budget=budget, n_streams=n_streams, n_warps=8, compile_threads=4)
+    server = m.Server(memory_budget=budget, n_streams=n_streams, n_warps=n_warps, compile_threads=4)
     tickets = []
     for i, (flat, gen, n, s0) in enumerate(reqs):
         tickets.append(_submit(server, flat, gen, s0, n))

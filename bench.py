@@ -422,7 +422,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--samples", type=int, default=19456)
-    ap.add_argument("--e2e-samples", type=int, default=512)
+    ap.add_argument("--e2e-samples", type=int, default=2432)
     ap.add_argument("--layers", type=int, default=2000)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--workload", default="single", choices=["single", "batched", "gradient", "serving"])
@@ -537,6 +537,13 @@ def main():
     e2e = None
     if rank == 0:
         n2 = args.e2e_samples
+        try:  # pinned host outputs: at most a quarter of the available host memory
+            with open("/proc/meminfo") as f:
+                avail = int(next(ln for ln in f if ln.startswith("MemAvailable")).split()[1]) * 1024
+            while n2 > 32 and n2 * (8 + 12 * E + 8 * L) > avail // 4:
+                n2 = n2 // 64 * 32
+        except (OSError, StopIteration, ValueError):
+            pass
         bufs = []
         for nbytes in (n2 * 8, n2 * E * 8, n2 * L * 8, n2 * E * 4):
             p = C.c_void_p()

@@ -134,6 +134,13 @@ int mcd_dag_describe(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag
 int32_t mcd_dag_node_count(const mcd_dag *dag);
 int32_t mcd_dag_activity_count(const mcd_dag *dag);
 int mcd_dag_get_info(const mcd_dag *dag, mcd_dag_info *info);
+/* Random-number streams of the links ([activity_count] each): a sampled link's
+ * draws come from Philox4x32-10 block block[l] (counter: sample seed, block,
+ * attempt); word[l] in 0..3 is the one 32-bit word an exponential or small
+ * empirical link takes from it (up to four such links first referenced by one
+ * event share a block), -1 when the link uses the whole block (gamma, large
+ * empirical tables).  block[l] = -1 for links of fixed duration. */
+int mcd_dag_link_streams(const mcd_dag *dag, int32_t *block, int32_t *word);
 /* The handle's stream (a cudaStream_t), for callers that order their own work on it. */
 void *mcd_dag_stream(const mcd_dag *dag);
 

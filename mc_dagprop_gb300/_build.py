@@ -13,10 +13,16 @@ copy shipped inside PyTorch's include directory.
 """
 from __future__ import annotations
 
+import sys
+
+# Run as a script, this file's directory leads sys.path, and the package's own
+# modules (types.py) would shadow the standard library's.
+if sys.path and sys.path[0] and __name__ == "__main__":
+    sys.path.pop(0)
+
 import os
 import shutil
 import subprocess
-import sys
 import sysconfig
 from concurrent.futures import ThreadPoolExecutor
 

@@ -101,14 +101,27 @@ void check_device_error(mcd_dag *g) {
 
 namespace {
 
-// Samples per chunk for the host-buffer entry points: two chunk buffer sets
-// (sample-minor rows + sample-major rows) within ~2 GiB, a multiple of 32.
-int64_t host_chunk(const mcd_dag *g, int64_t n) {
+// Samples per chunk for the host-buffer entry points, a multiple of 32, and the
+// number of chunk buffer sets (sample-minor rows + sample-major rows): one when
+// all n samples fit one chunk, else two (alternating streams overlap one
+// chunk's launch with the other's transposes and copies).  A chunk is one
+// launch in which every 32-sample tile walks the whole DAG, so a launch of few
+// tiles leaves SMs idle: chunks are as large as a workspace of a quarter of the
+// device memory not otherwise in use (at most 32 GiB) allows.
+int64_t host_chunk(const mcd_dag *g, int64_t n, int *sets) {
     const double per_sample = 2.0 * (12.0 * g->h.E + 8.0 * g->h.L) + 8.0;
-    int64_t c = (int64_t)((double)(1ll << 30) / std::max(per_sample, 1.0));
-    c = std::max<int64_t>(32, c / 32 * 32);
-    const int64_t n32 = (n + 31) / 32 * 32;
-    return std::min(c, std::max<int64_t>(32, n32));
+    size_t free_b = 0, total_b = 0;
+    cuda_check(cudaMemGetInfo(&free_b, &total_b), "device memory query");
+    const double budget =
+        std::min(std::max((double)(free_b + g->ws_bytes) / 4.0, (double)(1ll << 30)), (double)(32ll << 30));
+    const int64_t n32 = std::max<int64_t>(32, (n + 31) / 32 * 32);
+    if ((double)n32 * per_sample <= budget) {
+        *sets = 1;
+        return n32;
+    }
+    *sets = 2;
+    const int64_t c = (int64_t)(budget / (2.0 * std::max(per_sample, 1.0)));
+    return std::max<int64_t>(32, c / 32 * 32);
 }
 
 struct ChunkBufs {
@@ -119,15 +132,16 @@ struct ChunkBufs {
     int32_t *cause_major;
 };
 
-// Carves two chunk buffer sets of C samples out of the workspace.
-void carve(mcd_dag *g, int64_t C, ChunkBufs cb[2]) {
+// Carves `sets` chunk buffer sets of C samples out of the workspace (a single
+// set serves both slots).
+void carve(mcd_dag *g, int64_t C, int sets, ChunkBufs cb[2]) {
     const size_t E = (size_t)g->h.E, L = (size_t)g->h.L;
     const size_t sz_seed = align_up((size_t)C * 8, 256), sz_re = align_up(E * (size_t)C * 8, 256),
                  sz_du = align_up(L * (size_t)C * 8, 256), sz_ca = align_up(E * (size_t)C * 4, 256);
     const size_t per = sz_seed + 2 * (sz_re + sz_du + sz_ca);
-    ensure_ws(g, 2 * per);
+    ensure_ws(g, (size_t)sets * per);
     for (int k = 0; k < 2; ++k) {
-        char *p = g->ws + k * per;
+        char *p = g->ws + (size_t)(k % sets) * per;
         cb[k].seeds = (int64_t *)p;
         p += sz_seed;
         cb[k].real_minor = (double *)p;
@@ -307,6 +321,16 @@ int mcd_dag_get_info(const mcd_dag *g, mcd_dag_info *info) {
     });
 }
 
+int mcd_dag_link_streams(const mcd_dag *g, int32_t *block, int32_t *word) {
+    return guarded([&] {
+        if (!g || !block || !word) throw McdError(MCD_ERR_INVALID, "null argument");
+        for (int32_t l = 0; l < g->h.L; ++l) {
+            block[l] = g->h.link_block[(size_t)l];
+            word[l] = g->h.link_word[(size_t)l];
+        }
+    });
+}
+
 int mcd_dag_describe(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag_info *info) {
     return guarded([&] {
         if (!desc || !gen || !info) throw McdError(MCD_ERR_INVALID, "null argument");
@@ -381,9 +405,10 @@ int mcd_run_many_host(mcd_dag *g, const int64_t *seeds, int64_t n, double *reali
         if (!seeds) throw McdError(MCD_ERR_INVALID, "null seeds");
         cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
         const int64_t E = g->h.E, L = g->h.L;
-        const int64_t C = host_chunk(g, n);
+        int sets = 1;
+        const int64_t C = host_chunk(g, n, &sets);
         ChunkBufs cb[2];
-        carve(g, C, cb);
+        carve(g, C, sets, cb);
         int64_t idx = 0;
         for (int64_t off = 0; off < n; off += C, ++idx) {
             const int k = (int)(idx & 1);
@@ -431,9 +456,10 @@ int mcd_propagate_host(mcd_dag *g, const double *durations, int64_t n, double *r
         if (!durations && g->h.L > 0) throw McdError(MCD_ERR_INVALID, "null durations");
         cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
         const int64_t E = g->h.E, L = g->h.L;
-        const int64_t C = host_chunk(g, n);
+        int sets = 1;
+        const int64_t C = host_chunk(g, n, &sets);
         ChunkBufs cb[2];
-        carve(g, C, cb);
+        carve(g, C, sets, cb);
         int64_t idx = 0;
         for (int64_t off = 0; off < n; off += C, ++idx) {
             const int k = (int)(idx & 1);

@@ -109,7 +109,7 @@ static void verify_layout(const HostDag &H) {
     const int64_t E = H.E, P = (int64_t)H.pred.size(), NW = H.n_warps, NS = H.n_stages;
     if ((int64_t)H.ev.size() != E) fail("event records");
     if ((int64_t)H.stage_meta.size() != NS * 4 || (int64_t)H.wk_off.size() != NS * NW + 1) fail("stage tables");
-    // shared memory: [window][stage buffer 0][stage buffer 1][tables][2 mbarriers]
+    // shared memory: [window][stage buffer 0][stage buffer 1][tables][2 mbarriers, 2 stage counters]
     const int64_t win = H.win_smem ? (int64_t)H.window_slots * kTile * (int64_t)sizeof(double) : 0;
     const int64_t tables = H.tables_in_smem ? (int64_t)(H.dist.size() * sizeof(DistParam) +
                                                         H.alias.size() * sizeof(AliasEntry))
@@ -119,7 +119,8 @@ static void verify_layout(const HostDag &H) {
     if (H.smem_tables_off < (int64_t)H.smem_stage_off + 2 * (int64_t)H.stage_bytes || H.smem_tables_off % 16)
         fail("table offset");
     if (H.smem_bar_off % 8 || H.smem_bar_off < H.smem_tables_off + tables) fail("barrier offset");
-    if (H.smem_total < (int64_t)H.smem_bar_off + 16 || H.smem_total > (int64_t)kSmemMax) fail("shared memory total");
+    if (H.smem_total < (int64_t)H.smem_bar_off + kBarRegionBytes || H.smem_total > (int64_t)kSmemMax)
+        fail("shared memory total");
     // records
     std::vector<int32_t> stage_of((size_t)E, -1);  // by caller index
     std::vector<char> seen((size_t)E, 0);
@@ -163,6 +164,9 @@ static void verify_layout(const HostDag &H) {
                 if (p.link < -1 || p.link >= H.L) fail("link index");
                 const int kind = p.kd & KD_KIND_MASK;
                 if (kind < K_FIXED || kind > K_EMP_REL) fail("delay kind");
+                if (kind != K_FIXED && (p.link < 0 || p.block < 0 || p.block >= H.L ||
+                                        p.block != H.link_block[(size_t)p.link]))
+                    fail("Philox block");
                 if (kind != K_FIXED) {
                     const int64_t di = (int64_t)(p.kd >> 8);
                     if (di < 0 || di >= (int64_t)H.dist.size()) fail("distribution index");
@@ -460,6 +464,12 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
     for (int32_t e = 0; e < E; ++e)
         for (int64_t k = 0; k < tlen[e]; ++k) cost[e] += kind_cost(d.pred_act[tstart[e] + k]);
 
+    // Within a level, costliest events first: warps take a stage's events one at
+    // a time from a shared counter, so this is longest-processing-time order.
+    for (int32_t l = 0; l < n_levels; ++l)
+        std::stable_sort(by_level.begin() + lvl_off[l], by_level.begin() + lvl_off[l + 1],
+                         [&](int32_t x, int32_t y) { return cost[x] > cost[y]; });
+
     // ---- 9) shared-memory budget: window rows, two record staging buffers
     // (each stage's event and predecessor records), distribution tables
     const size_t table_bytes = H.dist.size() * sizeof(DistParam) + H.alias.size() * sizeof(AliasEntry);
@@ -545,7 +555,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
             pos += meta[(size_t)st * 3 + 2];
         }
     }
-    // layout: [window][stage buffer 0][stage buffer 1][tables][2 mbarriers]
+    // layout: [window][stage buffer 0][stage buffer 1][tables][2 mbarriers, 2 stage counters]
     {
         size_t off = H.win_smem ? win_bytes : 0;
         off = (off + 127) / 128 * 128;
@@ -556,7 +566,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         if (H.tables_in_smem) off += table_bytes;
         off = (off + 15) / 16 * 16;
         H.smem_bar_off = (int32_t)off;
-        off += 16;
+        off += kBarRegionBytes;
         H.smem_total = (int32_t)off;
         if (off > kSmemMax) throw McdError(MCD_ERR_INVALID, "compiled DAG does not fit the shared-memory budget");
     }
@@ -566,6 +576,14 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
     H.pred.clear();
     H.pred.reserve((size_t)(d.n_targets > 0 ? d.pred_offsets[d.n_targets] : 0));
     std::vector<char> referenced((size_t)L, 0), written((size_t)L, 0);
+    // Philox blocks (see KD_REUSE): one-word links group per event, the rest own one
+    auto one_word = [&](int32_t l) {
+        const int kind = H.link_kd[l] & KD_KIND_MASK;
+        return kind == K_EXP || ((kind == K_EMP_ABS || kind == K_EMP_REL) &&
+                                 H.dist[(size_t)(H.link_kd[l] >> 8)].tab_n <= kOneWordBins);
+    };
+    H.link_block.assign((size_t)L, -1);
+    H.link_word.assign((size_t)L, -1);
     H.earliest.assign(d.earliest, d.earliest + E);
     H.ub.resize((size_t)E);
     H.max_delay = d.max_delay;
@@ -590,6 +608,8 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         r.init_key = std::isnan(earliest) ? std::numeric_limits<int64_t>::max() : order_key_host(r.init_bits);
         r.ub_bits = bits_of(ub);
         r.ub_key = std::isnan(ub) ? std::numeric_limits<int64_t>::max() : order_key_host(r.ub_bits);
+        int32_t group = -1, group_n = 0;  // this event's open Philox block of one-word links
+        int32_t last_block = -1;          // block its last non-gamma random reference drew (in registers)
         for (int64_t k = 0; k < tlen[e]; ++k) {
             const int32_t src = d.pred_src[tstart[e] + k];
             const int32_t l = d.pred_act[tstart[e] + k];
@@ -610,6 +630,28 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
                 p.kd = H.link_kd[l];
                 p.v = H.link_v[l];
                 p.dv = H.link_dv[l];
+                p.block = -1;
+                if ((H.link_kd[l] & KD_KIND_MASK) != K_FIXED) {
+                    if (H.link_block[l] < 0) {  // first reference: the link's block and word
+                        if (one_word(l)) {
+                            if (group < 0 || group_n == 4) {
+                                group = l;
+                                group_n = 0;
+                            }
+                            H.link_block[l] = group;
+                            H.link_word[l] = (int8_t)group_n++;
+                        } else {
+                            H.link_block[l] = l;
+                        }
+                    }
+                    p.block = H.link_block[l];
+                    if ((H.link_kd[l] & KD_KIND_MASK) != K_GAMMA) {  // draws into the shared registers
+                        if (one_word(l)) p.kd |= (int32_t)H.link_word[l] << KD_WORD_SHIFT;
+                        else p.kd |= KD_TWO_WORD;
+                        if (p.block == last_block) p.kd |= KD_REUSE;
+                        last_block = p.block;
+                    }
+                }
                 if (!written[l]) {  // the first reference stores the link's duration row
                     p.kd |= KD_WRITE;
                     written[l] = 1;
@@ -636,7 +678,15 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
     H.n_orphan = 0;
     for (int32_t l = 0; l < L; ++l) {
         if (!referenced[l]) ++H.n_orphan;
-        if (!written[l]) H.aux.push_back(LinkRec{l, H.link_kd[l], H.link_v[l]});
+        if (written[l]) continue;
+        // an unreferenced random link owns its block (word 0)
+        int32_t kd = H.link_kd[l];
+        if ((kd & KD_KIND_MASK) != K_FIXED) {
+            H.link_block[l] = l;
+            if (one_word(l)) H.link_word[l] = 0;
+            else if ((kd & KD_KIND_MASK) != K_GAMMA) kd |= KD_TWO_WORD;
+        }
+        H.aux.push_back(LinkRec{l, kd, H.link_v[l]});
     }
     verify_layout(H);
 }

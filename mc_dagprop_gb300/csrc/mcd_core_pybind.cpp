@@ -325,6 +325,12 @@ class Propagator {
         d["grad_base"] = gb;
         return d;
     }
+    py::tuple link_streams() const {
+        const int32_t L = mcd_dag_activity_count(dag_.get());
+        py::array_t<int32_t> block(L), word(L);
+        raise_status(mcd_dag_link_streams(dag_.get(), block.mutable_data(), word.mutable_data()));
+        return py::make_tuple(block, word);
+    }
     py::dict info() const {
         mcd_dag_info i{};
         raise_status(mcd_dag_get_info(dag_.get(), &i));
@@ -707,6 +713,8 @@ PYBIND11_MODULE(_core, m) {
              "Pathwise gradient of J = mean_s sum_e (realized - earliest) over seeds seed0..seed0+n-1: "
              "dict of objective, grad_earliest (per event), grad_base (per link index)")
         .def("info", &Propagator::info, "Compiled-DAG facts")
+        .def("link_streams", &Propagator::link_streams,
+             "(block, word) per link: the Philox block of its draws and its word (-1: whole block)")
         .def("_handle", [](const Propagator &p) { return (uintptr_t)p.handle(); });
 
     py::class_<Batch>(m, "Batch")

@@ -90,11 +90,11 @@ __device__ __forceinline__ long long order_key(long long b) {
 }
 
 // ---------------------------------------------------------------- integer FP64 helpers
-constexpr unsigned long long kMant = 0xFFFFFFFFFFFFFull, kHidden = 1ull << 52;
-
-// Bits of the double 1 + x for a float x >= 0.  Exact when x >= 2^-29 (the
-// float's 24 significant bits then fit the double's fraction); smaller x are
-// truncated to 2^-52.  x >= 1 goes through the float sum 1 + x.
+// Bits of the double 1 + x for a float x >= 0, built with integer operations
+// (a float-to-double conversion would occupy the FP64 pipe).  Exact when
+// x >= 2^-29 (the float's 24 significant bits then fit the double's fraction);
+// smaller x are truncated to 2^-52.  x >= 1 goes through the float sum 1 + x.
+// A sampled duration is then base * (1 + X): one FP64 multiply.
 __device__ __forceinline__ long long one_plus(float x) {
     const uint32_t b = __float_as_uint(x);
     const int e = (int)((b >> 23) & 0xFF);
@@ -110,52 +110,29 @@ __device__ __forceinline__ long long one_plus(float x) {
     return (long long)(((fe + 896ull) << 52) | ((unsigned long long)(f & 0x7FFFFFu) << 29));
 }
 
-// a * g for a double a and a positive normal double g, truncated toward zero,
-// from the top 53 bits of the 106-bit mantissa product; other operands, or a
-// result out of the normal range, fall back to the FP64 multiply.
-__device__ __forceinline__ double mul_trunc(double a, long long gb) {
-    const long long ab = __double_as_longlong(a);
-    const int ea = (int)((ab >> 52) & 0x7FF), eg = (int)((gb >> 52) & 0x7FF);
-    int e = ea + eg - 1023;
-    if (gb <= 0 || eg == 0 || eg == 0x7FF || ea == 0 || ea == 0x7FF || e <= 0 || e >= 0x7FE)
-        return a * __longlong_as_double(gb);
-    const unsigned long long ma = ((ab & kMant) | kHidden) << 11, mg = ((gb & kMant) | kHidden) << 11;
-    const unsigned long long hi = __umul64hi(ma, mg);  // = (ma * mg) >> 42, in [2^62, 2^64)
-    unsigned long long m;
-    if (hi >> 63) {
-        m = hi >> 11;
-        e += 1;
-    } else {
-        m = hi >> 10;
-    }
-    return __longlong_as_double((long long)((ab & 0x8000000000000000ll) | ((unsigned long long)e << 52) |
-                                            (m & kMant)));
-}
-
 // ---------------------------------------------------------------- samplers
 // Each returns the link's duration (base + extra) for one sample.
 
 // Exponential with mean lambda_, redrawn above max_scale (_core.cpp:83-89).  The
 // redraw loop is replaced by the inverse CDF of the truncated law, which is the
 // same distribution: X = -lambda_ * log(1 - c u), c = 1 - exp(-max_scale/lambda_).
-__device__ __forceinline__ double draw_exponential(const DistParam &p, double base, uint32_t link, uint64_t seed,
-                                                   float &dfac) {
-    const U4 r = draw_words(seed, link, 0u, 0u);
-    const float w = u01_open0(r.x);       // plays the role of 1 - u
+// r: the link's random word.
+__device__ __forceinline__ double draw_exponential(const DistParam &p, double base, uint32_t r, float &dfac) {
+    const float w = u01_open0(r);         // plays the role of 1 - u
     const float V = fmaf(p.f1, w, p.f2);  // 1 - c (1 - w), in (1-c, 1]
     float X = -p.f0 * __logf(V);
     X = fmaxf(fminf(X, p.f3), 0.0f);
     dfac = 1.0f + X;
-    return mul_trunc(base, one_plus(X));  // base + X * base
+    return base * __longlong_as_double(one_plus(X));  // base + X * base
 }
 
 // Gamma(shape, scale) redrawn above max_scale (_core.cpp:98-104), by Marsaglia &
 // Tsang (ACM TOMS 26(3), 2000) in FP32, normals from Box-Muller.  Shapes below 1
 // draw Gamma(shape+1) times U^(1/shape).  Rejection loops are capped; a lane that
 // hits the cap latches ERR_GAMMA_REJECTION and returns the truncation point.
-// Not inlined: it is large, and keeping it out of line keeps the propagation
-// loop's register allocation small.
-static __device__ __noinline__ double draw_gamma(const DistParam &p, double base, uint32_t link, uint64_t seed,
+// Inlined: the out-of-line call measured 2.5 % slower on the five-kind workload
+// (the call convention costs the loop more than the sampler's temporaries).
+static __device__ __forceinline__ double draw_gamma(const DistParam &p, double base, uint32_t link, uint64_t seed,
                                                  int32_t *err, float *dfac) {
     const float d = p.f0, cc = p.f1;
     for (uint32_t attempt = 0; attempt < 4096u; ++attempt) {
@@ -183,47 +160,53 @@ static __device__ __noinline__ double draw_gamma(const DistParam &p, double base
         X *= p.f3;
         if (X > p.f4) continue;
         *dfac = 1.0f + X;
-        return mul_trunc(base, one_plus(X));
+        return base * __longlong_as_double(one_plus(X));
     }
     atomicOr(err, ERR_GAMMA_REJECTION);
     *dfac = 1.0f + p.f4;
-    return mul_trunc(base, one_plus(p.f4));
+    return base * __longlong_as_double(one_plus(p.f4));
 }
 
-// Empirical tables (_core.cpp:110-141) by Walker/Vose alias sampling: one
-// 32-bit word picks the bin, a second decides bin or alias.  The duration is
+// Empirical tables (_core.cpp:110-141) by Walker/Vose alias sampling.  One
+// word r: the bin is the high half of r * n and the low half, uniform on a
+// lattice of spacing n / 2^32, decides bin or alias (tables of at most
+// kOneWordBins bins); two words (r, r2): r picks the bin, r2 decides.  The duration is
 // formed exactly as the reference forms it -- base + value (absolute, :125, 328)
 // or base + factor * base (relative, :140, 328) -- so each bin yields the
 // reference's bit pattern: the values are atoms, and any last-bit difference
 // would separate the two discrete distributions.
 __device__ __forceinline__ double draw_empirical(const DistParam &p, const AliasEntry *alias, double base,
-                                                 bool relative, uint32_t link, uint64_t seed, float &dfac) {
-    const U4 r = draw_words(seed, link, 0u, 0u);
-    const uint32_t j = __umulhi(r.x, (uint32_t)p.tab_n);
+                                                 bool relative, uint32_t r, uint32_t r2, bool two_word,
+                                                 float &dfac) {
+    const uint32_t j = __umulhi(r, (uint32_t)p.tab_n);
+    const uint32_t u = two_word ? r2 : r * (uint32_t)p.tab_n;
     const AliasEntry &e = alias[p.tab_off + j];
-    const double val = r.y < e.thresh ? e.v_self : e.v_alias;
+    const double val = u < e.thresh ? e.v_self : e.v_alias;
     dfac = relative ? 1.0f + (float)val : 1.0f;
     return relative ? __dadd_rn(base, __dmul_rn(val, base)) : __dadd_rn(base, val);
 }
 
 // The link's duration for one sample, and (dfac) its derivative with respect to
 // the base duration: 1 + X for the multiplicative kinds, 1 for absolute tables,
-// the host-computed value (dv) for fixed links.
-__device__ __forceinline__ double link_duration(int32_t kd, double v, float dv, uint32_t link, uint64_t seed,
-                                                const DistParam *dists, const AliasEntry *alias, int32_t *err,
-                                                float &dfac) {
+// the host-computed value (dv) for fixed links.  block: the link's Philox
+// block; grp: the words of the block the event's previous exponential or
+// empirical reference drew, redrawn here unless KD_REUSE says they are this
+// link's block.
+__device__ __forceinline__ double link_duration(int32_t kd, double v, float dv, uint32_t block, uint64_t seed,
+                                                U4 &grp, const DistParam *dists, const AliasEntry *alias,
+                                                int32_t *err, float &dfac) {
     const int kind = kd & KD_KIND_MASK;
     if (kind == K_FIXED) {
         dfac = dv;
         return v;
     }
     const DistParam &p = dists[kd >> 8];
-    switch (kind) {
-        case K_EXP: return draw_exponential(p, v, link, seed, dfac);
-        case K_GAMMA: return draw_gamma(p, v, link, seed, err, &dfac);
-        case K_EMP_ABS: return draw_empirical(p, alias, v, false, link, seed, dfac);
-        default: return draw_empirical(p, alias, v, true, link, seed, dfac);
-    }
+    if (kind == K_GAMMA) return draw_gamma(p, v, block, seed, err, &dfac);
+    if (!(kd & KD_REUSE)) grp = draw_words(seed, block, 0u, 0u);
+    const int wsel = (kd >> KD_WORD_SHIFT) & 3;
+    const uint32_t r = wsel == 0 ? grp.x : wsel == 1 ? grp.y : wsel == 2 ? grp.z : grp.w;
+    if (kind == K_EXP) return draw_exponential(p, v, r, dfac);
+    return draw_empirical(p, alias, v, kind == K_EMP_REL, r, grp.y, (kd & KD_TWO_WORD) != 0, dfac);
 }
 
 // ---------------------------------------------------------------- TMA staging
@@ -345,10 +328,14 @@ __device__ __forceinline__ void accumulate_sum(const KArgs &a, const EvRec &ev, 
 // Returns false when a staged copy never landed (then every thread returns false).
 //
 // Shared memory: [window: window_slots x 32 doubles][stage buffer 0][stage
-// buffer 1][distribution params][alias table][2 mbarriers]; `bars` is that
-// layout's barrier pair, or one fixed pair for every tile of a persistent CTA
-// (a barrier stays where it was initialised: only the same address is
-// invalidated and initialised again between tiles).
+// buffer 1][distribution params][alias table][2 mbarriers, 2 stage counters];
+// `bars` is that layout's barrier region (kBarRegionBytes), or one fixed region
+// for every tile of a persistent CTA (a barrier stays where it was
+// initialised: only the same address is invalidated and initialised again
+// between tiles).
+// Warps take a stage's events one at a time from the stage's counter (the
+// compiler orders them costliest first), so a stage ends when its last event
+// does, not when the unluckiest static chunk does.
 // ADJ: the forward half of the adjoint: per event and sample, the winning
 // predecessor's position, clamp and delay flags and d(duration)/d(base) go to
 // a.adj_code / a.adj_dfac, and (realized - earliest) to the objective sum.
@@ -378,6 +365,8 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
         for (int i = threadIdx.x; i < a.n_dist; i += blockDim.x) s_dist[i] = a.dist[i];
         for (int i = threadIdx.x; i < a.n_alias; i += blockDim.x) s_alias[i] = a.alias[i];
     }
+    int *stage_ctr = reinterpret_cast<int *>(bars + 2);
+    U4 grp{};  // the words of the Philox block the current event last drew (see KD_REUSE)
     if (threadIdx.x == 0) {
         if (reuse) {
             asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bars[0])) : "memory");
@@ -386,6 +375,8 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        stage_ctr[0] = 0;
+        stage_ctr[1] = 0;
     }
     // A persistent CTA's previous tile may have had another layout: its window
     // stores (generic proxy) can lie where this tile's staged copies (async
@@ -412,9 +403,17 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
         const EvRec *sev = meta.y >= 0 ? reinterpret_cast<const EvRec *>(buf) : a.ev + meta.x;
         const PredRec *spred = meta.y >= 0 ? reinterpret_cast<const PredRec *>(buf + a.stage_pred_off)
                                            : a.pred + meta.z;
-        const int ib = __ldg(&a.wk_off[l * NW + warp]) - meta.x;
-        const int ie = __ldg(&a.wk_off[l * NW + warp + 1]) - meta.x;
-        for (int i = ib; i < ie; ++i) {
+        const int n_ev = meta.y >= 0 ? meta.y : -meta.y;
+        if (threadIdx.x == 0) stage_ctr[(l + 1) & 1] = 0;  // last used by stage l - 1, before the barrier
+        // the next index is taken before this event's work, hiding the atomic's
+        // latency (a warp holds at most one extra event: the cheapest, by order)
+        int i_next = 0;
+        if (lane == 0) i_next = atomicAdd(&stage_ctr[l & 1], 1);
+        i_next = __shfl_sync(0xFFFFFFFFu, i_next, 0);
+        while (i_next < n_ev) {
+            const int i = i_next;
+            if (lane == 0) i_next = atomicAdd(&stage_ctr[l & 1], 1);
+            i_next = __shfl_sync(0xFFFFFFFFu, i_next, 0);
             const EvRec ev = sev[i];
             long long lk = ev.init_key, lbits = ev.init_bits;
             int32_t cause = -1;
@@ -427,7 +426,8 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
                 if (GIVEN) {
                     dur = (active && pr.link >= 0) ? __ldg(&a.dur_in[(int64_t)pr.link * a.ld_in + s]) : 0.0;
                 } else {
-                    dur = link_duration(pr.kd, pr.v, pr.dv, (uint32_t)pr.link, seed, dists, alias, a.err, dfac);
+                    dur = link_duration(pr.kd, pr.v, pr.dv, (uint32_t)pr.block, seed, grp, dists, alias, a.err,
+                                        dfac);
                     if (!STATS && !ADJ && (pr.kd & KD_WRITE) && a.durations && active)
                         a.durations[(int64_t)pr.link * a.ld + s] = dur;
                 }
@@ -482,7 +482,9 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
         for (int i = warp; i < a.n_aux; i += NW) {
             const LinkRec lr = a.aux[i];
             float dfac;
-            const double dur = link_duration(lr.kd, lr.v, 0.0f, (uint32_t)lr.link, seed, dists, alias, a.err, dfac);
+            U4 own;  // an unreferenced link owns its block
+            const double dur =
+                link_duration(lr.kd, lr.v, 0.0f, (uint32_t)lr.link, seed, own, dists, alias, a.err, dfac);
             if (active) a.durations[(int64_t)lr.link * a.ld + s] = dur;
         }
     }

@@ -73,6 +73,8 @@ struct HostDag {
     std::vector<int32_t> link_kd;
     std::vector<double> link_v;
     std::vector<float> link_dv;    // FIXED links: d(duration)/d(base)
+    std::vector<int32_t> link_block;  // Philox block of each link's random words (-1: fixed)
+    std::vector<int8_t> link_word;    // word of a one-word link in its block; -1: the link owns the block
     std::vector<double> earliest;  // caller order
     std::vector<double> ub;        // earliest + max_delay, caller order
     double max_delay = 0.0;

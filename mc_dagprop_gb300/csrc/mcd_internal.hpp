@@ -16,11 +16,22 @@ namespace mcd {
 // the reference's two roundings (_core.cpp:75, 328).
 enum Kind : int32_t { K_FIXED = 0, K_EXP = 1, K_GAMMA = 2, K_EMP_ABS = 3, K_EMP_REL = 4 };
 
-// Packed kind word of a link reference: kind | KD_WRITE | dist << 8.  KD_WRITE
-// marks the one reference of a link that stores its duration row; links no
-// precedence entry references are stored by the kernel's aux-link pass.
-constexpr int32_t KD_KIND_MASK = 0x7F;
+// Packed kind word of a link reference:
+//   kind | word << KD_WORD_SHIFT | KD_REUSE | KD_TWO_WORD | KD_WRITE | dist << 8.
+// Random words: a link draws from the Philox block `block` of its PredRec.  One-
+// word links (exponential; empirical tables of at most kOneWordBins bins) share
+// a block with up to three other one-word links first referenced by the same
+// event, each taking its own word; KD_REUSE marks a reference whose block the
+// event's previous exponential or empirical reference already drew (the words
+// are still in registers).  Gamma links and larger empirical tables (KD_TWO_WORD) own their
+// block.  KD_WRITE marks the one reference of a link that stores its duration
+// row; links no precedence entry references are stored by the aux-link pass.
+constexpr int32_t KD_KIND_MASK = 0x07;
+constexpr int KD_WORD_SHIFT = 3;  // bits 3-4
+constexpr int32_t KD_REUSE = 0x20;
+constexpr int32_t KD_TWO_WORD = 0x40;
 constexpr int32_t KD_WRITE = 0x80;
+constexpr int32_t kOneWordBins = 4096;  // one 32-bit word picks bin and alias (threshold lattice <= 2^-20)
 
 // One event, in compiled (level) order.  48 bytes.
 struct alignas(16) EvRec {
@@ -40,10 +51,10 @@ struct alignas(16) PredRec {
     int32_t src_user;  // predecessor event index (cause_event value, global row)
     int32_t link;      // link index: durations row and Philox counter; -1 for an index
                        // past the last link, which has duration 0 (see the compiler)
-    int32_t kd;        // kind | KD_WRITE | dist << 8
+    int32_t kd;        // packed kind word (above)
     double v;          // FIXED: the duration; otherwise the base (minimal_duration)
     float dv;          // FIXED: d(duration)/d(base) (1 + factor, 1, or 0 for gaps)
-    int32_t pad;
+    int32_t block;     // Philox block of the link's random words (-1: fixed)
 };
 
 // A link whose duration row the aux pass stores: a link no precedence entry
@@ -169,5 +180,8 @@ struct FArgs {
 enum : int32_t { ERR_GAMMA_REJECTION = 1, ERR_STAGE_TIMEOUT = 2, ERR_LAYOUT = 4 };
 
 constexpr int kTile = 32;  // samples per tile: one per lane
+// End of a CTA's shared memory: two mbarriers (8 bytes each), then the two
+// stage work counters (int32 each), padded to 32 bytes.
+constexpr int kBarRegionBytes = 32;
 
 }  // namespace mcd

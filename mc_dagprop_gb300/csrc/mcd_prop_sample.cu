@@ -11,13 +11,14 @@ namespace mcd {
 // One instantiation per (window on chip, positive times): every DAG of a launch
 // shares both, so only one propagation variant is inlined (fewer registers).
 // DAGs whose window is not on chip use per-CTA scratch rows (32 samples each).
-// Each DAG has its own shared-memory layout; the barrier pair lives outside
-// all of them, in static shared memory, so it never moves between items.
+// Each DAG has its own shared-memory layout; the barrier pair and the stage
+// counters live outside all of them, in static shared memory, so they never
+// move between items.
 template <bool WIN_SMEM, bool POSITIVE>
 __global__ void __launch_bounds__(768, 1) k_batch_stats(const BatchArgs b) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ KArgs s_args;
-    __shared__ __align__(8) uint64_t s_bars[2];
+    __shared__ __align__(8) uint64_t s_bars[kBarRegionBytes / 8];
     __shared__ int s_item;
     bool reuse = false;
     for (;;) {

@@ -106,6 +106,10 @@ struct Request {
     Clock::time_point t_submit, t_done;
 };
 
+// Buffers grow geometrically and are never released while the server runs:
+// cudaFree and cudaFreeHost synchronise the whole device, which would stall the
+// scheduler behind every batch in flight.  Device metadata is stream-ordered;
+// outgrown pinned buffers are retired and freed with the server.
 struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
@@ -116,6 +120,7 @@ struct Slot {
     size_t meta_bytes = 0;
     double *pinned = nullptr;   // statistics of the batch, host side
     size_t pinned_elems = 0;
+    std::vector<void *> retired;  // outgrown pinned buffers
 };
 
 }  // namespace
@@ -207,30 +212,53 @@ void request_args(Request *r) {
     f.p_on_time = o + 4 * (size_t)h.E;
 }
 
+// A compile thread's pinned staging buffer: records are gathered there and
+// uploaded in one DMA copy (a copy from pageable memory is staged by the driver
+// on the calling thread and serialises with other threads' CUDA calls).
+struct Staging {
+    char *p = nullptr;
+    size_t bytes = 0;
+    std::vector<void *> retired;  // outgrown buffers, freed when the thread ends
+    ~Staging() {
+        if (p) cudaFreeHost(p);
+        for (void *q : retired) cudaFreeHost(q);
+    }
+};
+
 // Uploads the compiled records into the request's block and zeroes its
 // accumulators; returns when the copies have landed.  Only copies: a kernel
 // (such as a memset) would queue behind the persistent batch launches that
 // hold every SM, while the copy engines are free.
-void upload_request(const mcd_server *S, Request *r, cudaStream_t st) {
+void upload_request(const mcd_server *S, Request *r, cudaStream_t st, Staging &stage) {
     const HostDag &h = r->h;
     const Layout &L = r->lay;
+    if (L.err > stage.bytes) {
+        const size_t bytes = std::max(L.err, stage.bytes * 2);
+        if (stage.p) stage.retired.push_back(stage.p);
+        stage.p = nullptr;
+        stage.bytes = 0;
+        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&stage.p), bytes, cudaHostAllocDefault), "staging");
+        stage.bytes = bytes;
+    }
+    auto put = [&](size_t off, const void *src, size_t bytes) {
+        if (bytes) std::memcpy(stage.p + off, src, bytes);
+    };
+    put(L.ev, h.ev.data(), h.ev.size() * sizeof(EvRec));
+    put(L.pred, h.pred.data(), h.pred.size() * sizeof(PredRec));
+    put(L.aux, h.aux.data(), h.aux.size() * sizeof(LinkRec));
+    put(L.dist, h.dist.data(), h.dist.size() * sizeof(DistParam));
+    put(L.alias, h.alias.data(), h.alias.size() * sizeof(AliasEntry));
+    put(L.wk, h.wk_off.data(), h.wk_off.size() * 4);
+    put(L.meta, h.stage_meta.data(), h.stage_meta.size() * 4);
+    put(L.earliest, h.earliest.data(), (size_t)h.E * 8);
+    put(L.ub, h.ub.data(), (size_t)h.E * 8);
     cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&r->dblock), r->bytes, st), "request allocation");
     char *b = r->dblock;
-    auto up = [&](size_t off, const void *src, size_t bytes) {
-        if (bytes) cuda_check(cudaMemcpyAsync(b + off, src, bytes, cudaMemcpyHostToDevice, st), "request upload");
-    };
-    up(L.ev, h.ev.data(), h.ev.size() * sizeof(EvRec));
-    up(L.pred, h.pred.data(), h.pred.size() * sizeof(PredRec));
-    up(L.aux, h.aux.data(), h.aux.size() * sizeof(LinkRec));
-    up(L.dist, h.dist.data(), h.dist.size() * sizeof(DistParam));
-    up(L.alias, h.alias.data(), h.alias.size() * sizeof(AliasEntry));
-    up(L.wk, h.wk_off.data(), h.wk_off.size() * 4);
-    up(L.meta, h.stage_meta.data(), h.stage_meta.size() * 4);
-    up(L.earliest, h.earliest.data(), (size_t)h.E * 8);
-    up(L.ub, h.ub.data(), (size_t)h.E * 8);
+    cuda_check(cudaMemcpyAsync(b, stage.p, L.err, cudaMemcpyHostToDevice, st), "request upload");  // records
     for (size_t off = L.err; off < L.out; off += kZeroBytes)  // flags + accumulators
-        up(off, S->zeros, std::min(kZeroBytes, L.out - off));
-    cuda_check(cudaStreamSynchronize(st), "request upload sync");
+        cuda_check(cudaMemcpyAsync(b + off, S->zeros, std::min(kZeroBytes, L.out - off), cudaMemcpyHostToDevice, st),
+                   "request reset");
+    cuda_check(cudaStreamSynchronize(st), "request upload sync");  // the staging buffer is reused next
 }
 
 template <typename T>
@@ -240,6 +268,7 @@ void drop(std::vector<T> &v) {
 
 void compile_loop(mcd_server *S) {
     cudaStream_t st = nullptr;
+    Staging stage;
     if (cudaSetDevice(S->device) != cudaSuccess || cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
         std::lock_guard<std::mutex> lk(S->mu);
         if (S->fatal.empty()) S->fatal = "compile thread: no CUDA stream";
@@ -303,7 +332,7 @@ void compile_loop(mcd_server *S) {
                 holds_budget = true;
             }
             const Clock::time_point t1 = Clock::now();
-            upload_request(S, r, st);
+            upload_request(S, r, st, stage);
             request_args(r);
             HostDag &h = r->h;  // only the scalars stay
             drop(h.ev);
@@ -367,23 +396,25 @@ void launch_batch(mcd_server *S, Slot &slot, std::vector<Request *> &batch) {
                  s_items = align_up(n_items * 8, 256), s_ctr = 256;
     const size_t need = s_ka + s_fa + s_items + s_ctr;
     if (need > slot.meta_bytes) {  // the slot is idle: its stream has nothing in flight
-        if (slot.meta_dev) cuda_check(cudaFree(slot.meta_dev), "slot metadata free");
-        if (slot.meta_pinned) cuda_check(cudaFreeHost(slot.meta_pinned), "slot metadata free");
+        const size_t bytes = std::max(need * 2, slot.meta_bytes * 2);
+        if (slot.meta_dev) cuda_check(cudaFreeAsync(slot.meta_dev, st), "slot metadata free");
+        if (slot.meta_pinned) slot.retired.push_back(slot.meta_pinned);
         slot.meta_dev = nullptr;
         slot.meta_pinned = nullptr;
         slot.meta_bytes = 0;
-        cuda_check(cudaMalloc(reinterpret_cast<void **>(&slot.meta_dev), need * 2), "slot metadata");
-        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&slot.meta_pinned), need * 2, cudaHostAllocDefault),
+        cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&slot.meta_dev), bytes, st), "slot metadata");
+        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&slot.meta_pinned), bytes, cudaHostAllocDefault),
                    "slot metadata");
-        slot.meta_bytes = need * 2;
+        slot.meta_bytes = bytes;
     }
     if (out_elems > slot.pinned_elems) {
-        if (slot.pinned) cuda_check(cudaFreeHost(slot.pinned), "pinned results free");
+        const size_t elems = std::max(out_elems * 2, slot.pinned_elems * 2);
+        if (slot.pinned) slot.retired.push_back(slot.pinned);
         slot.pinned = nullptr;
         slot.pinned_elems = 0;
-        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&slot.pinned), out_elems * 2 * 8, cudaHostAllocDefault),
+        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&slot.pinned), elems * 8, cudaHostAllocDefault),
                    "pinned results");
-        slot.pinned_elems = out_elems * 2;
+        slot.pinned_elems = elems;
     }
     // metadata straight into pinned memory, one upload
     char *mh = slot.meta_pinned;
@@ -572,6 +603,7 @@ void mcd_server_destroy(mcd_server *S) {
         if (s.meta_dev) cudaFree(s.meta_dev);
         if (s.meta_pinned) cudaFreeHost(s.meta_pinned);
         if (s.pinned) cudaFreeHost(s.pinned);
+        for (void *p : s.retired) cudaFreeHost(p);
         if (s.done) cudaEventDestroy(s.done);
         if (s.stream) cudaStreamDestroy(s.stream);
     }

@@ -1,11 +1,14 @@
 """numpy model of the GPU delay sampler (test infrastructure).
 
-Restates, on the CPU, what ``mc_dagprop_gb300/csrc/mcd_kernels.cu`` draws for one
-(sample seed, link): Philox4x32-10 (Salmon et al., SC'11) keyed by the 64-bit
-seed with counter (link, attempt, 0, salt), and the per-kind transforms.  The
-integer parts (Philox words, alias-table bin choice) must match the GPU bit for
-bit; the FP32 transforms match to float rounding, so tests compare those with a
-tolerance.
+Restates, on the CPU, what ``mc_dagprop_gb300/csrc/mcd_device.cuh`` draws for one
+(sample seed, link): Philox4x32-10 (Salmon et al., SC'11) under a fixed key with
+the counter (seed low, seed high, block, salt ^ attempt), and the per-kind
+transforms.  A link's block and word come from the compiled DAG
+(``MonteCarloPropagator.link_streams``): exponential links and empirical tables
+of at most 4,096 bins take one 32-bit word of a block shared with up to three
+other links; a lone link (block = its index) takes word 0.  The integer parts
+(Philox words, alias-table bin choice) must match the GPU bit for bit; the FP32
+transforms match to float rounding, so tests compare those with a tolerance.
 """
 from __future__ import annotations
 
@@ -38,9 +41,12 @@ def philox4x32_10(c0, c1, c2, c3, k0, k1):
     return tuple(x.astype(np.uint32) for x in (c0, c1, c2, c3))
 
 
-def words(seeds, link, attempt=0, sel=0):
+ONE_WORD_BINS = 4096
+
+
+def words(seeds, block, attempt=0, sel=0):
     s = np.asarray(seeds, dtype=np.int64).view(np.uint64)
-    return philox4x32_10(s & MASK, s >> np.uint64(32), link, SALT ^ ((attempt << 1) | sel), KEY0, KEY1)
+    return philox4x32_10(s & MASK, s >> np.uint64(32), block, SALT ^ ((attempt << 1) | sel), KEY0, KEY1)
 
 
 def u01_open0(r):
@@ -49,36 +55,8 @@ def u01_open0(r):
     return (f.astype(np.float64) * 2.0 ** -32 + 2.0 ** -33).astype(np.float32)
 
 
-M52, H52 = (1 << 52) - 1, 1 << 52
-
-
-def _bits(x: float) -> int:
-    return struct.unpack("<q", struct.pack("<d", x))[0]
-
-
 def _from_bits(b: int) -> float:
     return struct.unpack("<d", struct.pack("<q", b))[0]
-
-
-def mul_trunc(a: float, g: float) -> float:
-    """The kernel's integer product a * g (top 53 bits of the mantissa product,
-    truncated), FP64 multiply for the operands it hands to the FP64 unit."""
-    ab, gb = _bits(a), _bits(g)
-    ea, eg = (ab >> 52) & 0x7FF, (gb >> 52) & 0x7FF
-    e = ea + eg - 1023
-    if gb <= 0 or eg in (0, 0x7FF) or ea in (0, 0x7FF) or e <= 0 or e >= 0x7FE:
-        return a * g
-    ma, mg = ((ab & M52) | H52) << 11, ((gb & M52) | H52) << 11
-    hi = (ma * mg) >> 64
-    if hi >> 63:
-        m, e = hi >> 11, e + 1
-    else:
-        m = hi >> 10
-    sign = ab & (1 << 63) if ab >= 0 else (1 << 63)
-    b = (sign | (e << 52) | (m & M52)) if ab < 0 else ((e << 52) | (m & M52))
-    if ab < 0:
-        b -= 1 << 64
-    return _from_bits(b)
 
 
 def one_plus(x) -> float:
@@ -95,9 +73,9 @@ def one_plus(x) -> float:
     return float(np.float32(1.0) + np.float32(x))
 
 
-def exponential_durations(seeds, link, base, lam, max_scale):
+def exponential_durations(seeds, link, base, lam, max_scale, block=None, word=0):
     """Truncated exponential by inverse CDF, the kernel's formula in float32."""
-    r0, _, _, _ = words(seeds, link)
+    r0 = words(seeds, link if block is None else block)[word]
     w = u01_open0(r0).astype(np.float64)
     ratio = max_scale / lam
     c = 1.0 if np.isinf(ratio) else -np.expm1(-ratio)
@@ -106,7 +84,7 @@ def exponential_durations(seeds, link, base, lam, max_scale):
     # the kernel takes the logarithm with the MUFU approximation (within 2^-21.4
     # absolute on [0.5, 2], 3 ulp elsewhere); this model takes the exact one
     X = np.maximum(np.minimum(-np.float32(lam) * np.log(V), np.float32(max_scale)), np.float32(0.0)).astype(np.float32)
-    return np.array([mul_trunc(float(base), one_plus(x)) for x in X])
+    return np.array([float(base) * one_plus(x) for x in X])  # one IEEE multiply, as the kernel
 
 
 def alias_table(values, weights):
@@ -141,18 +119,26 @@ def alias_table(values, weights):
     return th, v, va
 
 
-def empirical_durations(seeds, link, base, values, weights, relative):
+def empirical_durations(seeds, link, base, values, weights, relative, block=None, word=0):
     """The kernel's duration for each seed (exact): base + value, or
     base + factor * base, in IEEE double arithmetic as the reference forms them."""
-    v = empirical_values(seeds, link, values, weights)
+    v = empirical_values(seeds, link, values, weights, block, word)
     return base + v * base if relative else base + v
 
 
-def empirical_values(seeds, link, values, weights):
-    """The table value the kernel picks for each seed (exact)."""
-    r0, r1, _, _ = words(seeds, link)
+def empirical_values(seeds, link, values, weights, block=None, word=0):
+    """The table value the kernel picks for each seed (exact): the bin from the
+    high half of r * n, bin-or-alias from its low half (one word), or from a
+    second word for tables of more than ONE_WORD_BINS bins."""
     th, vs, va = alias_table(values, weights)
     n = len(vs)
-    j = ((r0.astype(np.uint64) * np.uint64(n)) >> np.uint64(32)).astype(np.int64)
-    keep = r1.astype(np.uint64) < th[j]
+    w = words(seeds, link if block is None else block)
+    if n <= ONE_WORD_BINS:
+        x = w[word].astype(np.uint64) * np.uint64(n)
+        j = (x >> np.uint64(32)).astype(np.int64)
+        u = x & MASK
+    else:
+        j = ((w[0].astype(np.uint64) * np.uint64(n)) >> np.uint64(32)).astype(np.int64)
+        u = w[1].astype(np.uint64)
+    keep = u < th[j]
     return np.where(keep, vs[j], va[j])

@@ -91,6 +91,65 @@ def test_gamma_distribution(cuda, shape, scale, ms):
     assert stats.kstest(x, cdf).pvalue > 0.01
 
 
+def _shared_block_dag():
+    """Event 10 reads ten links of mixed kinds from events 0-9; event 11 reads two of
+    the same links again (later references recompute the same words)."""
+    kinds = [2, 4, 5, 2, 1, 3, 4, 2, 6, 5]  # types: 1 constant, 2 exp, 3 gamma, 4 emp abs, 5 emp rel, 6 big table
+    links = {(i, 10): (i, 10.0 + i, kinds[i]) for i in range(10)}
+    links[(10, 11)] = (10, 1.0, 1)
+    prec = [(10, [(i, i) for i in range(10)]), (11, [(10, 10), (3, 3), (2, 2)])]
+    return flat_from_lists([0.0] * 12, links, prec, 1e12)
+
+
+BIG = (np.arange(5000) * 0.01, np.random.default_rng(11).random(5000) + 0.01)
+SHARED_GEN = [("constant", 1, 0.5), ("exponential", 2, 0.3, math.inf), ("gamma", 3, 2.0, 0.05, math.inf),
+              ("empirical_absolute", 4, np.array([0.0, 3.5, 7.25, 100.0]), np.array([1.0, 0.5, 2.0, 0.3])),
+              ("empirical_relative", 5, np.array([0.0, 0.25, 0.5]), np.array([0.2, 0.3, 0.5])),
+              ("empirical_absolute", 6, BIG[0], BIG[1])]
+
+
+def test_shared_philox_blocks_match_model(cuda):
+    """One-word links (exponential, small tables) first referenced by one event
+    share Philox blocks four at a time; gamma and a 5,000-bin table own theirs.
+    Every link's draws match the model at its (block, word)."""
+    flat = _shared_block_dag()
+    prop = propagator_from_flat(m, flat, SHARED_GEN)
+    block, word = prop.link_streams()
+    one_word = [0, 1, 2, 3, 6, 7, 9]  # links of types 2, 4, 5 in precedence order
+    assert list(block[one_word]) == [0, 0, 0, 0, 6, 6, 6] and list(word[one_word]) == [0, 1, 2, 3, 0, 1, 2]
+    assert block[4] == -1 and block[10] == -1  # constant
+    assert (block[5], word[5]) == (5, -1) and (block[8], word[8]) == (8, -1)  # gamma, big table
+    _, dur, _ = prop.run_many_arrays(SEEDS)
+    gen = {g[1]: g for g in SHARED_GEN}
+    kinds = flat["act_type"]
+    for l in range(10):
+        g, base = gen[int(kinds[l])], float(flat["act_duration"][l])
+        if g[0] == "exponential":
+            ref = PM.exponential_durations(SEEDS, l, base, g[2], g[3], block=block[l], word=word[l])
+            np.testing.assert_allclose(dur[:, l], ref, rtol=2e-6)
+        elif g[0].startswith("empirical"):
+            ref = PM.empirical_durations(SEEDS, l, base, g[2], g[3], g[0] == "empirical_relative",
+                                         block=block[l], word=max(0, word[l]))
+            assert np.array_equal(dur[:, l], ref), l
+
+
+def test_shared_block_words_independent(cuda):
+    """Links sharing a block are independent draws: pairwise correlation of their
+    uniforms and a chi-square of the joint bins of two small tables."""
+    flat = _shared_block_dag()
+    prop = propagator_from_flat(m, flat, SHARED_GEN)
+    n = 200_000
+    _, dur, _ = prop.run_many_arrays(np.arange(n, dtype=np.int64) + 5)
+    x = dur[:, [0, 3, 7]] - flat["act_duration"][[0, 3, 7]]  # three exponentials of block 0 / 6
+    c = np.corrcoef(x.T)
+    assert np.abs(c[np.triu_indices(3, 1)]).max() < 0.01
+    a = np.searchsorted([0.0, 3.5, 7.25, 100.0], dur[:, 1] - 11.0)      # empirical abs, word 1 of block 0
+    b = np.searchsorted([0.0, 0.25, 0.5], (dur[:, 2] - 12.0) / 12.0)    # empirical rel, word 2 of block 0
+    table = np.zeros((4, 3))
+    np.add.at(table, (a, b), 1)
+    assert stats.chi2_contingency(table).pvalue > 0.01
+
+
 def test_empirical_frequencies(cuda):
     n = 200_000
     values = np.linspace(0.0, 300.0, 16)

@@ -56,7 +56,7 @@ KArgs base_args(const mcd_dag *g) {
     a.pred = g->d_pred;
     a.aux = g->d_aux;
     a.dist = g->d_dist;
-    a.alias = g->d_alias;
+    a.vals = g->d_vals;
     a.wk_off = g->d_wk;
     a.stage_meta = g->d_stage_meta;
     a.n_stages = g->h.n_stages;
@@ -69,7 +69,6 @@ KArgs base_args(const mcd_dag *g) {
     a.win_smem = g->h.win_smem ? 1 : 0;
     a.positive = g->h.positive ? 1 : 0;
     a.stage_bytes = g->h.stage_bytes;
-    a.stage_pred_off = g->h.stage_pred_off;
     a.smem_stage_off = g->h.smem_stage_off;
     a.smem_tables_off = g->h.smem_tables_off;
     a.smem_bar_off = g->h.smem_bar_off;
@@ -241,12 +240,12 @@ int mcd_dag_create_ex(const mcd_dag_desc *desc, const mcd_generator *gen, const 
         const size_t s_ev = align_up(h.ev.size() * sizeof(EvRec), 256),
                      s_pred = align_up(h.pred.size() * sizeof(PredRec), 256),
                      s_aux = align_up(h.aux.size() * sizeof(LinkRec), 256),
-                     s_dist = align_up(h.dist.size() * sizeof(DistParam), 256),
-                     s_alias = align_up(h.alias.size() * sizeof(AliasEntry), 256),
+                     s_tables = align_up(tables_bytes(h), 256),
+                     s_vals = align_up(h.vals.size() * sizeof(double), 256),
                      s_wk = align_up(h.wk_off.size() * sizeof(int32_t), 256),
                      s_meta = align_up(h.stage_meta.size() * sizeof(int32_t), 256),
                      s_times = align_up(h.earliest.size() * sizeof(double), 256), s_err = 256;
-        g->dbytes = s_ev + s_pred + s_aux + s_dist + s_alias + s_wk + s_meta + 2 * s_times + s_err;
+        g->dbytes = s_ev + s_pred + s_aux + s_tables + s_vals + s_wk + s_meta + 2 * s_times + s_err;
         cuda_check(cudaMalloc(&g->dmem, g->dbytes), "compiled DAG allocation");
         char *p = g->dmem;
         auto place = [&](auto *&dst, const auto &vec, size_t sz) {
@@ -259,8 +258,11 @@ int mcd_dag_create_ex(const mcd_dag_desc *desc, const mcd_generator *gen, const 
         place(g->d_ev, h.ev, s_ev);
         place(g->d_pred, h.pred, s_pred);
         place(g->d_aux, h.aux, s_aux);
-        place(g->d_dist, h.dist, s_dist);
-        place(g->d_alias, h.alias, s_alias);
+        {
+            const std::vector<unsigned char> tb = tables_block(h);
+            place(g->d_dist, tb, s_tables);
+        }
+        place(g->d_vals, h.vals, s_vals);
         place(g->d_wk, h.wk_off, s_wk);
         place(g->d_stage_meta, h.stage_meta, s_meta);
         place(g->d_earliest, h.earliest, s_times);

@@ -38,6 +38,12 @@ static int64_t bits_of(double x) {
     return b;
 }
 
+static int32_t float_bits(float x) {
+    int32_t b;
+    std::memcpy(&b, &x, sizeof(b));
+    return b;
+}
+
 // Largest float not above x (x may be +inf).
 static float float_at_or_below(double x) {
     float f = (float)x;
@@ -54,7 +60,7 @@ static uint32_t keep_threshold(double prob) {
 
 // Walker/Vose alias table over weights w (validated: finite, >= 0, sum > 0).
 static void build_alias(const std::vector<double> &values, const std::vector<double> &w,
-                        std::vector<AliasEntry> &out) {
+                        std::vector<AliasEntry> &out, std::vector<AliasPick> &picks) {
     const size_t n = w.size();
     double sum = 0.0;
     for (double x : w) sum += x;
@@ -82,6 +88,7 @@ static void build_alias(const std::vector<double> &values, const std::vector<dou
         e.thresh = keep_threshold(prob[i]);
         e.v_alias = e.thresh == 0xFFFFFFFFu ? values[i] : values[(size_t)alias[i]];
         out.push_back(e);
+        picks.push_back(AliasPick{e.thresh, e.thresh == 0xFFFFFFFFu ? (int32_t)i : (int32_t)alias[i]});
     }
 }
 
@@ -108,14 +115,15 @@ static void verify_layout(const HostDag &H) {
     };
     const int64_t E = H.E, P = (int64_t)H.pred.size(), NW = H.n_warps, NS = H.n_stages;
     if ((int64_t)H.ev.size() != E) fail("event records");
-    if ((int64_t)H.stage_meta.size() != NS * 4 || (int64_t)H.wk_off.size() != NS * NW + 1) fail("stage tables");
+    if ((int64_t)H.stage_meta.size() != NS * 8 || (int64_t)H.wk_off.size() != NS * NW + 1) fail("stage tables");
+    if (H.picks.size() != H.alias.size()) fail("alias picks");
     // shared memory: [window][stage buffer 0][stage buffer 1][tables][2 mbarriers, 2 stage counters]
     const int64_t win = H.win_smem ? (int64_t)H.window_slots * kTile * (int64_t)sizeof(double) : 0;
     const int64_t tables = H.tables_in_smem ? (int64_t)(H.dist.size() * sizeof(DistParam) +
-                                                        H.alias.size() * sizeof(AliasEntry))
+                                                        H.alias.size() * (sizeof(AliasEntry) + sizeof(AliasPick)))
                                             : 0;
     if (H.smem_stage_off < win || H.smem_stage_off % 16) fail("stage buffer offset");
-    if (H.stage_pred_off % 16 || H.stage_bytes % 16 || H.stage_pred_off > H.stage_bytes) fail("stage buffer size");
+    if (H.stage_bytes % 16) fail("stage buffer size");
     if (H.smem_tables_off < (int64_t)H.smem_stage_off + 2 * (int64_t)H.stage_bytes || H.smem_tables_off % 16)
         fail("table offset");
     if (H.smem_bar_off % 8 || H.smem_bar_off < H.smem_tables_off + tables) fail("barrier offset");
@@ -124,14 +132,20 @@ static void verify_layout(const HostDag &H) {
     // records
     std::vector<int32_t> stage_of((size_t)E, -1);  // by caller index
     std::vector<char> seen((size_t)E, 0);
-    int64_t ev_next = 0, pred_next = 0;
+    int64_t ev_next = 0, pred_next = 0, val_next = 0;
     for (int64_t st = 0; st < NS; ++st) {
-        const int32_t *m = &H.stage_meta[(size_t)st * 4];
+        const int32_t *m = &H.stage_meta[(size_t)st * 8];
         const int64_t first = m[0], nev = m[1] >= 0 ? m[1] : -(int64_t)m[1], pfirst = m[2], npred = m[3];
+        const int64_t vfirst = m[4], nval = m[5];
         if (first != ev_next || nev <= 0 || first + nev > E || pfirst != pred_next) fail("stage ranges");
-        if (m[1] >= 0 && (nev * (int64_t)sizeof(EvRec) > H.stage_pred_off ||
-                          H.stage_pred_off + npred * (int64_t)sizeof(PredRec) > H.stage_bytes))
+        if (vfirst != val_next || nval < 0 || nval % 2 || vfirst + nval > (int64_t)H.vals.size())
+            fail("value region");
+        const int64_t pboff = m[6], vboff = m[7];
+        if (m[1] >= 0 && (pboff % 16 || vboff % 16 || nev * (int64_t)sizeof(EvRec) > pboff ||
+                          pboff + npred * (int64_t)sizeof(PredRec) > vboff ||
+                          vboff + nval * (int64_t)sizeof(double) > H.stage_bytes))
             fail("staged records exceed the buffer");
+        val_next = vfirst + nval;
         if (H.wk_off[(size_t)(st * NW)] != first) fail("warp chunk start");
         for (int64_t w = 0; w < NW; ++w)
             if (H.wk_off[(size_t)(st * NW + w + 1)] < H.wk_off[(size_t)(st * NW + w)]) fail("warp chunk order");
@@ -149,7 +163,7 @@ static void verify_layout(const HostDag &H) {
         ev_next = first + nev;
         pred_next = pfirst + npred;
     }
-    if (ev_next != E || pred_next != P) fail("stage coverage");
+    if (ev_next != E || pred_next != P || val_next != (int64_t)H.vals.size()) fail("stage coverage");
     // sources and window slots, in execution order
     std::vector<int32_t> slot_of((size_t)E, -1), tenant((size_t)std::max(H.window_slots, 1), -1),
         last_read((size_t)std::max(H.window_slots, 1), -1);
@@ -171,9 +185,30 @@ static void verify_layout(const HostDag &H) {
                     const int64_t di = (int64_t)(p.kd >> 8);
                     if (di < 0 || di >= (int64_t)H.dist.size()) fail("distribution index");
                     const DistParam &dp = H.dist[(size_t)di];
-                    if ((kind == K_EMP_ABS || kind == K_EMP_REL) &&
+                    const bool emp = kind == K_EMP_ABS || kind == K_EMP_REL;
+                    if (emp &&
                         (dp.tab_n <= 0 || dp.tab_off < 0 || (int64_t)dp.tab_off + dp.tab_n > (int64_t)H.alias.size()))
                         fail("alias table range");
+                    if (emp && dp.link_tab) {
+                        const int32_t *m = &H.stage_meta[(size_t)st * 8];
+                        int64_t first;  // the table's first entry in the stage's value region
+                        if (m[1] >= 0) {
+                            if (p.dvo < 0 || (p.dvo & kVtGlobal) || (p.dvo - m[7]) % (int32_t)sizeof(double))
+                                fail("link table offset");
+                            first = (p.dvo - m[7]) / (int32_t)sizeof(double);
+                        } else {
+                            if (p.dvo < 0 || !(p.dvo & kVtGlobal)) fail("link table index");
+                            first = (int64_t)(p.dvo ^ kVtGlobal) - m[4];
+                        }
+                        if (dp.tab_n > kLinkTableBins || first < 0 || first + dp.tab_n > m[5])
+                            fail("link table range");
+                        for (int32_t k = 0; k < dp.tab_n; ++k) {
+                            const AliasPick &pk = H.picks[(size_t)(dp.tab_off + k)];
+                            if (pk.alias < 0 || pk.alias >= dp.tab_n) fail("alias pick");
+                        }
+                    } else if (p.dvo != -1) {
+                        fail("link table without a table");
+                    }
                 }
                 if (!H.win_smem) {
                     if (p.src_slot != -1) fail("window slot without a window");
@@ -215,6 +250,8 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
     std::unordered_map<int32_t, TypeForm> form;
     H.dist.clear();
     H.alias.clear();
+    H.picks.clear();
+    std::unordered_map<int32_t, std::vector<double>> dist_values;  // empirical dists: values by bin
     for (const auto &kv : type_spec) {
         const DistSpec &s = g.dists[kv.second];
         TypeForm f{K_FIXED, -1, 0, 0.0, false};
@@ -269,6 +306,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
                 const double kk = k < 1.0 ? k + 1.0 : k;
                 const double dd = kk - 1.0 / 3.0;
                 p.boost = k < 1.0 ? 1 : 0;
+                p.erlang = (k == 1.0 || k == 2.0 || k == 3.0) ? (int32_t)k : 0;
                 p.f0 = (float)dd;
                 p.f1 = (float)(1.0 / std::sqrt(9.0 * dd));
                 p.f2 = (float)(1.0 / k);
@@ -292,9 +330,11 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
                 p.kind = f.relative ? K_EMP_REL : K_EMP_ABS;
                 p.tab_off = (int32_t)H.alias.size();
                 p.tab_n = (int32_t)s.values.size();
-                build_alias(s.values, s.weights, H.alias);
+                p.link_tab = p.tab_n <= kLinkTableBins ? 1 : 0;
+                build_alias(s.values, s.weights, H.alias, H.picks);
                 f.kind = p.kind;
                 f.dist = (int32_t)H.dist.size();
+                dist_values[f.dist] = s.values;
                 H.dist.push_back(p);
                 break;
             }
@@ -470,46 +510,62 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         std::stable_sort(by_level.begin() + lvl_off[l], by_level.begin() + lvl_off[l + 1],
                          [&](int32_t x, int32_t y) { return cost[x] > cost[y]; });
 
+    // per-link duration tables: bins of an empirical link's own table (kLinkTableBins), 0 without
+    auto table_bins = [&](int32_t l) -> int32_t {
+        if (l < 0 || l >= L) return 0;
+        const int kind = H.link_kd[l] & KD_KIND_MASK;
+        if (kind != K_EMP_ABS && kind != K_EMP_REL) return 0;
+        const DistParam &dp = H.dist[(size_t)(H.link_kd[l] >> 8)];
+        return dp.link_tab ? dp.tab_n : 0;
+    };
+    std::vector<int64_t> ev_vals((size_t)E, 0);  // value-region entries of an event's references
+    for (int32_t e = 0; e < E; ++e)
+        for (int64_t k = 0; k < tlen[e]; ++k) ev_vals[e] += table_bins(d.pred_act[tstart[e] + k]);
+
     // ---- 9) shared-memory budget: window rows, two record staging buffers
-    // (each stage's event and predecessor records), distribution tables
-    const size_t table_bytes = H.dist.size() * sizeof(DistParam) + H.alias.size() * sizeof(AliasEntry);
+    // (each stage's event and predecessor records and value region), distribution tables
+    const size_t table_bytes =
+        H.dist.size() * sizeof(DistParam) + H.alias.size() * (sizeof(AliasEntry) + sizeof(AliasPick));
     H.tables_in_smem = table_bytes <= kMaxTableBytes;
     const size_t fixed_bytes = (H.tables_in_smem ? table_bytes : 0) + 3 * 128;
     const size_t win_bytes = (size_t)H.window_slots * kTile * sizeof(double);
     H.win_smem = win_bytes <= kMaxWindowBytes && win_bytes + fixed_bytes + 2 * kMinStageBytes <= kSmemMax &&
                  std::getenv("MCD_NO_SMEM_WINDOW") == nullptr;
     const size_t avail = kSmemMax - fixed_bytes - (H.win_smem ? win_bytes : 0);
-    size_t budget = std::min(kMaxStageBytes, avail / 2);
+    size_t budget = std::min(kMaxStageBytes, avail / 2 > 256 ? avail / 2 - 256 : avail / 2);  // room for padding
 
     // ---- 10) stages (a level, or a slice of a wide level that fits a buffer)
     // and per-(stage, warp) chunks balanced by cost
     std::vector<int32_t> order;
-    std::vector<int32_t> meta;  // ev_first, n_ev (negated: unstaged), n_pred
+    std::vector<int32_t> meta;  // ev_first, n_ev (negated: unstaged), n_pred, n_val (even)
     std::vector<int32_t> wk;
     for (;;) {
         order.clear();
         meta.clear();
         wk.clear();
-        size_t max_ev = 0, max_pred = 0;
+        size_t max_bytes = 0;
         for (int32_t l = 0; l < n_levels; ++l) {
             int32_t i = lvl_off[l];
             while (i < lvl_off[l + 1]) {
                 // one stage: events i .. j-1 of this level
                 int32_t j = i;
-                size_t bytes = 0, nev = 0, npred = 0;
+                size_t bytes = 0, nev = 0, npred = 0, nval = 0;
                 while (j < lvl_off[l + 1]) {
-                    const size_t add = sizeof(EvRec) + (size_t)tlen[by_level[j]] * sizeof(PredRec);
+                    const size_t add = sizeof(EvRec) + (size_t)tlen[by_level[j]] * sizeof(PredRec) +
+                                       (size_t)ev_vals[by_level[j]] * sizeof(double);
                     if (j > i && bytes + add > budget) break;
                     bytes += add;
                     nev += 1;
                     npred += (size_t)tlen[by_level[j]];
+                    nval += (size_t)ev_vals[by_level[j]];
                     ++j;
                 }
+                nval = (nval + 1) / 2 * 2;  // 16-byte copies
+                if (nval > (size_t)std::numeric_limits<int32_t>::max() / 2)
+                    throw McdError(MCD_ERR_INVALID, "too many per-link table entries in one level");
                 const bool staged = bytes <= budget;
-                if (staged) {
-                    max_ev = std::max(max_ev, nev);
-                    max_pred = std::max(max_pred, npred);
-                }
+                if (staged) max_bytes = std::max(max_bytes, nev * sizeof(EvRec) + npred * sizeof(PredRec) +
+                                                               nval * sizeof(double));
                 double total = 0.0;
                 for (int32_t k = i; k < j; ++k) total += cost[by_level[k]];
                 const int32_t first = (int32_t)order.size();
@@ -532,27 +588,39 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
                 meta.push_back(first);
                 meta.push_back(staged ? (int32_t)nev : -(int32_t)nev);
                 meta.push_back((int32_t)npred);
+                meta.push_back((int32_t)nval);
+                meta.push_back((int32_t)(nev * sizeof(EvRec)));  // 48-byte records: 16-byte aligned offsets
+                meta.push_back((int32_t)(nev * sizeof(EvRec) + npred * sizeof(PredRec)));
                 i = j;
             }
         }
         wk.push_back((int32_t)order.size());
-        H.stage_pred_off = (int32_t)((max_ev * sizeof(EvRec) + 15) / 16 * 16);
-        H.stage_bytes = (int32_t)((H.stage_pred_off + max_pred * sizeof(PredRec) + 127) / 128 * 128);
+        H.stage_bytes = (int32_t)((max_bytes + 127) / 128 * 128);
         if (2 * (size_t)H.stage_bytes <= avail || budget <= kMinStageBytes) break;
         budget = std::max(kMinStageBytes, budget * 3 / 4);
     }
-    H.n_stages = (int32_t)(meta.size() / 3);
+    H.n_stages = (int32_t)(meta.size() / 6);
     H.wk_off = wk;
-    // stage_meta with predecessor offsets (records are laid out in compiled order)
-    H.stage_meta.assign((size_t)H.n_stages * 4, 0);
+    // stage_meta with predecessor and value offsets (records and value regions
+    // are laid out in compiled order)
+    H.stage_meta.assign((size_t)H.n_stages * 8, 0);
     {
-        int64_t pos = 0;
+        int64_t pos = 0, vpos = 0;
         for (int32_t st = 0; st < H.n_stages; ++st) {
-            H.stage_meta[(size_t)st * 4 + 0] = meta[(size_t)st * 3 + 0];
-            H.stage_meta[(size_t)st * 4 + 1] = meta[(size_t)st * 3 + 1];
-            H.stage_meta[(size_t)st * 4 + 2] = (int32_t)pos;
-            H.stage_meta[(size_t)st * 4 + 3] = meta[(size_t)st * 3 + 2];
-            pos += meta[(size_t)st * 3 + 2];
+            int32_t *m = &H.stage_meta[(size_t)st * 8];
+            const int32_t *q = &meta[(size_t)st * 6];
+            m[0] = q[0];
+            m[1] = q[1];
+            m[2] = (int32_t)pos;
+            m[3] = q[2];
+            if (vpos + q[3] >= (int64_t)kVtGlobal)  // table indices must stay below the flag bit
+                throw McdError(MCD_ERR_INVALID, "too many per-link table entries");
+            m[4] = (int32_t)vpos;
+            m[5] = q[3];
+            m[6] = q[4];
+            m[7] = q[5];
+            pos += q[2];
+            vpos += q[3];
         }
     }
     // layout: [window][stage buffer 0][stage buffer 1][tables][2 mbarriers, 2 stage counters]
@@ -596,8 +664,25 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         H.max_abs_time = std::max(H.max_abs_time, std::max(std::fabs(d.earliest[e]), std::fabs(H.ub[e])));
         H.max_span = std::max(H.max_span, H.ub[e] - d.earliest[e]);
     }
+    H.vals.clear();
+    int32_t st_cur = -1;
+    int64_t st_end = 0, vbase = 0;
+    auto close_stage = [&]() {  // pad the stage's value region to its recorded (even) size
+        if (st_cur < 0) return;
+        const int32_t *m = &H.stage_meta[(size_t)st_cur * 8];
+        if ((int64_t)H.vals.size() - vbase > m[5]) throw McdError(MCD_ERR_RUNTIME, "value region overflow");
+        while ((int64_t)H.vals.size() < vbase + m[5]) H.vals.push_back(0.0);
+    };
     for (int32_t i = 0; i < E; ++i) {
         const int32_t e = order[i];
+        while (i >= st_end) {  // the first event of the next stage
+            close_stage();
+            ++st_cur;
+            const int32_t *m = &H.stage_meta[(size_t)st_cur * 8];
+            st_end = (int64_t)m[0] + (m[1] >= 0 ? m[1] : -(int64_t)m[1]);
+            vbase = (int64_t)H.vals.size();
+            if (vbase != m[4]) throw McdError(MCD_ERR_RUNTIME, "value region offset");
+        }
         EvRec r{};
         r.user = e;
         r.slot = H.win_smem ? slot[e] : -1;
@@ -624,12 +709,12 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
                 p.link = -1;
                 p.kd = K_FIXED;
                 p.v = 0.0;
-                p.dv = 0.0f;
+                p.dvo = float_bits(0.0f);
             } else {
                 p.link = l;
                 p.kd = H.link_kd[l];
                 p.v = H.link_v[l];
-                p.dv = H.link_dv[l];
+                p.dvo = float_bits(H.link_dv[l]);
                 p.block = -1;
                 if ((H.link_kd[l] & KD_KIND_MASK) != K_FIXED) {
                     if (H.link_block[l] < 0) {  // first reference: the link's block and word
@@ -652,6 +737,19 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
                         last_block = p.block;
                     }
                 }
+                if ((H.link_kd[l] & KD_KIND_MASK) != K_FIXED) p.dvo = -1;
+                if (const int32_t nb = table_bins(l)) {  // the link's duration table, bin by bin
+                    const int32_t di = H.link_kd[l] >> 8;
+                    const bool rel = (H.link_kd[l] & KD_KIND_MASK) == K_EMP_REL;
+                    const double base = H.link_v[l];
+                    const int32_t *sm = &H.stage_meta[(size_t)st_cur * 8];
+                    const int64_t local = (int64_t)H.vals.size() - vbase;
+                    if (sm[1] >= 0) p.dvo = (int32_t)(sm[7] + local * (int64_t)sizeof(double));  // staged: byte offset
+                    else p.dvo = kVtGlobal | (int32_t)(vbase + local);                           // index in vals
+                    const std::vector<double> &vv = dist_values[di];
+                    for (int32_t k = 0; k < nb; ++k)
+                        H.vals.push_back(rel ? base + vv[(size_t)k] * base : base + vv[(size_t)k]);  // _core.cpp:140, 328
+                }
                 if (!written[l]) {  // the first reference stores the link's duration row
                     p.kd |= KD_WRITE;
                     written[l] = 1;
@@ -663,6 +761,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         r.pred_end = (int32_t)H.pred.size();
         H.ev[i] = r;
     }
+    close_stage();
     // ---- 12) positive mode: every earliest, bound and duration is a non-negative
     // finite double, so t = src + dur never is NaN or negative and the raw bit
     // patterns order like the values
@@ -672,6 +771,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         for (int32_t e = 0; pos && e < E; ++e) pos = nonneg(d.earliest[e]) && nonneg(H.ub[e]);
         for (int32_t l = 0; pos && l < L; ++l) pos = nonneg(H.link_v[l]) && H.link_v[l] < 1e300;
         for (const AliasEntry &ae : H.alias) pos = pos && nonneg(ae.v_self) && nonneg(ae.v_alias) && ae.v_self < 1e300;
+        for (double x : H.vals) pos = pos && nonneg(x);
         H.positive = pos;
     }
     H.aux.clear();
@@ -689,6 +789,23 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         H.aux.push_back(LinkRec{l, kd, H.link_v[l]});
     }
     verify_layout(H);
+}
+
+size_t tables_bytes(const HostDag &h) {
+    return h.dist.size() * sizeof(DistParam) + h.alias.size() * (sizeof(AliasEntry) + sizeof(AliasPick));
+}
+
+std::vector<unsigned char> tables_block(const HostDag &h) {
+    std::vector<unsigned char> b(tables_bytes(h));
+    size_t o = 0;
+    auto put = [&](const void *src, size_t n) {
+        if (n) std::memcpy(b.data() + o, src, n);
+        o += n;
+    };
+    put(h.dist.data(), h.dist.size() * sizeof(DistParam));
+    put(h.alias.data(), h.alias.size() * sizeof(AliasEntry));
+    put(h.picks.data(), h.picks.size() * sizeof(AliasPick));
+    return b;
 }
 
 // Ticks of 2^-q seconds: every |time| * 2^q must stay below 2^62, and the sum

@@ -90,24 +90,39 @@ __device__ __forceinline__ long long order_key(long long b) {
 }
 
 // ---------------------------------------------------------------- integer FP64 helpers
-// Bits of the double 1 + x for a float x >= 0, built with integer operations
-// (a float-to-double conversion would occupy the FP64 pipe).  Exact when
-// x >= 2^-29 (the float's 24 significant bits then fit the double's fraction);
-// smaller x are truncated to 2^-52.  x >= 1 goes through the float sum 1 + x.
-// A sampled duration is then base * (1 + X): one FP64 multiply.
-__device__ __forceinline__ long long one_plus(float x) {
-    const uint32_t b = __float_as_uint(x);
-    const int e = (int)((b >> 23) & 0xFF);
-    if (e == 0) return 0x3FF0000000000000ll;  // zero (or subnormal): 1.0
-    if (e < 127) {
-        const unsigned long long m = (b & 0x7FFFFFu) | 0x800000u;
-        const int sh = e - 98;  // m * 2^(e-150) * 2^52
-        const unsigned long long frac = sh >= 0 ? (m << sh) : (sh > -24 ? (m >> -sh) : 0ull);
-        return (long long)(0x3FF0000000000000ull | frac);
-    }
-    const uint32_t f = __float_as_uint(1.0f + x);  // x >= 1: 1 + x in float
-    const unsigned long long fe = (f >> 23) & 0xFF;
-    return (long long)(((fe + 896ull) << 52) | ((unsigned long long)(f & 0x7FFFFFu) << 29));
+// 32 x 32 -> 64-bit unsigned product (one wide integer multiply).
+__device__ __forceinline__ unsigned long long mul_wide(uint32_t a, uint32_t b) {
+    unsigned long long r;
+    asm("mul.wide.u32 %0, %1, %2;" : "=l"(r) : "r"(a), "r"(b));
+    return r;
+}
+
+// The rare cases of scale_by, out of line so that the compiler branches around
+// them instead of predicating a conversion and a multiply on the FP64 pipe.
+static __device__ __noinline__ double scale_by_fp64(double base, float m) { return __dmul_rn(base, (double)m); }
+
+// base * m for a double base and a float m >= 1: the 53 leading bits of the
+// exact product (truncated), from two 32 x 32-bit integer products -- the FP64
+// pipe of this part issues about 1.6 lane-operations per clock per SM, so a
+// sampled duration spends none of it.  Zero, subnormal and non-finite bases,
+// an infinite m, and products within a factor of two of overflow take one FP64
+// multiply instead.
+__device__ __forceinline__ double scale_by(double base, float m) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(base);
+    const uint32_t bh = (uint32_t)(b >> 32);
+    const uint32_t eb = (bh >> 20) & 0x7FFu;
+    const uint32_t fm = __float_as_uint(m);
+    const uint32_t e = eb + (fm >> 23) - 127u;  // m >= 1: sign 0, exponent field >= 127
+    if (eb == 0u || e >= 0x7FEu || fm >= 0x7F800000u) return scale_by_fp64(base, m);  // a branch, not predicated
+    const uint32_t mf = (fm & 0x7FFFFFu) | 0x800000u;                  // 24 bits
+    const unsigned long long hi = mul_wide((bh & 0xFFFFFu) | 0x100000u, mf);  // < 2^45
+    const unsigned long long lo = mul_wide((uint32_t)b, mf);                  // < 2^56
+    // floor(P / 2^23) of the 77-bit mantissa product P = (hi << 32) + lo in [2^75, 2^77)
+    unsigned long long q = (hi << 9) + (lo >> 23);
+    const uint32_t top = (uint32_t)(q >> 53);  // P >= 2^76: one more exponent step
+    q >>= top;                                 // [2^52, 2^53): the hidden bit carries into the exponent
+    return __longlong_as_double(
+        (long long)((b & 0x8000000000000000ull) + ((unsigned long long)(e + top - 1u) << 52) + q));
 }
 
 // ---------------------------------------------------------------- samplers
@@ -116,70 +131,93 @@ __device__ __forceinline__ long long one_plus(float x) {
 // Exponential with mean lambda_, redrawn above max_scale (_core.cpp:83-89).  The
 // redraw loop is replaced by the inverse CDF of the truncated law, which is the
 // same distribution: X = -lambda_ * log(1 - c u), c = 1 - exp(-max_scale/lambda_).
-// r: the link's random word.
+// r: the link's random word.  The duration is base * (1 + X), 1 + X in float.
 __device__ __forceinline__ double draw_exponential(const DistParam &p, double base, uint32_t r, float &dfac) {
     const float w = u01_open0(r);         // plays the role of 1 - u
     const float V = fmaf(p.f1, w, p.f2);  // 1 - c (1 - w), in (1-c, 1]
     float X = -p.f0 * __logf(V);
     X = fmaxf(fminf(X, p.f3), 0.0f);
     dfac = 1.0f + X;
-    return base * __longlong_as_double(one_plus(X));  // base + X * base
+    return scale_by(base, dfac);
 }
 
-// Gamma(shape, scale) redrawn above max_scale (_core.cpp:98-104), by Marsaglia &
-// Tsang (ACM TOMS 26(3), 2000) in FP32, normals from Box-Muller.  Shapes below 1
-// draw Gamma(shape+1) times U^(1/shape).  Rejection loops are capped; a lane that
+// Gamma(shape, scale) redrawn above max_scale (_core.cpp:98-104).  Shapes 1, 2
+// and 3 are sums of that many exponentials (Erlang): X = -scale * log(U1 U2 U3),
+// one Philox block per attempt.  Other shapes by Marsaglia & Tsang (ACM TOMS
+// 26(3), 2000) in FP32, normals from Box-Muller; shapes below 1 draw
+// Gamma(shape+1) times U^(1/shape).  Rejection loops are capped; a lane that
 // hits the cap latches ERR_GAMMA_REJECTION and returns the truncation point.
 // Inlined: the out-of-line call measured 2.5 % slower on the five-kind workload
 // (the call convention costs the loop more than the sampler's temporaries).
 static __device__ __forceinline__ double draw_gamma(const DistParam &p, double base, uint32_t link, uint64_t seed,
                                                  int32_t *err, float *dfac) {
-    const float d = p.f0, cc = p.f1;
-    for (uint32_t attempt = 0; attempt < 4096u; ++attempt) {
-        const U4 r = draw_words(seed, link, attempt, 0u);
-        const float rad = __fsqrt_rn(-2.0f * __logf(u01_open0(r.x)));
-        float sn, cs;
-        __sincosf(6.2831853071795865f * ((float)(r.y >> 8) * 5.9604644775390625e-08f), &sn, &cs);
-        float X = -1.0f;
+    if (p.erlang) {
+        for (uint32_t attempt = 0; attempt < 4096u; ++attempt) {
+            const U4 r = draw_words(seed, link, attempt, 0u);
+            float prod = u01_open0(r.x);
+            if (p.erlang > 1) prod *= u01_open0(r.y);
+            if (p.erlang > 2) prod *= u01_open0(r.z);
+            const float X = fmaxf(-p.f3 * __logf(prod), 0.0f);
+            if (X > p.f4) continue;
+            *dfac = 1.0f + X;
+            return scale_by(base, *dfac);
+        }
+    } else {
+        const float d = p.f0, cc = p.f1;
+        for (uint32_t attempt = 0; attempt < 4096u; ++attempt) {
+            const U4 r = draw_words(seed, link, attempt, 0u);
+            const float rad = __fsqrt_rn(-2.0f * __logf(u01_open0(r.x)));
+            float sn, cs;
+            __sincosf(6.2831853071795865f * ((float)(r.y >> 8) * 5.9604644775390625e-08f), &sn, &cs);
+            float X = -1.0f;
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
-            const float z = j == 0 ? rad * cs : rad * sn;
-            const float t = fmaf(cc, z, 1.0f);
-            if (X < 0.0f && t > 0.0f) {
-                const float v = t * t * t;
-                const float u = u01_open0(j == 0 ? r.z : r.w);
-                const float z2 = z * z;
-                if (u < 1.0f - 0.0331f * z2 * z2 || __logf(u) < 0.5f * z2 + d * (1.0f - v + __logf(v))) X = d * v;
+            for (int j = 0; j < 2; ++j) {
+                const float z = j == 0 ? rad * cs : rad * sn;
+                const float t = fmaf(cc, z, 1.0f);
+                if (X < 0.0f && t > 0.0f) {
+                    const float v = t * t * t;
+                    const float u = u01_open0(j == 0 ? r.z : r.w);
+                    const float z2 = z * z;
+                    if (u < 1.0f - 0.0331f * z2 * z2 || __logf(u) < 0.5f * z2 + d * (1.0f - v + __logf(v)))
+                        X = d * v;
+                }
             }
+            if (X < 0.0f) continue;
+            if (p.boost) {
+                const U4 r2 = draw_words(seed, link, attempt, 1u);
+                X *= exp2f(__log2f(u01_open0(r2.x)) * p.f2);
+            }
+            X *= p.f3;
+            if (X > p.f4) continue;
+            *dfac = 1.0f + X;
+            return scale_by(base, *dfac);
         }
-        if (X < 0.0f) continue;
-        if (p.boost) {
-            const U4 r2 = draw_words(seed, link, attempt, 1u);
-            X *= exp2f(__log2f(u01_open0(r2.x)) * p.f2);
-        }
-        X *= p.f3;
-        if (X > p.f4) continue;
-        *dfac = 1.0f + X;
-        return base * __longlong_as_double(one_plus(X));
     }
     atomicOr(err, ERR_GAMMA_REJECTION);
     *dfac = 1.0f + p.f4;
-    return base * __longlong_as_double(one_plus(p.f4));
+    return scale_by(base, *dfac);
 }
 
 // Empirical tables (_core.cpp:110-141) by Walker/Vose alias sampling.  One
 // word r: the bin is the high half of r * n and the low half, uniform on a
 // lattice of spacing n / 2^32, decides bin or alias (tables of at most
-// kOneWordBins bins); two words (r, r2): r picks the bin, r2 decides.  The duration is
-// formed exactly as the reference forms it -- base + value (absolute, :125, 328)
-// or base + factor * base (relative, :140, 328) -- so each bin yields the
-// reference's bit pattern: the values are atoms, and any last-bit difference
-// would separate the two discrete distributions.
-__device__ __forceinline__ double draw_empirical(const DistParam &p, const AliasEntry *alias, double base,
-                                                 bool relative, uint32_t r, uint32_t r2, bool two_word,
-                                                 float &dfac) {
+// kOneWordBins bins); two words (r, r2): r picks the bin, r2 decides.  The
+// duration is the reference's -- base + value (absolute, :125, 328) or base +
+// factor * base (relative, :140, 328) -- bit for bit, because the values are
+// atoms and any last-bit difference would separate the two discrete
+// distributions: read from the link's own table (vt, kLinkTableBins) or, for
+// larger tables and links without one, evaluated here in FP64.
+__device__ __forceinline__ double draw_empirical(const DistParam &p, const AliasEntry *alias, const AliasPick *picks,
+                                                 const double *vt, double base, bool relative, uint32_t r,
+                                                 uint32_t r2, bool two_word, float &dfac) {
     const uint32_t j = __umulhi(r, (uint32_t)p.tab_n);
     const uint32_t u = two_word ? r2 : r * (uint32_t)p.tab_n;
+    if (vt) {
+        const AliasPick pk = picks[p.tab_off + j];
+        const int k = u < pk.thresh ? (int)j : pk.alias;
+        dfac = relative ? 1.0f + (float)alias[p.tab_off + k].v_self : 1.0f;
+        return vt[k];
+    }
     const AliasEntry &e = alias[p.tab_off + j];
     const double val = u < e.thresh ? e.v_self : e.v_alias;
     dfac = relative ? 1.0f + (float)val : 1.0f;
@@ -188,25 +226,68 @@ __device__ __forceinline__ double draw_empirical(const DistParam &p, const Alias
 
 // The link's duration for one sample, and (dfac) its derivative with respect to
 // the base duration: 1 + X for the multiplicative kinds, 1 for absolute tables,
-// the host-computed value (dv) for fixed links.  block: the link's Philox
-// block; grp: the words of the block the event's previous exponential or
-// empirical reference drew, redrawn here unless KD_REUSE says they are this
-// link's block.
-__device__ __forceinline__ double link_duration(int32_t kd, double v, float dv, uint32_t block, uint64_t seed,
-                                                U4 &grp, const DistParam *dists, const AliasEntry *alias,
-                                                int32_t *err, float &dfac) {
+// the host-computed value for fixed links.  block: the link's Philox block;
+// grp: the words of the block the event's previous exponential or empirical
+// reference drew, redrawn here unless KD_REUSE says they are this link's block.
+// dvo: the record's dvo (PredRec); stage: the stage whose staging buffer holds
+// the link's duration table.  dists: the tables block (distributions, then
+// alias entries and picks); every other table address is derived here from
+// the kernel arguments, so that the propagation loop keeps no more pointers live.
+__device__ __forceinline__ double link_duration(const KArgs &a, int32_t kd, double v, int32_t dvo, uint32_t block,
+                                                uint64_t seed, U4 &grp, const DistParam *dists,
+                                                const unsigned char *smem, int stage, float &dfac) {
     const int kind = kd & KD_KIND_MASK;
     if (kind == K_FIXED) {
-        dfac = dv;
+        dfac = __int_as_float(dvo);
         return v;
     }
     const DistParam &p = dists[kd >> 8];
+    int32_t *err = a.err;
+    const AliasEntry *alias = reinterpret_cast<const AliasEntry *>(dists + a.n_dist);
+    const AliasPick *picks = reinterpret_cast<const AliasPick *>(alias + a.n_alias);
     if (kind == K_GAMMA) return draw_gamma(p, v, block, seed, err, &dfac);
     if (!(kd & KD_REUSE)) grp = draw_words(seed, block, 0u, 0u);
     const int wsel = (kd >> KD_WORD_SHIFT) & 3;
     const uint32_t r = wsel == 0 ? grp.x : wsel == 1 ? grp.y : wsel == 2 ? grp.z : grp.w;
     if (kind == K_EXP) return draw_exponential(p, v, r, dfac);
-    return draw_empirical(p, alias, v, kind == K_EMP_REL, r, grp.y, (kd & KD_TWO_WORD) != 0, dfac);
+    const double *vt = nullptr;
+    if (dvo >= 0)
+        vt = (dvo & kVtGlobal) ? a.vals + (dvo ^ kVtGlobal)
+                               : reinterpret_cast<const double *>(smem + a.smem_stage_off + (stage & 1) * a.stage_bytes +
+                                                                  dvo);
+    return draw_empirical(p, alias, picks, vt, v, kind == K_EMP_REL, r, grp.y, (kd & KD_TWO_WORD) != 0, dfac);
+}
+
+// ---------------------------------------------------------------- records
+// Record reads as 16-byte vector loads (two for a predecessor, three for an event).
+__device__ __forceinline__ PredRec load_pred(const PredRec *p) {
+    const int4 a = reinterpret_cast<const int4 *>(p)[0];
+    const int4 b = reinterpret_cast<const int4 *>(p)[1];
+    PredRec r;
+    r.src_slot = a.x;
+    r.src_user = a.y;
+    r.link = a.z;
+    r.kd = a.w;
+    r.v = __hiloint2double(b.y, b.x);
+    r.dvo = b.z;
+    r.block = b.w;
+    return r;
+}
+
+__device__ __forceinline__ EvRec load_ev(const EvRec *p) {
+    const int4 a = reinterpret_cast<const int4 *>(p)[0];
+    const int4 b = reinterpret_cast<const int4 *>(p)[1];
+    const int4 c = reinterpret_cast<const int4 *>(p)[2];
+    EvRec r;
+    r.user = a.x;
+    r.slot = a.y;
+    r.pred_begin = a.z;
+    r.pred_end = a.w;
+    r.init_bits = (int64_t)(((uint64_t)(uint32_t)b.y << 32) | (uint32_t)b.x);
+    r.init_key = (int64_t)(((uint64_t)(uint32_t)b.w << 32) | (uint32_t)b.z);
+    r.ub_bits = (int64_t)(((uint64_t)(uint32_t)c.y << 32) | (uint32_t)c.x);
+    r.ub_key = (int64_t)(((uint64_t)(uint32_t)c.w << 32) | (uint32_t)c.z);
+    return r;
 }
 
 // ---------------------------------------------------------------- TMA staging
@@ -240,18 +321,24 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
         : "memory");
 }
 
-// Issues the copies of one stage's event and predecessor records into a buffer.
-// A stage too large for the buffer (n_ev stored negated) copies nothing; its
-// barrier phase still completes, so the buffers' phases stay in step.
+// Issues the copies of one stage's event records, predecessor records and value
+// region into a buffer.  A stage too large for the buffer (n_ev stored negated)
+// copies nothing; its barrier phase still completes, so the buffers' phases
+// stay in step.  A value region holds an even number of doubles (16-byte sizes
+// and offsets).
 __device__ __forceinline__ void stage_issue(const KArgs &a, int stage, char *buf, uint64_t *bar) {
-    const int4 m = __ldg(reinterpret_cast<const int4 *>(a.stage_meta) + stage);  // ev_first, n_ev, pred_first, n_pred
+    const int4 *meta = reinterpret_cast<const int4 *>(a.stage_meta) + 2 * stage;
+    const int4 m = __ldg(meta);       // ev_first, n_ev, pred_first, n_pred
+    const int4 mv = __ldg(meta + 1);  // val_first, n_val, byte offsets of predecessor records and values
     const bool staged = m.y >= 0;
     const uint32_t ev_bytes = staged ? (uint32_t)m.y * (uint32_t)sizeof(EvRec) : 0u;
     const uint32_t pr_bytes = staged ? (uint32_t)m.w * (uint32_t)sizeof(PredRec) : 0u;
+    const uint32_t va_bytes = staged ? (uint32_t)mv.y * (uint32_t)sizeof(double) : 0u;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_expect_tx(bar, ev_bytes + pr_bytes);
+    mbar_expect_tx(bar, ev_bytes + pr_bytes + va_bytes);
     if (ev_bytes) bulk_g2s(buf, a.ev + m.x, ev_bytes, bar);
-    if (pr_bytes) bulk_g2s(buf + a.stage_pred_off, a.pred + m.z, pr_bytes, bar);
+    if (pr_bytes) bulk_g2s(buf + mv.z, a.pred + m.z, pr_bytes, bar);
+    if (va_bytes) bulk_g2s(buf + mv.w, a.vals + mv.x, va_bytes, bar);
 }
 
 // Bounded wait for a stage buffer; false (and the error flag latched) if the copy
@@ -328,7 +415,9 @@ __device__ __forceinline__ void accumulate_sum(const KArgs &a, const EvRec &ev, 
 // Returns false when a staged copy never landed (then every thread returns false).
 //
 // Shared memory: [window: window_slots x 32 doubles][stage buffer 0][stage
-// buffer 1][distribution params][alias table][2 mbarriers, 2 stage counters];
+// buffer 1][distribution params][alias entries][alias picks][2 mbarriers, 2
+// stage counters]; a stage buffer holds [event records][predecessor
+// records][value region];
 // `bars` is that layout's barrier region (kBarRegionBytes), or one fixed region
 // for every tile of a persistent CTA (a barrier stays where it was
 // initialised: only the same address is invalidated and initialised again
@@ -346,9 +435,7 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
     double *win = reinterpret_cast<double *>(smem);
     char *stage_buf0 = reinterpret_cast<char *>(smem + a.smem_stage_off);
     DistParam *s_dist = reinterpret_cast<DistParam *>(smem + a.smem_tables_off);
-    AliasEntry *s_alias = reinterpret_cast<AliasEntry *>(smem + a.smem_tables_off + a.n_dist * sizeof(DistParam));
     const DistParam *dists = a.tables_in_smem ? s_dist : a.dist;
-    const AliasEntry *alias = a.tables_in_smem ? s_alias : a.alias;
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -361,9 +448,10 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
     if (!GIVEN && active) seed = a.seeds ? (uint64_t)a.seeds[s] : (uint64_t)(a.seed0 + s);
 
     // distribution tables into shared memory; fresh barriers for this tile
-    if (a.tables_in_smem) {
-        for (int i = threadIdx.x; i < a.n_dist; i += blockDim.x) s_dist[i] = a.dist[i];
-        for (int i = threadIdx.x; i < a.n_alias; i += blockDim.x) s_alias[i] = a.alias[i];
+    if (a.tables_in_smem) {  // the tables block, 8 bytes at a time (its size is a multiple of 8)
+        const int n8 = (a.n_dist * (int)sizeof(DistParam) + a.n_alias * (int)(sizeof(AliasEntry) + sizeof(AliasPick))) / 8;
+        for (int i = threadIdx.x; i < n8; i += blockDim.x)
+            reinterpret_cast<uint2 *>(s_dist)[i] = reinterpret_cast<const uint2 *>(a.dist)[i];
     }
     int *stage_ctr = reinterpret_cast<int *>(bars + 2);
     U4 grp{};  // the words of the Philox block the current event last drew (see KD_REUSE)
@@ -398,11 +486,11 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
             __syncthreads();
             return false;
         }
-        const int4 meta = __ldg(reinterpret_cast<const int4 *>(a.stage_meta) + l);
+        const int4 meta = __ldg(reinterpret_cast<const int4 *>(a.stage_meta) + 2 * l);
+        const int4 mv = __ldg(reinterpret_cast<const int4 *>(a.stage_meta) + 2 * l + 1);
         // a stage whose records exceed the buffer is read from global memory
         const EvRec *sev = meta.y >= 0 ? reinterpret_cast<const EvRec *>(buf) : a.ev + meta.x;
-        const PredRec *spred = meta.y >= 0 ? reinterpret_cast<const PredRec *>(buf + a.stage_pred_off)
-                                           : a.pred + meta.z;
+        const PredRec *spred = meta.y >= 0 ? reinterpret_cast<const PredRec *>(buf + mv.z) : a.pred + meta.z;
         const int n_ev = meta.y >= 0 ? meta.y : -meta.y;
         if (threadIdx.x == 0) stage_ctr[(l + 1) & 1] = 0;  // last used by stage l - 1, before the barrier
         // the next index is taken before this event's work, hiding the atomic's
@@ -414,19 +502,19 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
             const int i = i_next;
             if (lane == 0) i_next = atomicAdd(&stage_ctr[l & 1], 1);
             i_next = __shfl_sync(0xFFFFFFFFu, i_next, 0);
-            const EvRec ev = sev[i];
+            const EvRec ev = load_ev(sev + i);
             long long lk = ev.init_key, lbits = ev.init_bits;
             int32_t cause = -1;
             uint32_t win_code = kAdjNone;  // ADJ: winner position | clamp flag
             float win_dfac = 0.0f;
             for (int p = ev.pred_begin - meta.z; p < ev.pred_end - meta.z; ++p) {
-                const PredRec pr = spred[p];
+                const PredRec pr = load_pred(spred + p);
                 double dur;
                 float dfac = 0.0f;
                 if (GIVEN) {
                     dur = (active && pr.link >= 0) ? __ldg(&a.dur_in[(int64_t)pr.link * a.ld_in + s]) : 0.0;
                 } else {
-                    dur = link_duration(pr.kd, pr.v, pr.dv, (uint32_t)pr.block, seed, grp, dists, alias, a.err,
+                    dur = link_duration(a, pr.kd, pr.v, pr.dvo, (uint32_t)pr.block, seed, grp, dists, smem, l,
                                         dfac);
                     if (!STATS && !ADJ && (pr.kd & KD_WRITE) && a.durations && active)
                         a.durations[(int64_t)pr.link * a.ld + s] = dur;
@@ -483,8 +571,7 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
             const LinkRec lr = a.aux[i];
             float dfac;
             U4 own;  // an unreferenced link owns its block
-            const double dur =
-                link_duration(lr.kd, lr.v, 0.0f, (uint32_t)lr.link, seed, own, dists, alias, a.err, dfac);
+            const double dur = link_duration(a, lr.kd, lr.v, -1, (uint32_t)lr.link, seed, own, dists, smem, 0, dfac);
             if (active) a.durations[(int64_t)lr.link * a.ld + s] = dur;
         }
     }

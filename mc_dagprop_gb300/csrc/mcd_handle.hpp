@@ -19,8 +19,8 @@ struct mcd_dag {
     mcd::EvRec *d_ev = nullptr;
     mcd::PredRec *d_pred = nullptr;
     mcd::LinkRec *d_aux = nullptr;
-    mcd::DistParam *d_dist = nullptr;
-    mcd::AliasEntry *d_alias = nullptr;
+    mcd::DistParam *d_dist = nullptr;  // tables block: distributions, alias entries, alias picks
+    double *d_vals = nullptr;
     int32_t *d_wk = nullptr;
     int32_t *d_stage_meta = nullptr;
     double *d_earliest = nullptr;  // caller order, for the statistics finish

@@ -48,7 +48,7 @@ constexpr int32_t kMaxBatchWarps = 24;  // persistent batch kernel: 768 threads 
 // n_warps request: automatic, rounded up to 2, 4, 8, 12 or 24 warps -- block
 // sizes whose CTAs fill an SM's 24 warps at the batch kernel's 80 registers
 constexpr int32_t kBatchClassWarps = -1;
-constexpr size_t kMaxStageBytes = 24 * 1024;
+constexpr size_t kMaxStageBytes = 40 * 1024;
 constexpr size_t kMinStageBytes = 4 * 1024;
 constexpr size_t kMaxTableBytes = 16 * 1024;
 constexpr size_t kSmemMax = 226 * 1024;  // 227 KB per CTA, less room for static shared data
@@ -60,15 +60,17 @@ struct HostDag {
     bool positive = false;        // all times non-negative and finite
     int64_t max_preds = 0;        // largest predecessor list
     bool tables_in_smem = true;
-    int32_t n_stages = 0, stage_bytes = 0, stage_pred_off = 0;
+    int32_t n_stages = 0, stage_bytes = 0;
     int32_t smem_stage_off = 0, smem_tables_off = 0, smem_bar_off = 0, smem_total = 0;
-    std::vector<int32_t> stage_meta;  // 4 ints per stage
+    std::vector<int32_t> stage_meta;  // 8 ints per stage (KArgs::stage_meta)
     std::vector<EvRec> ev;
     std::vector<PredRec> pred;
     std::vector<LinkRec> aux;  // links stored by the aux pass
     int32_t n_orphan = 0;      // sampled links no precedence entry references
     std::vector<DistParam> dist;
     std::vector<AliasEntry> alias;
+    std::vector<AliasPick> picks;  // parallel to alias
+    std::vector<double> vals;      // per-link duration tables, stage by stage
     std::vector<int32_t> wk_off;
     std::vector<int32_t> link_kd;
     std::vector<double> link_v;
@@ -93,6 +95,11 @@ struct StatsParams {
     double bin_w = 0.0;  // seconds per bin
 };
 StatsParams stats_params(const HostDag &h, int64_t n);
+
+// The tables block as the kernels read it (KArgs::dist): DistParam[n_dist],
+// AliasEntry[n_alias], AliasPick[n_alias], back to back.
+size_t tables_bytes(const HostDag &h);
+std::vector<unsigned char> tables_block(const HostDag &h);
 
 // n_warps: warps per CTA the kernels will run with (0: chosen from the DAG's width).
 void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &out, int32_t n_warps);

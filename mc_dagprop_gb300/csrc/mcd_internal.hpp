@@ -53,9 +53,23 @@ struct alignas(16) PredRec {
                        // past the last link, which has duration 0 (see the compiler)
     int32_t kd;        // packed kind word (above)
     double v;          // FIXED: the duration; otherwise the base (minimal_duration)
-    float dv;          // FIXED: d(duration)/d(base) (1 + factor, 1, or 0 for gaps)
+    int32_t dvo;       // FIXED: bits of the float d(duration)/d(base) (1 + factor, 1, or 0
+                       // for gaps); empirical kinds: where the link's duration table is
+                       // (see kLinkTableBins), -1 without one
     int32_t block;     // Philox block of the link's random words (-1: fixed)
 };
+
+// Empirical links whose table has at most kLinkTableBins bins carry a duration
+// table of their own: entry k is the reference's duration for bin k, evaluated
+// once on the host with its two roundings (base + value, _core.cpp:125, 328;
+// base + factor * base, :140, 328).  The tables of a stage's references follow
+// its predecessor records (the stage's value region, staged with them), so a
+// draw is a bin choice and one shared-memory read -- no FP64 arithmetic.
+// PredRec::dvo locates the table: the byte offset of its first entry inside the
+// staging buffer, or, for a stage read from global memory, kVtGlobal | the index
+// of its first entry in KArgs::vals.
+constexpr int32_t kLinkTableBins = 32;
+constexpr int32_t kVtGlobal = 0x40000000;
 
 // A link whose duration row the aux pass stores: a link no precedence entry
 // references (its duration is still part of SimResult.durations).  16 bytes.
@@ -76,7 +90,8 @@ struct alignas(16) DistParam {
     //              f3 = largest float <= max_scale
     // gamma:       f0 = d = shape' - 1/3, f1 = 1/sqrt(9 d), f2 = 1/shape, f3 = scale,
     //              f4 = largest float <= max_scale
-    int32_t pad[2];
+    int32_t erlang;    // gamma: the shape when it is 1, 2 or 3 (sum of exponentials), else 0
+    int32_t link_tab;  // empirical: tables of at most kLinkTableBins bins (per-link duration tables)
 };
 
 // Walker/Vose alias entry: bin j is kept when a 32-bit uniform is below
@@ -87,6 +102,15 @@ struct alignas(16) AliasEntry {
     double v_alias;
     uint32_t thresh;
     uint32_t pad[3];
+};
+
+// The bin choice of the same table, 8 bytes per bin so that 32 lanes reading
+// random bins of a table of up to 32 bins hit distinct shared-memory banks:
+// bin j is kept when the uniform is below `thresh`, else bin `alias` is taken
+// (alias == j when thresh is 0xFFFFFFFF).  Parallel to the AliasEntry array.
+struct alignas(8) AliasPick {
+    uint32_t thresh;
+    int32_t alias;
 };
 
 // Adjoint forward record per (event, sample): the winning predecessor's position
@@ -111,10 +135,12 @@ struct KArgs {
     const EvRec *ev;
     const PredRec *pred;
     const LinkRec *aux;
-    const DistParam *dist;
-    const AliasEntry *alias;
+    const DistParam *dist;    // tables block: DistParam[n_dist], AliasEntry[n_alias], AliasPick[n_alias]
     const int32_t *wk_off;    // [n_stages * n_warps + 1] event chunk per (stage, warp), compiled indices
-    const int32_t *stage_meta;  // [n_stages][4] {first event, events (negated: read from global), first pred, preds}
+    const int32_t *stage_meta;  // [n_stages][8] {first event, events (negated: read from global), first pred, preds,
+                                //  first value, values, byte offsets of the predecessor records and of the
+                                //  value region inside a staging buffer}
+    const double *vals;         // per-link duration tables, stage by stage (value regions)
     int32_t n_stages;
     int32_t n_warps;
     int32_t n_aux;
@@ -124,7 +150,6 @@ struct KArgs {
     int32_t win_smem;         // window on chip (batch kernel dispatch)
     int32_t positive;         // every time non-negative and finite: raw bits order like doubles
     int32_t stage_bytes;      // one staging buffer
-    int32_t stage_pred_off;   // predecessor records' offset inside a staging buffer
     int32_t smem_stage_off, smem_tables_off, smem_bar_off, smem_total;  // shared-memory layout (bytes)
     const int64_t *seeds;  // [n] per-sample seeds; null: sample s uses seed0 + s
     int64_t seed0;

@@ -52,7 +52,7 @@ enum State : int { Q_COMPILE = 0, Q_READY = 1, Q_RUNNING = 2, Q_DONE = 3, Q_FAIL
 // Offsets of one request's device block: compiled records, then the
 // accumulators (zeroed at upload), then the statistics.
 struct Layout {
-    size_t ev, pred, aux, dist, alias, wk, meta, earliest, ub, err, acc, hist, out, total;
+    size_t ev, pred, aux, tables, vals, wk, meta, earliest, ub, err, acc, hist, out, total;
 };
 
 Layout layout_of(const HostDag &h) {
@@ -66,8 +66,8 @@ Layout layout_of(const HostDag &h) {
     L.ev = take(h.ev.size() * sizeof(EvRec));
     L.pred = take(h.pred.size() * sizeof(PredRec));
     L.aux = take(h.aux.size() * sizeof(LinkRec));
-    L.dist = take(h.dist.size() * sizeof(DistParam));
-    L.alias = take(h.alias.size() * sizeof(AliasEntry));
+    L.tables = take(tables_bytes(h));
+    L.vals = take(h.vals.size() * sizeof(double));
     L.wk = take(h.wk_off.size() * 4);
     L.meta = take(h.stage_meta.size() * 4);
     L.earliest = take((size_t)h.E * 8);
@@ -164,8 +164,8 @@ void request_args(Request *r) {
     a.ev = reinterpret_cast<const EvRec *>(b + L.ev);
     a.pred = reinterpret_cast<const PredRec *>(b + L.pred);
     a.aux = reinterpret_cast<const LinkRec *>(b + L.aux);
-    a.dist = reinterpret_cast<const DistParam *>(b + L.dist);
-    a.alias = reinterpret_cast<const AliasEntry *>(b + L.alias);
+    a.dist = reinterpret_cast<const DistParam *>(b + L.tables);
+    a.vals = reinterpret_cast<const double *>(b + L.vals);
     a.wk_off = reinterpret_cast<const int32_t *>(b + L.wk);
     a.stage_meta = reinterpret_cast<const int32_t *>(b + L.meta);
     a.n_stages = h.n_stages;
@@ -178,7 +178,6 @@ void request_args(Request *r) {
     a.win_smem = h.win_smem ? 1 : 0;
     a.positive = h.positive ? 1 : 0;
     a.stage_bytes = h.stage_bytes;
-    a.stage_pred_off = h.stage_pred_off;
     a.smem_stage_off = h.smem_stage_off;
     a.smem_tables_off = h.smem_tables_off;
     a.smem_bar_off = h.smem_bar_off;
@@ -246,8 +245,11 @@ void upload_request(const mcd_server *S, Request *r, cudaStream_t st, Staging &s
     put(L.ev, h.ev.data(), h.ev.size() * sizeof(EvRec));
     put(L.pred, h.pred.data(), h.pred.size() * sizeof(PredRec));
     put(L.aux, h.aux.data(), h.aux.size() * sizeof(LinkRec));
-    put(L.dist, h.dist.data(), h.dist.size() * sizeof(DistParam));
-    put(L.alias, h.alias.data(), h.alias.size() * sizeof(AliasEntry));
+    {
+        const std::vector<unsigned char> tb = tables_block(h);
+        put(L.tables, tb.data(), tb.size());
+    }
+    put(L.vals, h.vals.data(), h.vals.size() * sizeof(double));
     put(L.wk, h.wk_off.data(), h.wk_off.size() * 4);
     put(L.meta, h.stage_meta.data(), h.stage_meta.size() * 4);
     put(L.earliest, h.earliest.data(), (size_t)h.E * 8);
@@ -340,6 +342,8 @@ void compile_loop(mcd_server *S) {
             drop(h.aux);
             drop(h.dist);
             drop(h.alias);
+            drop(h.picks);
+            drop(h.vals);
             drop(h.wk_off);
             drop(h.stage_meta);
             drop(h.link_kd);

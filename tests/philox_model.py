@@ -59,18 +59,22 @@ def _from_bits(b: int) -> float:
     return struct.unpack("<d", struct.pack("<q", b))[0]
 
 
-def one_plus(x) -> float:
-    """The kernel's double 1 + x for a float32 x >= 0."""
-    b = int(np.asarray(x, np.float32).view(np.uint32))
-    e = (b >> 23) & 0xFF
-    if e == 0:
-        return 1.0
-    if e < 127:
-        m = (b & 0x7FFFFF) | 0x800000
-        sh = e - 98
-        frac = (m << sh) if sh >= 0 else ((m >> -sh) if sh > -24 else 0)
-        return _from_bits(0x3FF0000000000000 | frac)
-    return float(np.float32(1.0) + np.float32(x))
+def scale_by(base: float, m) -> float:
+    """The kernel's base * m for a float32 m >= 1: the 53 leading bits of the exact
+    product, truncated (an FP64 multiply for zero, subnormal or non-finite bases)."""
+    b = struct.unpack("<Q", struct.pack("<d", float(base)))[0]
+    fm = int(np.asarray(m, np.float32).view(np.uint32))
+    eb = (b >> 52) & 0x7FF
+    e = eb + (fm >> 23) - 127
+    if eb == 0 or e >= 0x7FE or fm >= 0x7F800000:
+        return float(base) * float(np.float32(m))
+    mb = (b & ((1 << 52) - 1)) | (1 << 52)
+    mf = (fm & 0x7FFFFF) | 0x800000
+    q = (mb * mf) >> 23
+    top = q >> 53
+    q >>= top
+    bits = (b & (1 << 63)) + ((e + top - 1) << 52) + q
+    return _from_bits(bits - (1 << 64) if bits >= 1 << 63 else bits)
 
 
 def exponential_durations(seeds, link, base, lam, max_scale, block=None, word=0):
@@ -84,7 +88,7 @@ def exponential_durations(seeds, link, base, lam, max_scale, block=None, word=0)
     # the kernel takes the logarithm with the MUFU approximation (within 2^-21.4
     # absolute on [0.5, 2], 3 ulp elsewhere); this model takes the exact one
     X = np.maximum(np.minimum(-np.float32(lam) * np.log(V), np.float32(max_scale)), np.float32(0.0)).astype(np.float32)
-    return np.array([float(base) * one_plus(x) for x in X])  # one IEEE multiply, as the kernel
+    return np.array([scale_by(base, np.float32(1.0) + x) for x in X])  # base * (1 + X), 1 + X in float
 
 
 def alias_table(values, weights):

@@ -422,7 +422,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--samples", type=int, default=19456)
-    ap.add_argument("--e2e-samples", type=int, default=2432)
+    ap.add_argument("--e2e-samples", type=int, default=4864)
     ap.add_argument("--layers", type=int, default=2000)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--workload", default="single", choices=["single", "batched", "gradient", "serving"])

@@ -102,25 +102,45 @@ namespace {
 
 // Samples per chunk for the host-buffer entry points, a multiple of 32, and the
 // number of chunk buffer sets (sample-minor rows + sample-major rows): one when
-// all n samples fit one chunk, else two (alternating streams overlap one
-// chunk's launch with the other's transposes and copies).  A chunk is one
-// launch in which every 32-sample tile walks the whole DAG, so a launch of few
-// tiles leaves SMs idle: chunks are as large as a workspace of a quarter of the
-// device memory not otherwise in use (at most 32 GiB) allows.
+// all n samples fit one chunk, else two, used alternately by the handle's two
+// streams.  A chunk is one launch in which every 32-sample tile walks the whole
+// DAG at one CTA per SM, so a chunk of half a wave of tiles leaves the other
+// half of the SMs to the previous chunk's transposes and copies: the host
+// transfer, the bound of these entry points, overlaps the next chunk's sampling.
+// Chunks also stay within a workspace of a quarter of the device memory not
+// otherwise in use (at most 32 GiB).
 int64_t host_chunk(const mcd_dag *g, int64_t n, int *sets) {
     const double per_sample = 2.0 * (12.0 * g->h.E + 8.0 * g->h.L) + 8.0;
     size_t free_b = 0, total_b = 0;
     cuda_check(cudaMemGetInfo(&free_b, &total_b), "device memory query");
+    int sms = 0;
+    cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g->device), "device query");
+    const int64_t half_wave = (int64_t)kTile * std::max(1, sms / 2);
     const double budget =
         std::min(std::max((double)(free_b + g->ws_bytes) / 4.0, (double)(1ll << 30)), (double)(32ll << 30));
     const int64_t n32 = std::max<int64_t>(32, (n + 31) / 32 * 32);
-    if ((double)n32 * per_sample <= budget) {
+    if (n32 <= half_wave && (double)n32 * per_sample <= budget) {
         *sets = 1;
         return n32;
     }
     *sets = 2;
-    const int64_t c = (int64_t)(budget / (2.0 * std::max(per_sample, 1.0)));
+    const int64_t c = std::min<int64_t>(half_wave, (int64_t)(budget / (2.0 * std::max(per_sample, 1.0))));
     return std::max<int64_t>(32, c / 32 * 32);
+}
+
+// The device-side address of a host buffer a kernel may access directly
+// (pinned or registered memory, mapped under unified addressing), or null when
+// the buffer must be copied (pageable memory).  Writing outputs straight from
+// the transpose kernels saves the device staging copy and a copy-engine pass.
+template <typename T>
+T *device_view(T *host) {
+    if (!host) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? static_cast<T *>(at.devicePointer) : nullptr;
 }
 
 struct ChunkBufs {
@@ -411,6 +431,15 @@ int mcd_run_many_host(mcd_dag *g, const int64_t *seeds, int64_t n, double *reali
         const int64_t C = host_chunk(g, n, &sets);
         ChunkBufs cb[2];
         carve(g, C, sets, cb);
+        double *real_dv = device_view(realized), *dur_dv = device_view(durations);
+        int32_t *cause_dv = device_view(cause);
+        // chunk k waits for chunk k - 2 (same buffers, same stream); the two streams
+        // start together, after work already queued on the handle's first stream
+        cudaEvent_t start;
+        cuda_check(cudaEventCreateWithFlags(&start, cudaEventDisableTiming), "event create");
+        cuda_check(cudaEventRecord(start, g->stream[0]), "event record");
+        cuda_check(cudaStreamWaitEvent(g->stream[1], start, 0), "stream wait");
+        cudaEventDestroy(start);
         int64_t idx = 0;
         for (int64_t off = 0; off < n; off += C, ++idx) {
             const int k = (int)(idx & 1);
@@ -426,19 +455,25 @@ int mcd_run_many_host(mcd_dag *g, const int64_t *seeds, int64_t n, double *reali
             a.durations = durations ? cb[k].dur_minor : nullptr;
             a.cause = cause ? cb[k].cause_minor : nullptr;
             cuda_check(launch_propagate(a, false, g->h.win_smem, false, st), "propagate launch");
-            if (realized) {
+            if (real_dv) {
+                cuda_check(launch_transpose_f64(cb[k].real_minor, C, real_dv + off * E, E, E, m, st), "transpose");
+            } else if (realized) {
                 cuda_check(launch_transpose_f64(cb[k].real_minor, C, cb[k].real_major, E, E, m, st), "transpose");
                 cuda_check(cudaMemcpyAsync(realized + off * E, cb[k].real_major, (size_t)(m * E) * 8,
                                            cudaMemcpyDeviceToHost, st),
                            "realized download");
             }
-            if (durations) {
+            if (dur_dv) {
+                cuda_check(launch_transpose_f64(cb[k].dur_minor, C, dur_dv + off * L, L, L, m, st), "transpose");
+            } else if (durations) {
                 cuda_check(launch_transpose_f64(cb[k].dur_minor, C, cb[k].dur_major, L, L, m, st), "transpose");
                 cuda_check(cudaMemcpyAsync(durations + off * L, cb[k].dur_major, (size_t)(m * L) * 8,
                                            cudaMemcpyDeviceToHost, st),
                            "durations download");
             }
-            if (cause) {
+            if (cause_dv) {
+                cuda_check(launch_transpose_i32(cb[k].cause_minor, C, cause_dv + off * E, E, E, m, st), "transpose");
+            } else if (cause) {
                 cuda_check(launch_transpose_i32(cb[k].cause_minor, C, cb[k].cause_major, E, E, m, st),
                            "transpose");
                 cuda_check(cudaMemcpyAsync(cause + off * E, cb[k].cause_major, (size_t)(m * E) * 4,
@@ -462,12 +497,22 @@ int mcd_propagate_host(mcd_dag *g, const double *durations, int64_t n, double *r
         const int64_t C = host_chunk(g, n, &sets);
         ChunkBufs cb[2];
         carve(g, C, sets, cb);
+        const double *dur_dv = device_view(durations);
+        double *real_dv = device_view(realized);
+        int32_t *cause_dv = device_view(cause);
+        cudaEvent_t start;
+        cuda_check(cudaEventCreateWithFlags(&start, cudaEventDisableTiming), "event create");
+        cuda_check(cudaEventRecord(start, g->stream[0]), "event record");
+        cuda_check(cudaStreamWaitEvent(g->stream[1], start, 0), "stream wait");
+        cudaEventDestroy(start);
         int64_t idx = 0;
         for (int64_t off = 0; off < n; off += C, ++idx) {
             const int k = (int)(idx & 1);
             cudaStream_t st = g->stream[k];
             const int64_t m = std::min(C, n - off);
-            if (L > 0) {
+            if (L > 0 && dur_dv) {
+                cuda_check(launch_transpose_f64(dur_dv + off * L, L, cb[k].dur_minor, C, m, L, st), "transpose");
+            } else if (L > 0) {
                 cuda_check(cudaMemcpyAsync(cb[k].dur_major, durations + off * L, (size_t)(m * L) * 8,
                                            cudaMemcpyHostToDevice, st),
                            "durations upload");
@@ -481,13 +526,17 @@ int mcd_propagate_host(mcd_dag *g, const double *durations, int64_t n, double *r
             a.dur_in = cb[k].dur_minor;
             a.ld_in = C;
             cuda_check(launch_propagate(a, true, g->h.win_smem, false, st), "propagate launch");
-            if (realized) {
+            if (real_dv) {
+                cuda_check(launch_transpose_f64(cb[k].real_minor, C, real_dv + off * E, E, E, m, st), "transpose");
+            } else if (realized) {
                 cuda_check(launch_transpose_f64(cb[k].real_minor, C, cb[k].real_major, E, E, m, st), "transpose");
                 cuda_check(cudaMemcpyAsync(realized + off * E, cb[k].real_major, (size_t)(m * E) * 8,
                                            cudaMemcpyDeviceToHost, st),
                            "realized download");
             }
-            if (cause) {
+            if (cause_dv) {
+                cuda_check(launch_transpose_i32(cb[k].cause_minor, C, cause_dv + off * E, E, E, m, st), "transpose");
+            } else if (cause) {
                 cuda_check(launch_transpose_i32(cb[k].cause_minor, C, cb[k].cause_major, E, E, m, st),
                            "transpose");
                 cuda_check(cudaMemcpyAsync(cause + off * E, cb[k].cause_major, (size_t)(m * E) * 4,

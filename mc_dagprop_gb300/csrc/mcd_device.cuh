@@ -89,41 +89,24 @@ __device__ __forceinline__ long long order_key(long long b) {
     return mag > 0x7FF0000000000000ll ? (long long)0x8000000000000000ull : k;
 }
 
-// ---------------------------------------------------------------- integer FP64 helpers
-// 32 x 32 -> 64-bit unsigned product (one wide integer multiply).
-__device__ __forceinline__ unsigned long long mul_wide(uint32_t a, uint32_t b) {
-    unsigned long long r;
-    asm("mul.wide.u32 %0, %1, %2;" : "=l"(r) : "r"(a), "r"(b));
-    return r;
+// ---------------------------------------------------------------- duration scaling
+// The double equal to a float m >= 1, built with integer operations: a
+// float-to-double conversion would occupy the FP64 pipe, which on this part
+// issues about 1.6 lane-operations per clock per SM.  An infinite m stays
+// infinite.
+__device__ __forceinline__ double widen(float m) {
+    const uint32_t b = __float_as_uint(m);
+    uint32_t hi = (((b >> 23) + 896u) << 20) | ((b >> 3) & 0x000FFFFFu);
+    uint32_t lo = b << 29;
+    if (b >= 0x7F800000u) {
+        hi = 0x7FF00000u;
+        lo = 0u;
+    }
+    return __hiloint2double((int)hi, (int)lo);
 }
 
-// The rare cases of scale_by, out of line so that the compiler branches around
-// them instead of predicating a conversion and a multiply on the FP64 pipe.
-static __device__ __noinline__ double scale_by_fp64(double base, float m) { return __dmul_rn(base, (double)m); }
-
-// base * m for a double base and a float m >= 1: the 53 leading bits of the
-// exact product (truncated), from two 32 x 32-bit integer products -- the FP64
-// pipe of this part issues about 1.6 lane-operations per clock per SM, so a
-// sampled duration spends none of it.  Zero, subnormal and non-finite bases,
-// an infinite m, and products within a factor of two of overflow take one FP64
-// multiply instead.
-__device__ __forceinline__ double scale_by(double base, float m) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(base);
-    const uint32_t bh = (uint32_t)(b >> 32);
-    const uint32_t eb = (bh >> 20) & 0x7FFu;
-    const uint32_t fm = __float_as_uint(m);
-    const uint32_t e = eb + (fm >> 23) - 127u;  // m >= 1: sign 0, exponent field >= 127
-    if (eb == 0u || e >= 0x7FEu || fm >= 0x7F800000u) return scale_by_fp64(base, m);  // a branch, not predicated
-    const uint32_t mf = (fm & 0x7FFFFFu) | 0x800000u;                  // 24 bits
-    const unsigned long long hi = mul_wide((bh & 0xFFFFFu) | 0x100000u, mf);  // < 2^45
-    const unsigned long long lo = mul_wide((uint32_t)b, mf);                  // < 2^56
-    // floor(P / 2^23) of the 77-bit mantissa product P = (hi << 32) + lo in [2^75, 2^77)
-    unsigned long long q = (hi << 9) + (lo >> 23);
-    const uint32_t top = (uint32_t)(q >> 53);  // P >= 2^76: one more exponent step
-    q >>= top;                                 // [2^52, 2^53): the hidden bit carries into the exponent
-    return __longlong_as_double(
-        (long long)((b & 0x8000000000000000ull) + ((unsigned long long)(e + top - 1u) << 52) + q));
-}
+// A sampled duration base * (1 + X), 1 + X rounded to float: one FP64 multiply.
+__device__ __forceinline__ double scale_by(double base, float m) { return __dmul_rn(base, widen(m)); }
 
 // ---------------------------------------------------------------- samplers
 // Each returns the link's duration (base + extra) for one sample.

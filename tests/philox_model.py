@@ -60,21 +60,9 @@ def _from_bits(b: int) -> float:
 
 
 def scale_by(base: float, m) -> float:
-    """The kernel's base * m for a float32 m >= 1: the 53 leading bits of the exact
-    product, truncated (an FP64 multiply for zero, subnormal or non-finite bases)."""
-    b = struct.unpack("<Q", struct.pack("<d", float(base)))[0]
-    fm = int(np.asarray(m, np.float32).view(np.uint32))
-    eb = (b >> 52) & 0x7FF
-    e = eb + (fm >> 23) - 127
-    if eb == 0 or e >= 0x7FE or fm >= 0x7F800000:
-        return float(base) * float(np.float32(m))
-    mb = (b & ((1 << 52) - 1)) | (1 << 52)
-    mf = (fm & 0x7FFFFF) | 0x800000
-    q = (mb * mf) >> 23
-    top = q >> 53
-    q >>= top
-    bits = (b & (1 << 63)) + ((e + top - 1) << 52) + q
-    return _from_bits(bits - (1 << 64) if bits >= 1 << 63 else bits)
+    """The kernel's base * m for a float32 m >= 1: one IEEE double multiply by the
+    double equal to m."""
+    return float(base) * float(np.float32(m))
 
 
 def exponential_durations(seeds, link, base, lam, max_scale, block=None, word=0):

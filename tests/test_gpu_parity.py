@@ -15,7 +15,8 @@ import pytest
 import mc_dagprop_gb300 as m
 import oracle
 from mc_dagprop_gb300 import workloads as W
-from mcd_testlib import MCD_OK, flat_from_lists, last_error, lib, load_golden, propagator_from_flat, six_event_flat
+from mcd_testlib import (MCD_OK, flat_from_lists, last_error, lib, load_golden, propagator_from_flat, ptr,
+                         six_event_flat)
 
 pytestmark = pytest.mark.gpu
 
@@ -204,3 +205,47 @@ def test_large_sample_counts_chunk_correctly(cuda):
     r2, _, c2 = prop.run_many_arrays(seeds[1000:], durations=False)
     assert_bits_equal(real[1000:], r2)
     assert np.array_equal(cause[1000:], c2)
+
+
+def _pinned(nbytes):
+    p = C.c_void_p()
+    assert lib().mcd_host_alloc(nbytes, C.byref(p)) == MCD_OK, last_error()
+    return p
+
+
+def test_host_paths_pinned_and_pageable_agree(cuda):
+    """The host-buffer entry points over several chunks: pinned buffers (written and
+    read by the transpose kernels directly) and pageable buffers (staged copies)
+    give the same bits, and a sample's result does not depend on its chunk."""
+    flat, gen = W.config1(seed=5, n_layers=20, width=50)
+    prop = propagator_from_flat(m, flat, gen)
+    h = C.c_void_p(prop._handle())
+    E, L = prop.node_count(), prop.activity_count()
+    n = 32 * 152 + 1000  # more than two half-wave chunks on a 152-SM part
+    seeds = np.arange(7, 7 + n, dtype=np.int64)
+    real = np.empty((n, E)); dur = np.empty((n, L)); cause = np.empty((n, E), np.int32)
+    assert lib().mcd_run_many_host(h, ptr(seeds), n, ptr(real), ptr(dur), ptr(cause)) == MCD_OK, last_error()
+    bufs = [_pinned(n * 8), _pinned(n * E * 8), _pinned(n * L * 8), _pinned(n * E * 4)]
+    try:
+        ps = np.ctypeslib.as_array(C.cast(bufs[0], C.POINTER(C.c_int64)), (n,))
+        pr = np.ctypeslib.as_array(C.cast(bufs[1], C.POINTER(C.c_double)), (n, E))
+        pd = np.ctypeslib.as_array(C.cast(bufs[2], C.POINTER(C.c_double)), (n, L))
+        pc = np.ctypeslib.as_array(C.cast(bufs[3], C.POINTER(C.c_int32)), (n, E))
+        ps[:] = seeds
+        pr.fill(-1.0); pd.fill(-1.0); pc.fill(-9)
+        assert lib().mcd_run_many_host(h, bufs[0], n, bufs[1], bufs[2], bufs[3]) == MCD_OK, last_error()
+        assert_bits_equal(pr, real)
+        assert_bits_equal(pd, dur)
+        assert np.array_equal(pc, cause)
+        # propagation of the pinned durations, written into pinned outputs
+        pr.fill(-1.0); pc.fill(-9)
+        assert lib().mcd_propagate_host(h, bufs[2], n, bufs[1], bufs[3]) == MCD_OK, last_error()
+        assert_bits_equal(pr, real)
+        assert np.array_equal(pc, cause)
+    finally:
+        for b in bufs:
+            lib().mcd_host_free(b)
+    r2, d2, c2 = prop.run_many_arrays(seeds[-700:])
+    assert_bits_equal(r2, real[-700:])
+    assert_bits_equal(d2, dur[-700:])
+    assert np.array_equal(c2, cause[-700:])

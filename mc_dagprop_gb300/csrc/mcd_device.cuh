@@ -385,6 +385,110 @@ __device__ __forceinline__ void accumulate_sum(const KArgs &a, const EvRec &ev, 
     if ((threadIdx.x & 31) == 0 && d != 0) atomicAdd(&a.acc[ev.user], (unsigned long long)d);
 }
 
+// ---------------------------------------------------------------- stage bodies
+// A tile's per-lane state: its sample, seed, and output columns.
+struct TileCtx {
+    int lane;
+    int64_t s;                 // the lane's sample
+    bool active;               // s < n
+    unsigned active_mask;
+    uint64_t seed;
+    double *rows;              // global realized rows (window off chip, or output), or null
+    int64_t rows_ld, rcol;
+    double *dcol;              // durations output column of this lane (null: none, or inactive)
+    int32_t *ccol;             // cause_event output column of this lane (null: none, or inactive)
+    int64_t ld;                // leading dimension of the outputs
+};
+
+// Lane 0 takes the next event index of a stage from its shared-memory counter.
+// (Inline PTX: a plain atomicAdd under a lane test is compiled into a
+// warp-aggregated atomic, several instructions per event for one active lane.)
+__device__ __forceinline__ int take_next(uint32_t ctr) {
+    int v;
+    asm volatile("atom.shared.add.u32 %0, [%1], 1;" : "=r"(v) : "r"(ctr) : "memory");
+    return v;
+}
+
+// One stage's events, taken one at a time from the stage's counter (the
+// compiler orders them costliest first).  STAGED: sev/spred point into the
+// staging buffer in shared memory; otherwise into global memory.  pred0: the
+// stage's first predecessor record (the records' pred_begin/pred_end are
+// global indices).
+template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ, bool STAGED>
+__device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec *sev, const PredRec *spred, int pred0,
+                                             int n_ev, uint32_t ctr, const TileCtx &t, const DistParam *dists,
+                                             unsigned char *smem, U4 &grp) {
+    double *win = reinterpret_cast<double *>(smem);
+    const int lane = t.lane;
+    // the next index is taken before this event's work, hiding the atomic's
+    // latency (a warp holds at most one extra event: the cheapest, by order)
+    int i_next = 0;
+    if (lane == 0) i_next = take_next(ctr);
+    i_next = __shfl_sync(0xFFFFFFFFu, i_next, 0);
+    while (i_next < n_ev) {
+        const int i = i_next;
+        if (lane == 0) i_next = take_next(ctr);
+        const EvRec ev = load_ev(sev + i);
+        // POSITIVE: keys are the bits themselves (init_key == init_bits, ub_key == ub_bits),
+        // so one 64-bit value carries both
+        long long lk = POSITIVE ? ev.init_bits : ev.init_key, lbits = ev.init_bits;
+        const long long ub_key = POSITIVE ? ev.ub_bits : ev.ub_key;
+        int32_t cause = -1;
+        uint32_t win_code = kAdjNone;  // ADJ: winner position | clamp flag
+        float win_dfac = 0.0f;
+        const int pb = ev.pred_begin - pred0, pe = ev.pred_end - pred0;
+        for (int p = pb; p < pe; ++p) {
+            const PredRec pr = load_pred(spred + p);
+            double dur;
+            float dfac = 0.0f;
+            if (GIVEN) {
+                dur = (t.active && pr.link >= 0) ? __ldg(&a.dur_in[(int64_t)pr.link * a.ld_in + t.s]) : 0.0;
+            } else {
+                dur = link_duration(a, pr.kd, pr.v, pr.dvo, (uint32_t)pr.block, t.seed, grp, dists, smem, l, dfac);
+                if (!STATS && !ADJ && (pr.kd & KD_WRITE) && t.dcol) t.dcol[(int64_t)pr.link * t.ld] = dur;
+            }
+            // with the window on chip every source has a slot (the compiler checks it)
+            const double src = WIN_SMEM ? win[pr.src_slot * kTile + lane]
+                                        : (t.active ? t.rows[(int64_t)pr.src_user * t.rows_ld + t.rcol] : 0.0);
+            const double tt = src + dur;  // the one FP64 add of the edge (_core.cpp:341)
+            long long tb = __double_as_longlong(tt);
+            long long tk = order_key<POSITIVE>(tb);
+            const bool clamp = ub_key < tk;
+            if (clamp) {  // t = std::min(t, ub)
+                tk = ub_key;
+                tb = ev.ub_bits;
+            }
+            if (tk >= lk) {  // if (t >= latest) { latest = t; cause = src; }
+                lk = tk;
+                lbits = POSITIVE ? tk : tb;
+                cause = pr.src_user;
+                if (ADJ) {
+                    win_code = (uint32_t)(p - pb) | (clamp ? kAdjClamped : 0u);
+                    win_dfac = dfac;
+                }
+            }
+        }
+        // realized = std::min(latest, ub): latest only exceeds ub when earliest does, which
+        // non-negative max_delay rules out in POSITIVE mode
+        if (!POSITIVE && ub_key < lk) lbits = ev.ub_bits;
+        const double real = __longlong_as_double(lbits);
+        if (WIN_SMEM && ev.slot >= 0) win[ev.slot * kTile + lane] = real;
+        if (STATS) accumulate_stats(a, ev, lbits, t.active, t.active_mask);
+        if (ADJ) {
+            const bool delayed = lk > (POSITIVE ? ev.init_bits : ev.init_key);  // realized > earliest
+            accumulate_sum(a, ev, lbits, t.active);
+            if (t.active) {
+                const int64_t o = (int64_t)ev.user * a.ld + t.s;
+                a.adj_code[o] = (uint16_t)(win_code | (delayed ? kAdjDelayed : 0u));
+                a.adj_dfac[o] = win_dfac;
+            }
+        }
+        if (t.active && t.rows) t.rows[(int64_t)ev.user * t.rows_ld + t.rcol] = real;
+        if (!STATS && !ADJ && t.ccol) t.ccol[(int64_t)ev.user * t.ld] = cause;
+        i_next = __shfl_sync(0xFFFFFFFFu, i_next, 0);
+    }
+}
+
 // ---------------------------------------------------------------- propagation
 // Walks the compiled DAG for one tile of 32 samples (the tile's sample s is
 // tile * 32 + lane) with all warps of the CTA.
@@ -400,14 +504,10 @@ __device__ __forceinline__ void accumulate_sum(const KArgs &a, const EvRec &ev, 
 // Shared memory: [window: window_slots x 32 doubles][stage buffer 0][stage
 // buffer 1][distribution params][alias entries][alias picks][2 mbarriers, 2
 // stage counters]; a stage buffer holds [event records][predecessor
-// records][value region];
-// `bars` is that layout's barrier region (kBarRegionBytes), or one fixed region
-// for every tile of a persistent CTA (a barrier stays where it was
-// initialised: only the same address is invalidated and initialised again
-// between tiles).
-// Warps take a stage's events one at a time from the stage's counter (the
-// compiler orders them costliest first), so a stage ends when its last event
-// does, not when the unluckiest static chunk does.
+// records][value region]; `bars` is that layout's barrier region
+// (kBarRegionBytes), or one fixed region for every tile of a persistent CTA (a
+// barrier stays where it was initialised: only the same address is invalidated
+// and initialised again between tiles).
 // ADJ: the forward half of the adjoint: per event and sample, the winning
 // predecessor's position, clamp and delay flags and d(duration)/d(base) go to
 // a.adj_code / a.adj_dfac, and (realized - earliest) to the objective sum.
@@ -415,20 +515,24 @@ template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ = false
 __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, double *rows, int64_t rows_ld,
                                                bool rows_tile_local, unsigned char *smem, uint64_t *bars,
                                                bool reuse) {
-    double *win = reinterpret_cast<double *>(smem);
-    char *stage_buf0 = reinterpret_cast<char *>(smem + a.smem_stage_off);
     DistParam *s_dist = reinterpret_cast<DistParam *>(smem + a.smem_tables_off);
     const DistParam *dists = a.tables_in_smem ? s_dist : a.dist;
 
-    const int lane = threadIdx.x & 31;
+    TileCtx t;
+    t.lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int NW = a.n_warps;
-    const int64_t s = tile * kTile + lane;
-    const int64_t rcol = rows_tile_local ? (int64_t)lane : s;
-    const bool active = s < a.n;
-    const unsigned active_mask = __ballot_sync(0xFFFFFFFFu, active);
-    uint64_t seed = 0;
-    if (!GIVEN && active) seed = a.seeds ? (uint64_t)a.seeds[s] : (uint64_t)(a.seed0 + s);
+    t.s = tile * kTile + t.lane;
+    t.active = t.s < a.n;
+    t.active_mask = __ballot_sync(0xFFFFFFFFu, t.active);
+    t.seed = 0;
+    if (!GIVEN && t.active) t.seed = a.seeds ? (uint64_t)a.seeds[t.s] : (uint64_t)(a.seed0 + t.s);
+    t.rows = rows;
+    t.rows_ld = rows_ld;
+    t.rcol = rows_tile_local ? (int64_t)t.lane : t.s;
+    t.ld = a.ld;
+    t.dcol = (!STATS && !ADJ && !GIVEN && a.durations && t.active) ? a.durations + t.s : nullptr;
+    t.ccol = (!STATS && !ADJ && a.cause && t.active) ? a.cause + t.s : nullptr;
 
     // distribution tables into shared memory; fresh barriers for this tile
     if (a.tables_in_smem) {  // the tables block, 8 bytes at a time (its size is a multiple of 8)
@@ -454,6 +558,7 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
     // proxy) land, so every thread orders its stores before the copies.
     if (reuse) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
+    char *stage_buf0 = reinterpret_cast<char *>(smem + a.smem_stage_off);
     if (threadIdx.x == 0) {
         if (a.n_stages > 0) stage_issue(a, 0, stage_buf0, &bars[0]);
         if (a.n_stages > 1) stage_issue(a, 1, stage_buf0 + a.stage_bytes, &bars[1]);
@@ -461,7 +566,6 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
 
     for (int l = 0; l < a.n_stages; ++l) {
         const int b = l & 1;
-        const char *buf = stage_buf0 + b * a.stage_bytes;
         const bool ok = stage_wait(&bars[b], (uint32_t)((l >> 1) & 1), a.err);
         if (__syncthreads_or(!ok)) {  // a copy that never landed: drain, then leave together
             if (threadIdx.x == 0 && l + 1 < a.n_stages)
@@ -471,78 +575,16 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
         }
         const int4 meta = __ldg(reinterpret_cast<const int4 *>(a.stage_meta) + 2 * l);
         const int4 mv = __ldg(reinterpret_cast<const int4 *>(a.stage_meta) + 2 * l + 1);
-        // a stage whose records exceed the buffer is read from global memory
-        const EvRec *sev = meta.y >= 0 ? reinterpret_cast<const EvRec *>(buf) : a.ev + meta.x;
-        const PredRec *spred = meta.y >= 0 ? reinterpret_cast<const PredRec *>(buf + mv.z) : a.pred + meta.z;
-        const int n_ev = meta.y >= 0 ? meta.y : -meta.y;
         if (threadIdx.x == 0) stage_ctr[(l + 1) & 1] = 0;  // last used by stage l - 1, before the barrier
-        // the next index is taken before this event's work, hiding the atomic's
-        // latency (a warp holds at most one extra event: the cheapest, by order)
-        int i_next = 0;
-        if (lane == 0) i_next = atomicAdd(&stage_ctr[l & 1], 1);
-        i_next = __shfl_sync(0xFFFFFFFFu, i_next, 0);
-        while (i_next < n_ev) {
-            const int i = i_next;
-            if (lane == 0) i_next = atomicAdd(&stage_ctr[l & 1], 1);
-            i_next = __shfl_sync(0xFFFFFFFFu, i_next, 0);
-            const EvRec ev = load_ev(sev + i);
-            long long lk = ev.init_key, lbits = ev.init_bits;
-            int32_t cause = -1;
-            uint32_t win_code = kAdjNone;  // ADJ: winner position | clamp flag
-            float win_dfac = 0.0f;
-            for (int p = ev.pred_begin - meta.z; p < ev.pred_end - meta.z; ++p) {
-                const PredRec pr = load_pred(spred + p);
-                double dur;
-                float dfac = 0.0f;
-                if (GIVEN) {
-                    dur = (active && pr.link >= 0) ? __ldg(&a.dur_in[(int64_t)pr.link * a.ld_in + s]) : 0.0;
-                } else {
-                    dur = link_duration(a, pr.kd, pr.v, pr.dvo, (uint32_t)pr.block, seed, grp, dists, smem, l,
-                                        dfac);
-                    if (!STATS && !ADJ && (pr.kd & KD_WRITE) && a.durations && active)
-                        a.durations[(int64_t)pr.link * a.ld + s] = dur;
-                }
-                double src;
-                if (WIN_SMEM && pr.src_slot >= 0) {
-                    src = win[pr.src_slot * kTile + lane];
-                } else {
-                    src = active ? rows[(int64_t)pr.src_user * rows_ld + rcol] : 0.0;
-                }
-                const double t = src + dur;  // the one FP64 add of the edge (_core.cpp:341)
-                long long tb = __double_as_longlong(t);
-                long long tk = order_key<POSITIVE>(tb);
-                const bool clamp = ev.ub_key < tk;
-                if (clamp) {  // t = std::min(t, ub)
-                    tk = ev.ub_key;
-                    tb = ev.ub_bits;
-                }
-                if (tk >= lk) {  // if (t >= latest) { latest = t; cause = src; }
-                    lk = tk;
-                    lbits = tb;
-                    cause = pr.src_user;
-                    if (ADJ) {
-                        win_code = (uint32_t)(p - (ev.pred_begin - meta.z)) | (clamp ? kAdjClamped : 0u);
-                        win_dfac = dfac;
-                    }
-                }
-            }
-            if (ev.ub_key < lk) lbits = ev.ub_bits;  // realized = std::min(latest, ub)
-            const double real = __longlong_as_double(lbits);
-            if (WIN_SMEM && ev.slot >= 0) win[ev.slot * kTile + lane] = real;
-            if (STATS) accumulate_stats(a, ev, lbits, active, active_mask);
-            if (ADJ) {
-                const bool delayed = lk > ev.init_key;  // realized > earliest
-                accumulate_sum(a, ev, lbits, active);
-                if (active) {
-                    const int64_t o = (int64_t)ev.user * a.ld + s;
-                    a.adj_code[o] = (uint16_t)(win_code | (delayed ? kAdjDelayed : 0u));
-                    a.adj_dfac[o] = win_dfac;
-                }
-            }
-            if (active) {
-                if (rows) rows[(int64_t)ev.user * rows_ld + rcol] = real;
-                if (!STATS && !ADJ && a.cause) a.cause[(int64_t)ev.user * a.ld + s] = cause;
-            }
+        const uint32_t ctr = smem_u32(&stage_ctr[l & 1]);
+        if (meta.y >= 0) {  // records in the staging buffer (shared memory)
+            const unsigned char *buf = smem + a.smem_stage_off + b * a.stage_bytes;
+            stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, true>(
+                a, l, reinterpret_cast<const EvRec *>(buf), reinterpret_cast<const PredRec *>(buf + mv.z), meta.z,
+                meta.y, ctr, t, dists, smem, grp);
+        } else {  // a stage whose records exceed the buffer is read from global memory
+            stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, false>(a, l, a.ev + meta.x, a.pred + meta.z, meta.z,
+                                                                       -meta.y, ctr, t, dists, smem, grp);
         }
         __syncthreads();
         if (threadIdx.x == 0 && l + 2 < a.n_stages)
@@ -554,8 +596,9 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
             const LinkRec lr = a.aux[i];
             float dfac;
             U4 own;  // an unreferenced link owns its block
-            const double dur = link_duration(a, lr.kd, lr.v, -1, (uint32_t)lr.link, seed, own, dists, smem, 0, dfac);
-            if (active) a.durations[(int64_t)lr.link * a.ld + s] = dur;
+            const double dur =
+                link_duration(a, lr.kd, lr.v, -1, (uint32_t)lr.link, t.seed, own, dists, smem, 0, dfac);
+            if (t.dcol) t.dcol[(int64_t)lr.link * t.ld] = dur;
         }
     }
     return true;

@@ -136,10 +136,12 @@ int32_t mcd_dag_activity_count(const mcd_dag *dag);
 int mcd_dag_get_info(const mcd_dag *dag, mcd_dag_info *info);
 /* Random-number streams of the links ([activity_count] each): a sampled link's
  * draws come from Philox4x32-10 block block[l] (counter: sample seed, block,
- * attempt); word[l] in 0..3 is the one 32-bit word an exponential or small
- * empirical link takes from it (up to four such links first referenced by one
- * event share a block), -1 when the link uses the whole block (gamma, large
- * empirical tables).  block[l] = -1 for links of fixed duration. */
+ * attempt); word[l] in 0..3 is the first 32-bit word the link takes from it --
+ * one word for exponential and small empirical links, 1-3 words for gamma of
+ * shape 1-3, links first referenced by one event sharing blocks of four words --
+ * and -1 when the link uses the whole block (other gamma shapes, large empirical
+ * tables).  Gamma redraws above max_scale use blocks keyed by the link and the
+ * attempt.  block[l] = -1 for links of fixed duration. */
 int mcd_dag_link_streams(const mcd_dag *dag, int32_t *block, int32_t *word);
 /* The handle's stream (a cudaStream_t), for callers that order their own work on it. */
 void *mcd_dag_stream(const mcd_dag *dag);

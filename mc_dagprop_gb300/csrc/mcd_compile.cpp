@@ -644,11 +644,17 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
     H.pred.clear();
     H.pred.reserve((size_t)(d.n_targets > 0 ? d.pred_offsets[d.n_targets] : 0));
     std::vector<char> referenced((size_t)L, 0), written((size_t)L, 0);
-    // Philox blocks (see KD_REUSE): one-word links group per event, the rest own one
+    // Philox blocks (see KD_REUSE): links drawing from a shared block group per
+    // event, up to four words a block; the rest own one
     auto one_word = [&](int32_t l) {
         const int kind = H.link_kd[l] & KD_KIND_MASK;
         return kind == K_EXP || ((kind == K_EMP_ABS || kind == K_EMP_REL) &&
                                  H.dist[(size_t)(H.link_kd[l] >> 8)].tab_n <= kOneWordBins);
+    };
+    auto link_words = [&](int32_t l) -> int32_t {  // words of a shared block the link's first draw takes
+        if (one_word(l)) return 1;
+        if ((H.link_kd[l] & KD_KIND_MASK) == K_GAMMA) return H.dist[(size_t)(H.link_kd[l] >> 8)].erlang;
+        return 0;
     };
     H.link_block.assign((size_t)L, -1);
     H.link_word.assign((size_t)L, -1);
@@ -717,21 +723,24 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
                 p.dvo = float_bits(H.link_dv[l]);
                 p.block = -1;
                 if ((H.link_kd[l] & KD_KIND_MASK) != K_FIXED) {
-                    if (H.link_block[l] < 0) {  // first reference: the link's block and word
-                        if (one_word(l)) {
-                            if (group < 0 || group_n == 4) {
+                    const int32_t nw = link_words(l);
+                    if (H.link_block[l] < 0) {  // first reference: the link's block and first word
+                        if (nw > 0) {
+                            if (group < 0 || group_n + nw > 4) {
                                 group = l;
                                 group_n = 0;
                             }
                             H.link_block[l] = group;
-                            H.link_word[l] = (int8_t)group_n++;
+                            H.link_word[l] = (int8_t)group_n;
+                            group_n += nw;
                         } else {
                             H.link_block[l] = l;
                         }
                     }
                     p.block = H.link_block[l];
-                    if ((H.link_kd[l] & KD_KIND_MASK) != K_GAMMA) {  // draws into the shared registers
-                        if (one_word(l)) p.kd |= (int32_t)H.link_word[l] << KD_WORD_SHIFT;
+                    const bool mt_gamma = (H.link_kd[l] & KD_KIND_MASK) == K_GAMMA && nw == 0;
+                    if (!mt_gamma) {  // draws into the shared registers
+                        if (nw > 0) p.kd |= (int32_t)H.link_word[l] << KD_WORD_SHIFT;
                         else p.kd |= KD_TWO_WORD;
                         if (p.block == last_block) p.kd |= KD_REUSE;
                         last_block = p.block;
@@ -783,7 +792,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         int32_t kd = H.link_kd[l];
         if ((kd & KD_KIND_MASK) != K_FIXED) {
             H.link_block[l] = l;
-            if (one_word(l)) H.link_word[l] = 0;
+            if (link_words(l) > 0) H.link_word[l] = 0;
             else if ((kd & KD_KIND_MASK) != K_GAMMA) kd |= KD_TWO_WORD;
         }
         H.aux.push_back(LinkRec{l, kd, H.link_v[l]});

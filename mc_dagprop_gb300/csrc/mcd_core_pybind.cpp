@@ -714,7 +714,7 @@ PYBIND11_MODULE(_core, m) {
              "dict of objective, grad_earliest (per event), grad_base (per link index)")
         .def("info", &Propagator::info, "Compiled-DAG facts")
         .def("link_streams", &Propagator::link_streams,
-             "(block, word) per link: the Philox block of its draws and its word (-1: whole block)")
+             "(block, word) per link: the Philox block of its draws and its first word (-1: whole block)")
         .def("_handle", [](const Propagator &p) { return (uintptr_t)p.handle(); });
 
     py::class_<Batch>(m, "Batch")

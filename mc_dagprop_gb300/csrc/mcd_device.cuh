@@ -124,57 +124,70 @@ __device__ __forceinline__ double draw_exponential(const DistParam &p, double ba
     return scale_by(base, dfac);
 }
 
+__device__ __forceinline__ uint32_t word_of(const U4 &g, int i) {
+    return i == 0 ? g.x : i == 1 ? g.y : i == 2 ? g.z : g.w;
+}
+
 // Gamma(shape, scale) redrawn above max_scale (_core.cpp:98-104).  Shapes 1, 2
-// and 3 are sums of that many exponentials (Erlang): X = -scale * log(U1 U2 U3),
-// one Philox block per attempt.  Other shapes by Marsaglia & Tsang (ACM TOMS
-// 26(3), 2000) in FP32, normals from Box-Muller; shapes below 1 draw
-// Gamma(shape+1) times U^(1/shape).  Rejection loops are capped; a lane that
-// hits the cap latches ERR_GAMMA_REJECTION and returns the truncation point.
-// Inlined: the out-of-line call measured 2.5 % slower on the five-kind workload
-// (the call convention costs the loop more than the sampler's temporaries).
+// and 3 are sums of that many exponentials (Erlang): X = -scale * log(U1 U2 U3).
+// The first attempt takes its uniforms from words w.. of the block the event's
+// links share (grp); redraws use blocks of the link's own, keyed by the attempt.
+// Rejection loops are capped; a lane that hits the cap latches
+// ERR_GAMMA_REJECTION and returns the truncation point.
+static __device__ __forceinline__ double draw_erlang(const DistParam &p, double base, uint32_t link, uint64_t seed,
+                                                  const U4 &grp, int w, int32_t *err, float *dfac) {
+    float prod = u01_open0(word_of(grp, w));
+    if (p.erlang > 1) prod *= u01_open0(word_of(grp, w + 1));
+    if (p.erlang > 2) prod *= u01_open0(word_of(grp, w + 2));
+    float X = fmaxf(-p.f3 * __logf(prod), 0.0f);
+    for (uint32_t attempt = 1; X > p.f4; ++attempt) {
+        if (attempt == 4096u) {
+            atomicOr(err, ERR_GAMMA_REJECTION);
+            X = p.f4;
+            break;
+        }
+        const U4 r = draw_words(seed, link, attempt, 0u);
+        prod = u01_open0(r.x);
+        if (p.erlang > 1) prod *= u01_open0(r.y);
+        if (p.erlang > 2) prod *= u01_open0(r.z);
+        X = fmaxf(-p.f3 * __logf(prod), 0.0f);
+    }
+    *dfac = 1.0f + X;
+    return scale_by(base, *dfac);
+}
+
+// Other shapes by Marsaglia & Tsang (ACM TOMS 26(3), 2000) in FP32, normals from
+// Box-Muller; shapes below 1 draw Gamma(shape+1) times U^(1/shape).  The link
+// owns its blocks.  Same rejection cap.
 static __device__ __forceinline__ double draw_gamma(const DistParam &p, double base, uint32_t link, uint64_t seed,
                                                  int32_t *err, float *dfac) {
-    if (p.erlang) {
-        for (uint32_t attempt = 0; attempt < 4096u; ++attempt) {
-            const U4 r = draw_words(seed, link, attempt, 0u);
-            float prod = u01_open0(r.x);
-            if (p.erlang > 1) prod *= u01_open0(r.y);
-            if (p.erlang > 2) prod *= u01_open0(r.z);
-            const float X = fmaxf(-p.f3 * __logf(prod), 0.0f);
-            if (X > p.f4) continue;
-            *dfac = 1.0f + X;
-            return scale_by(base, *dfac);
-        }
-    } else {
-        const float d = p.f0, cc = p.f1;
-        for (uint32_t attempt = 0; attempt < 4096u; ++attempt) {
-            const U4 r = draw_words(seed, link, attempt, 0u);
-            const float rad = __fsqrt_rn(-2.0f * __logf(u01_open0(r.x)));
-            float sn, cs;
-            __sincosf(6.2831853071795865f * ((float)(r.y >> 8) * 5.9604644775390625e-08f), &sn, &cs);
-            float X = -1.0f;
+    const float d = p.f0, cc = p.f1;
+    for (uint32_t attempt = 0; attempt < 4096u; ++attempt) {
+        const U4 r = draw_words(seed, link, attempt, 0u);
+        const float rad = __fsqrt_rn(-2.0f * __logf(u01_open0(r.x)));
+        float sn, cs;
+        __sincosf(6.2831853071795865f * ((float)(r.y >> 8) * 5.9604644775390625e-08f), &sn, &cs);
+        float X = -1.0f;
 #pragma unroll
-            for (int j = 0; j < 2; ++j) {
-                const float z = j == 0 ? rad * cs : rad * sn;
-                const float t = fmaf(cc, z, 1.0f);
-                if (X < 0.0f && t > 0.0f) {
-                    const float v = t * t * t;
-                    const float u = u01_open0(j == 0 ? r.z : r.w);
-                    const float z2 = z * z;
-                    if (u < 1.0f - 0.0331f * z2 * z2 || __logf(u) < 0.5f * z2 + d * (1.0f - v + __logf(v)))
-                        X = d * v;
-                }
+        for (int j = 0; j < 2; ++j) {
+            const float z = j == 0 ? rad * cs : rad * sn;
+            const float t = fmaf(cc, z, 1.0f);
+            if (X < 0.0f && t > 0.0f) {
+                const float v = t * t * t;
+                const float u = u01_open0(j == 0 ? r.z : r.w);
+                const float z2 = z * z;
+                if (u < 1.0f - 0.0331f * z2 * z2 || __logf(u) < 0.5f * z2 + d * (1.0f - v + __logf(v))) X = d * v;
             }
-            if (X < 0.0f) continue;
-            if (p.boost) {
-                const U4 r2 = draw_words(seed, link, attempt, 1u);
-                X *= exp2f(__log2f(u01_open0(r2.x)) * p.f2);
-            }
-            X *= p.f3;
-            if (X > p.f4) continue;
-            *dfac = 1.0f + X;
-            return scale_by(base, *dfac);
         }
+        if (X < 0.0f) continue;
+        if (p.boost) {
+            const U4 r2 = draw_words(seed, link, attempt, 1u);
+            X *= exp2f(__log2f(u01_open0(r2.x)) * p.f2);
+        }
+        X *= p.f3;
+        if (X > p.f4) continue;
+        *dfac = 1.0f + X;
+        return scale_by(base, *dfac);
     }
     atomicOr(err, ERR_GAMMA_REJECTION);
     *dfac = 1.0f + p.f4;
@@ -212,12 +225,13 @@ __device__ __forceinline__ double draw_empirical(const DistParam &p, const Alias
 // the host-computed value for fixed links.  block: the link's Philox block;
 // grp: the words of the block the event's previous exponential or empirical
 // reference drew, redrawn here unless KD_REUSE says they are this link's block.
-// dvo: the record's dvo (PredRec); stage: the stage whose staging buffer holds
-// the link's duration table.  dists: the tables block (distributions, then
+// link: the link's index (the key of its own redraw blocks); dvo: the record's
+// dvo (PredRec); stage: the stage whose staging buffer holds the link's
+// duration table.  dists: the tables block (distributions, then
 // alias entries and picks); every other table address is derived here from
 // the kernel arguments, so that the propagation loop keeps no more pointers live.
 __device__ __forceinline__ double link_duration(const KArgs &a, int32_t kd, double v, int32_t dvo, uint32_t block,
-                                                uint64_t seed, U4 &grp, const DistParam *dists,
+                                                uint32_t link, uint64_t seed, U4 &grp, const DistParam *dists,
                                                 const unsigned char *smem, int stage, float &dfac) {
     const int kind = kd & KD_KIND_MASK;
     if (kind == K_FIXED) {
@@ -228,10 +242,11 @@ __device__ __forceinline__ double link_duration(const KArgs &a, int32_t kd, doub
     int32_t *err = a.err;
     const AliasEntry *alias = reinterpret_cast<const AliasEntry *>(dists + a.n_dist);
     const AliasPick *picks = reinterpret_cast<const AliasPick *>(alias + a.n_alias);
-    if (kind == K_GAMMA) return draw_gamma(p, v, block, seed, err, &dfac);
+    if (kind == K_GAMMA && !p.erlang) return draw_gamma(p, v, block, seed, err, &dfac);
     if (!(kd & KD_REUSE)) grp = draw_words(seed, block, 0u, 0u);
     const int wsel = (kd >> KD_WORD_SHIFT) & 3;
-    const uint32_t r = wsel == 0 ? grp.x : wsel == 1 ? grp.y : wsel == 2 ? grp.z : grp.w;
+    if (kind == K_GAMMA) return draw_erlang(p, v, link, seed, grp, wsel, err, &dfac);
+    const uint32_t r = word_of(grp, wsel);
     if (kind == K_EXP) return draw_exponential(p, v, r, dfac);
     const double *vt = nullptr;
     if (dvo >= 0)
@@ -444,7 +459,8 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec 
             if (GIVEN) {
                 dur = (t.active && pr.link >= 0) ? __ldg(&a.dur_in[(int64_t)pr.link * a.ld_in + t.s]) : 0.0;
             } else {
-                dur = link_duration(a, pr.kd, pr.v, pr.dvo, (uint32_t)pr.block, t.seed, grp, dists, smem, l, dfac);
+                dur = link_duration(a, pr.kd, pr.v, pr.dvo, (uint32_t)pr.block, (uint32_t)pr.link, t.seed, grp, dists,
+                                    smem, l, dfac);
                 if (!STATS && !ADJ && (pr.kd & KD_WRITE) && t.dcol) t.dcol[(int64_t)pr.link * t.ld] = dur;
             }
             // with the window on chip every source has a slot (the compiler checks it)
@@ -597,7 +613,7 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
             float dfac;
             U4 own;  // an unreferenced link owns its block
             const double dur =
-                link_duration(a, lr.kd, lr.v, -1, (uint32_t)lr.link, t.seed, own, dists, smem, 0, dfac);
+                link_duration(a, lr.kd, lr.v, -1, (uint32_t)lr.link, (uint32_t)lr.link, t.seed, own, dists, smem, 0, dfac);
             if (t.dcol) t.dcol[(int64_t)lr.link * t.ld] = dur;
         }
     }

@@ -18,13 +18,14 @@ enum Kind : int32_t { K_FIXED = 0, K_EXP = 1, K_GAMMA = 2, K_EMP_ABS = 3, K_EMP_
 
 // Packed kind word of a link reference:
 //   kind | word << KD_WORD_SHIFT | KD_REUSE | KD_TWO_WORD | KD_WRITE | dist << 8.
-// Random words: a link draws from the Philox block `block` of its PredRec.  One-
-// word links (exponential; empirical tables of at most kOneWordBins bins) share
-// a block with up to three other one-word links first referenced by the same
-// event, each taking its own word; KD_REUSE marks a reference whose block the
-// event's previous exponential or empirical reference already drew (the words
-// are still in registers).  Gamma links and larger empirical tables (KD_TWO_WORD) own their
-// block.  KD_WRITE marks the one reference of a link that stores its duration
+// Random words: a link draws from the Philox block `block` of its PredRec.
+// Links first referenced by the same event share blocks of four words: one-word
+// links (exponential; empirical tables of at most kOneWordBins bins) take one
+// word, gamma links of shape 1, 2 or 3 (sum of exponentials) take that many
+// words for their first attempt; `word` is the first of them.  KD_REUSE marks a
+// reference whose block the event's previous reference of these kinds already
+// drew (the words are still in registers).  Other gamma links and larger
+// empirical tables (KD_TWO_WORD) own their block.  KD_WRITE marks the one reference of a link that stores its duration
 // row; links no precedence entry references are stored by the aux-link pass.
 constexpr int32_t KD_KIND_MASK = 0x07;
 constexpr int KD_WORD_SHIFT = 3;  // bits 3-4

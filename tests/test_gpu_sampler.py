@@ -109,16 +109,18 @@ SHARED_GEN = [("constant", 1, 0.5), ("exponential", 2, 0.3, math.inf), ("gamma",
 
 
 def test_shared_philox_blocks_match_model(cuda):
-    """One-word links (exponential, small tables) first referenced by one event
-    share Philox blocks four at a time; gamma and a 5,000-bin table own theirs.
-    Every link's draws match the model at its (block, word)."""
+    """Links first referenced by one event share Philox blocks of four words:
+    one-word links (exponential, small tables) take a word, shape-2 gamma two; a
+    5,000-bin table owns its block.  Every link's draws match the model at its
+    (block, word)."""
     flat = _shared_block_dag()
     prop = propagator_from_flat(m, flat, SHARED_GEN)
     block, word = prop.link_streams()
     one_word = [0, 1, 2, 3, 6, 7, 9]  # links of types 2, 4, 5 in precedence order
-    assert list(block[one_word]) == [0, 0, 0, 0, 6, 6, 6] and list(word[one_word]) == [0, 1, 2, 3, 0, 1, 2]
+    assert list(block[one_word]) == [0, 0, 0, 0, 5, 5, 9] and list(word[one_word]) == [0, 1, 2, 3, 2, 3, 0]
     assert block[4] == -1 and block[10] == -1  # constant
-    assert (block[5], word[5]) == (5, -1) and (block[8], word[8]) == (8, -1)  # gamma, big table
+    assert (block[5], word[5]) == (5, 0)  # shape-2 gamma: words 0 and 1 of block 5
+    assert (block[8], word[8]) == (8, -1)  # big table
     _, dur, _ = prop.run_many_arrays(SEEDS)
     gen = {g[1]: g for g in SHARED_GEN}
     kinds = flat["act_type"]

@@ -220,28 +220,20 @@ __device__ __forceinline__ double draw_empirical(const DistParam &p, const Alias
     return relative ? __dadd_rn(base, __dmul_rn(val, base)) : __dadd_rn(base, val);
 }
 
-// The link's duration for one sample, and (dfac) its derivative with respect to
-// the base duration: 1 + X for the multiplicative kinds, 1 for absolute tables,
-// the host-computed value for fixed links.  block: the link's Philox block;
-// grp: the words of the block the event's previous exponential or empirical
-// reference drew, redrawn here unless KD_REUSE says they are this link's block.
-// link: the link's index (the key of its own redraw blocks); dvo: the record's
-// dvo (PredRec); stage: the stage whose staging buffer holds the link's
-// duration table.  dists: the tables block (distributions, then
-// alias entries and picks); every other table address is derived here from
-// the kernel arguments, so that the propagation loop keeps no more pointers live.
-__device__ __forceinline__ double link_duration(const KArgs &a, int32_t kd, double v, int32_t dvo, uint32_t block,
-                                                uint32_t link, uint64_t seed, U4 &grp, const DistParam *dists,
-                                                const unsigned char *smem, int stage, float &dfac) {
-    const int kind = kd & KD_KIND_MASK;
-    if (kind == K_FIXED) {
-        dfac = __int_as_float(dvo);
-        return v;
-    }
+// A sampled link's duration.  TSMEM: the tables block is in shared memory;
+// STAGED: the link's duration table (if any) is in the current stage's staging
+// buffer.  Both are compile-time here so that every table read is a
+// shared-memory load (or a global one) rather than a generic load.
+template <bool STAGED, bool TSMEM>
+__device__ __forceinline__ double sampled_duration(const KArgs &a, int32_t kd, double v, int32_t dvo, uint32_t block,
+                                                   uint32_t link, uint64_t seed, U4 &grp, const unsigned char *smem,
+                                                   int stage, float &dfac) {
+    const DistParam *dists = TSMEM ? reinterpret_cast<const DistParam *>(smem + a.smem_tables_off) : a.dist;
     const DistParam &p = dists[kd >> 8];
     int32_t *err = a.err;
     const AliasEntry *alias = reinterpret_cast<const AliasEntry *>(dists + a.n_dist);
     const AliasPick *picks = reinterpret_cast<const AliasPick *>(alias + a.n_alias);
+    const int kind = kd & KD_KIND_MASK;
     if (kind == K_GAMMA && !p.erlang) return draw_gamma(p, v, block, seed, err, &dfac);
     if (!(kd & KD_REUSE)) grp = draw_words(seed, block, 0u, 0u);
     const int wsel = (kd >> KD_WORD_SHIFT) & 3;
@@ -250,10 +242,31 @@ __device__ __forceinline__ double link_duration(const KArgs &a, int32_t kd, doub
     if (kind == K_EXP) return draw_exponential(p, v, r, dfac);
     const double *vt = nullptr;
     if (dvo >= 0)
-        vt = (dvo & kVtGlobal) ? a.vals + (dvo ^ kVtGlobal)
-                               : reinterpret_cast<const double *>(smem + a.smem_stage_off + (stage & 1) * a.stage_bytes +
-                                                                  dvo);
+        vt = STAGED ? reinterpret_cast<const double *>(smem + a.smem_stage_off + (stage & 1) * a.stage_bytes + dvo)
+                    : a.vals + (dvo ^ kVtGlobal);
     return draw_empirical(p, alias, picks, vt, v, kind == K_EMP_REL, r, grp.y, (kd & KD_TWO_WORD) != 0, dfac);
+}
+
+// The link's duration for one sample, and (dfac) its derivative with respect to
+// the base duration: 1 + X for the multiplicative kinds, 1 for absolute tables,
+// the host-computed value for fixed links.  block: the link's Philox block;
+// grp: the words of the block the event's previous exponential or empirical
+// reference drew, redrawn here unless KD_REUSE says they are this link's block.
+// link: the link's index (the key of its own redraw blocks); dvo: the record's
+// dvo (PredRec); stage: the stage whose staging buffer holds the link's
+// duration table (STAGED; otherwise the table is in KArgs::vals).  Every table
+// address is derived here from the kernel arguments, so that the propagation
+// loop keeps no table pointers live.
+template <bool STAGED>
+__device__ __forceinline__ double link_duration(const KArgs &a, int32_t kd, double v, int32_t dvo, uint32_t block,
+                                                uint32_t link, uint64_t seed, U4 &grp, const unsigned char *smem,
+                                                int stage, float &dfac) {
+    if ((kd & KD_KIND_MASK) == K_FIXED) {
+        dfac = __int_as_float(dvo);
+        return v;
+    }
+    if (a.tables_in_smem) return sampled_duration<STAGED, true>(a, kd, v, dvo, block, link, seed, grp, smem, stage, dfac);
+    return sampled_duration<STAGED, false>(a, kd, v, dvo, block, link, seed, grp, smem, stage, dfac);
 }
 
 // ---------------------------------------------------------------- records
@@ -431,8 +444,8 @@ __device__ __forceinline__ int take_next(uint32_t ctr) {
 // global indices).
 template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ, bool STAGED>
 __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec *sev, const PredRec *spred, int pred0,
-                                             int n_ev, uint32_t ctr, const TileCtx &t, const DistParam *dists,
-                                             unsigned char *smem, U4 &grp) {
+                                             int n_ev, uint32_t ctr, const TileCtx &t, unsigned char *smem,
+                                             U4 &grp) {
     double *win = reinterpret_cast<double *>(smem);
     const int lane = t.lane;
     // the next index is taken before this event's work, hiding the atomic's
@@ -459,8 +472,8 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec 
             if (GIVEN) {
                 dur = (t.active && pr.link >= 0) ? __ldg(&a.dur_in[(int64_t)pr.link * a.ld_in + t.s]) : 0.0;
             } else {
-                dur = link_duration(a, pr.kd, pr.v, pr.dvo, (uint32_t)pr.block, (uint32_t)pr.link, t.seed, grp, dists,
-                                    smem, l, dfac);
+                dur = link_duration<STAGED>(a, pr.kd, pr.v, pr.dvo, (uint32_t)pr.block, (uint32_t)pr.link, t.seed,
+                                            grp, smem, l, dfac);
                 if (!STATS && !ADJ && (pr.kd & KD_WRITE) && t.dcol) t.dcol[(int64_t)pr.link * t.ld] = dur;
             }
             // with the window on chip every source has a slot (the compiler checks it)
@@ -532,7 +545,6 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
                                                bool rows_tile_local, unsigned char *smem, uint64_t *bars,
                                                bool reuse) {
     DistParam *s_dist = reinterpret_cast<DistParam *>(smem + a.smem_tables_off);
-    const DistParam *dists = a.tables_in_smem ? s_dist : a.dist;
 
     TileCtx t;
     t.lane = threadIdx.x & 31;
@@ -597,10 +609,10 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
             const unsigned char *buf = smem + a.smem_stage_off + b * a.stage_bytes;
             stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, true>(
                 a, l, reinterpret_cast<const EvRec *>(buf), reinterpret_cast<const PredRec *>(buf + mv.z), meta.z,
-                meta.y, ctr, t, dists, smem, grp);
+                meta.y, ctr, t, smem, grp);
         } else {  // a stage whose records exceed the buffer is read from global memory
             stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, false>(a, l, a.ev + meta.x, a.pred + meta.z, meta.z,
-                                                                       -meta.y, ctr, t, dists, smem, grp);
+                                                                       -meta.y, ctr, t, smem, grp);
         }
         __syncthreads();
         if (threadIdx.x == 0 && l + 2 < a.n_stages)
@@ -613,7 +625,7 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
             float dfac;
             U4 own;  // an unreferenced link owns its block
             const double dur =
-                link_duration(a, lr.kd, lr.v, -1, (uint32_t)lr.link, (uint32_t)lr.link, t.seed, own, dists, smem, 0, dfac);
+                link_duration<false>(a, lr.kd, lr.v, -1, (uint32_t)lr.link, (uint32_t)lr.link, t.seed, own, smem, 0, dfac);
             if (t.dcol) t.dcol[(int64_t)lr.link * t.ld] = dur;
         }
     }

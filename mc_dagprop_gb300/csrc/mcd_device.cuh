@@ -90,23 +90,20 @@ __device__ __forceinline__ long long order_key(long long b) {
 }
 
 // ---------------------------------------------------------------- duration scaling
-// The double equal to a float m >= 1, built with integer operations: a
+// The double equal to a finite float m >= 1, built with integer operations: a
 // float-to-double conversion would occupy the FP64 pipe, which on this part
-// issues about 1.6 lane-operations per clock per SM.  An infinite m stays
-// infinite.
+// issues about 1.6 lane-operations per clock per SM.
 __device__ __forceinline__ double widen(float m) {
     const uint32_t b = __float_as_uint(m);
-    uint32_t hi = (((b >> 23) + 896u) << 20) | ((b >> 3) & 0x000FFFFFu);
-    uint32_t lo = b << 29;
-    if (b >= 0x7F800000u) {
-        hi = 0x7FF00000u;
-        lo = 0u;
-    }
-    return __hiloint2double((int)hi, (int)lo);
+    const uint32_t hi = (((b >> 23) + 896u) << 20) | ((b >> 3) & 0x000FFFFFu);
+    return __hiloint2double((int)hi, (int)(b << 29));
 }
 
-// A sampled duration base * (1 + X), 1 + X rounded to float: one FP64 multiply.
-__device__ __forceinline__ double scale_by(double base, float m) { return __dmul_rn(base, widen(m)); }
+// A sampled duration base * (1 + X), 1 + X rounded to float and held below
+// float overflow (reached only for means above ~1e37): one FP64 multiply.
+__device__ __forceinline__ double scale_by(double base, float m) {
+    return __dmul_rn(base, widen(fminf(m, 3.4028234663852886e38f)));
+}
 
 // ---------------------------------------------------------------- samplers
 // Each returns the link's duration (base + extra) for one sample.
@@ -429,11 +426,12 @@ struct TileCtx {
 };
 
 // Lane 0 takes the next event index of a stage from its shared-memory counter.
-// (Inline PTX: a plain atomicAdd under a lane test is compiled into a
-// warp-aggregated atomic, several instructions per event for one active lane.)
+// (An increment with wrap-around at 2^31 - 1, which equals an add of one here: an
+// add of a constant is compiled into a warp-aggregated atomic, several
+// instructions per event for one active lane.)
 __device__ __forceinline__ int take_next(uint32_t ctr) {
     int v;
-    asm volatile("atom.shared.add.u32 %0, [%1], 1;" : "=r"(v) : "r"(ctr) : "memory");
+    asm volatile("atom.shared.inc.u32 %0, [%1], 0x7FFFFFFF;" : "=r"(v) : "r"(ctr) : "memory");
     return v;
 }
 

@@ -62,7 +62,7 @@ def _from_bits(b: int) -> float:
 def scale_by(base: float, m) -> float:
     """The kernel's base * m for a float32 m >= 1: one IEEE double multiply by the
     double equal to m."""
-    return float(base) * float(np.float32(m))
+    return float(base) * float(min(np.float32(m), np.float32(3.4028234663852886e38)))
 
 
 def exponential_durations(seeds, link, base, lam, max_scale, block=None, word=0):

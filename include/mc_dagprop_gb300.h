@@ -21,6 +21,8 @@
  *   mcd_stats_*               per-event statistics (no reference counterpart; the
  *                             reference's users stack run_many results in numpy,
  *                             demo/monte_carlo.py:48-49)
+ *   mcd_analytic_*            the analytic PMF propagator, src/mc_dagprop/analytic/
+ *                             (pure Python in the reference)
  *
  * Layouts.  "Sample-major" (host entry points) is the reference's SimResult
  * layout: one contiguous row per sample, realized[s*E + e], durations[s*L + l],
@@ -279,6 +281,57 @@ int mcd_server_submit(mcd_server *server, const mcd_dag_desc *desc, const mcd_ge
 int mcd_server_wait(mcd_server *server, int64_t ticket, double wait_ms, const mcd_stats *host, int32_t *done,
                     double *latency_ms);
 int mcd_server_counters(mcd_server *server, mcd_server_info *info);
+
+/* ---- Analytic PMF propagation ----
+ * The reference's analytic engine (src/mc_dagprop/analytic/, pure Python there)
+ * on the GPU: discrete PMFs on an integer step grid are propagated level by
+ * level -- convolution along each incoming activity (_pmf.py:107-125), maximum
+ * over predecessors by cumulative products (_pmf.py:127-148), clipping to the
+ * event's bounds under the underflow/overflow rules (_propagator.py:150-265).
+ * One CTA per event of a level; results stay on the device until fetched.
+ *
+ *   mcd_analytic_create   create_analytic_propagator (_propagator.py:48-72):
+ *                         checks indices, orders the DAG, plans supports, uploads
+ *   mcd_analytic_run      AnalyticPropagator.run (_propagator.py:89-148)
+ *   mcd_analytic_fetch    the SimulatedEvent tuple (_context.py:29-40): per event
+ *                         its PMF (first value, probabilities) and the underflow
+ *                         and overflow masses
+ *
+ * Activity PMFs are probability arrays on the context's step grid: PMF k has
+ * probabilities pmf_probs[pmf_off[k] .. pmf_off[k+1]) at values
+ * pmf_first[k] + i * step.  The PMF of a predecessor entry is the one of its
+ * (source, target) activity, pred_pmf[p]. */
+#define MCD_RULE_TRUNCATE 1
+#define MCD_RULE_REMOVE 2
+#define MCD_RULE_REDISTRIBUTE 3
+typedef struct mcd_analytic mcd_analytic;
+typedef struct mcd_analytic_desc {
+    int32_t n_events;
+    const double *earliest;    /* [n_events] EventTimestamp.earliest */
+    const double *latest;      /* [n_events] EventTimestamp.latest */
+    int32_t n_pmfs;
+    const int64_t *pmf_off;    /* [n_pmfs + 1] */
+    const double *pmf_first;   /* [n_pmfs] */
+    const double *pmf_probs;   /* [pmf_off[n_pmfs]] */
+    int32_t n_targets;
+    const int32_t *target;     /* [n_targets] */
+    const int64_t *pred_off;   /* [n_targets + 1] */
+    const int32_t *pred_src;   /* [pred_off[n_targets]] predecessor events, in order */
+    const int32_t *pred_pmf;   /* [pred_off[n_targets]] activity PMF of each entry */
+    int32_t step;              /* grid spacing, > 0 */
+    double max_delay;          /* NaN: none */
+    int32_t underflow_rule;    /* MCD_RULE_* */
+    int32_t overflow_rule;
+} mcd_analytic_desc;
+int mcd_analytic_create(const mcd_analytic_desc *desc, mcd_analytic **out);
+void mcd_analytic_destroy(mcd_analytic *an);
+int mcd_analytic_run(mcd_analytic *an);
+/* Total probability entries of the last run's results (the size of `probs` below). */
+int64_t mcd_analytic_bins(const mcd_analytic *an);
+/* Per event: first value, offset and length of its probabilities in `probs`,
+ * underflow and overflow mass.  Any output may be NULL. */
+int mcd_analytic_fetch(const mcd_analytic *an, double *first, int64_t *offset, int64_t *length, double *probs,
+                       double *underflow, double *overflow);
 
 /* ---- Pinned host memory ---- */
 int mcd_host_alloc(size_t bytes, void **out);

@@ -28,7 +28,24 @@ except ImportError as exc:  # the compiled module is missing: fail loudly
         "(CUDA, sm_103a). Build it with `python mc_dagprop_gb300/_build.py`."
     ) from exc
 
+from .analytic import (  # noqa: E402
+    AnalyticContext,
+    AnalyticPropagator,
+    DiscretePMF,
+    OverflowRule,
+    SimulatedEvent,
+    UnderflowRule,
+    create_analytic_propagator,
+)
+
 __all__ = [
+    "DiscretePMF",
+    "SimulatedEvent",
+    "UnderflowRule",
+    "OverflowRule",
+    "AnalyticContext",
+    "AnalyticPropagator",
+    "create_analytic_propagator",
     "Batch",
     "Server",
     "GenericDelayGenerator",

@@ -59,3 +59,25 @@ def load():
     loader.exec_module(core)
     mc._core = core
     return core
+
+
+def load_analytic():
+    """Return the reference's pure-Python analytic package ``mc_dagprop.analytic``
+    (loaded from its sources; it imports ``Event`` from the package root, which is
+    the compiled module's class)."""
+    name = "mc_dagprop.analytic"
+    if name in sys.modules:
+        return sys.modules[name]
+    core = load()
+    root = sys.modules["mc_dagprop"]
+    for attr in ("Event", "EventTimestamp", "Activity", "DagContext", "GenericDelayGenerator", "SimResult"):
+        if hasattr(core, attr):
+            setattr(root, attr, getattr(core, attr))
+    pkg_dir = os.path.join(REF_ROOT, "src", "mc_dagprop", "analytic")
+    spec = importlib.util.spec_from_file_location(name, os.path.join(pkg_dir, "__init__.py"),
+                                                  submodule_search_locations=[pkg_dir])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    root.analytic = mod
+    return mod

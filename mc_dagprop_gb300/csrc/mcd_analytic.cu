@@ -2,8 +2,10 @@
 // src/mc_dagprop/analytic/, pure Python there), behind the mcd_analytic_* C ABI.
 //
 // A PMF is (first value, probabilities) on the context's step grid.  Events are
-// processed level by level (longest path from a source); one CTA of 256 threads
-// computes one event:
+// processed level by level (longest path from a source), two launches a level:
+// k_an_conv computes every convolution of the level, its outputs split into
+// chunks of 256 across CTAs (the FP64 multiply-adds are the bulk of the work);
+// k_an_fold then takes one event per CTA:
 //   convolution along each incoming activity       _pmf.py:107-125
 //   maximum over the predecessors, pairwise in      _pmf.py:127-148
 //   precedence order, by cumulative products
@@ -73,6 +75,8 @@ struct AnArgs {
     AnOut *out;
     double *pool;
     double *scratch;
+    double *convbuf;          // the level's convolutions, conv_off[p] per predecessor entry
+    const int64_t *conv_off;
     int32_t *err;
     int32_t step;
     int32_t urule, orule;
@@ -139,27 +143,35 @@ __device__ void block_scan(double *x, int64_t n, double *red) {
     __syncthreads();
 }
 
-// The convolution of a pred PMF (p, n) with an activity PMF (q, m) into
-// dst[0, n + m - 1) (or the scaled copy of the one-entry cases, _pmf.py:109-116).
-__device__ void convolve_into(const double *p, int64_t n, const double *q, int64_t m, double *dst) {
-    if (n == 1) {
-        for (int64_t j = threadIdx.x; j < m; j += kAnThreads) dst[j] = q[j] * p[0];
-    } else if (m == 1) {
-        for (int64_t j = threadIdx.x; j < n; j += kAnThreads) dst[j] = p[j] * q[0];
-    } else {
-        for (int64_t j = threadIdx.x; j < n + m - 1; j += kAnThreads) {
-            const int64_t i0 = j - (m - 1) > 0 ? j - (m - 1) : 0, i1 = j < n - 1 ? j : n - 1;
-            double acc = 0.0;
-            for (int64_t i = i0; i <= i1; ++i) acc = fma(p[i], q[j - i], acc);
-            dst[j] = acc;
-        }
-    }
-    __syncthreads();
-}
-
 __device__ __forceinline__ int64_t round_half_even(double x) { return (int64_t)rint(x); }
 
-__global__ void __launch_bounds__(kAnThreads) k_analytic_level(const AnArgs A, const int32_t *__restrict__ level_ev) {
+// Length of the convolution of a pred PMF of n entries with an activity PMF of m.
+__device__ __forceinline__ int64_t conv_len(int64_t n, int64_t m) { return n == 1 ? m : (m == 1 ? n : n + m - 1); }
+
+// One chunk of 256 outputs of one convolution: chunks[blockIdx.x] = (predecessor
+// entry, chunk index).  Chunks past the convolution's actual length exit.
+__global__ void __launch_bounds__(kAnThreads) k_an_conv(const AnArgs A, const int2 *__restrict__ chunks) {
+    const int2 c = chunks[blockIdx.x];
+    const int32_t s = A.pred_src[c.x], k = A.pred_pmf[c.x];
+    const int64_t n = A.out[s].len, m = A.pmf_off[k + 1] - A.pmf_off[k];
+    const int64_t j = (int64_t)c.y * kAnThreads + threadIdx.x;
+    if (j >= conv_len(n, m)) return;
+    const double *p = A.pool + A.ev[s].pool_off, *q = A.pmf_probs + A.pmf_off[k];
+    double v;
+    if (n == 1) {
+        v = q[j] * p[0];
+    } else if (m == 1) {
+        v = p[j] * q[0];
+    } else {
+        const int64_t i0 = j - (m - 1) > 0 ? j - (m - 1) : 0, i1 = j < n - 1 ? j : n - 1;
+        double acc = 0.0;
+        for (int64_t i = i0; i <= i1; ++i) acc = fma(p[i], q[j - i], acc);
+        v = acc;
+    }
+    A.convbuf[A.conv_off[c.x] + j] = v;
+}
+
+__global__ void __launch_bounds__(kAnThreads) k_an_fold(const AnArgs A, const int32_t *__restrict__ level_ev) {
     extern __shared__ __align__(16) double sm[];
     __shared__ double red[kAnThreads / 32];
     const int32_t e = level_ev[blockIdx.x];
@@ -181,13 +193,15 @@ __global__ void __launch_bounds__(kAnThreads) k_analytic_level(const AnArgs A, c
         const int32_t s = A.pred_src[ev.pred_begin], k = A.pred_pmf[ev.pred_begin];
         const AnOut ps = A.out[s];
         const int64_t m = A.pmf_off[k + 1] - A.pmf_off[k];
-        nX = (ps.len == 1) ? m : (m == 1 ? ps.len : ps.len + m - 1);
+        nX = conv_len(ps.len, m);
         fX = ps.first + A.pmf_first[k];
         if (nX > G) {
             fail(AN_ERR_CAPACITY);
             return;
         }
-        convolve_into(A.pool + A.ev[s].pool_off, ps.len, A.pmf_probs + A.pmf_off[k], m, X);
+        const double *conv = A.convbuf + A.conv_off[ev.pred_begin];
+        for (int64_t j = threadIdx.x; j < nX; j += kAnThreads) X[j] = conv[j];
+        __syncthreads();
         const double expct = expected_mass(ps.mass, A.pmf_mass[k]);
         const double tot = range_sum(X, 0, nX, red);
         if (tot > 0.0 && !close12(tot, expct)) range_scale(X, 0, nX, expct / tot);
@@ -198,7 +212,7 @@ __global__ void __launch_bounds__(kAnThreads) k_analytic_level(const AnArgs A, c
         const int32_t s = A.pred_src[pi], k = A.pred_pmf[pi];
         const AnOut ps = A.out[s];
         const int64_t m = A.pmf_off[k + 1] - A.pmf_off[k];
-        const int64_t nC = (ps.len == 1) ? m : (m == 1 ? ps.len : ps.len + m - 1);
+        const int64_t nC = conv_len(ps.len, m);
         const double fC = ps.first + A.pmf_first[k];
         // common grid: np.arange(min start, max end + step, step) (_pmf.py:129-134)
         const double lo = fmin(fX, fC);
@@ -214,7 +228,11 @@ __global__ void __launch_bounds__(kAnThreads) k_analytic_level(const AnArgs A, c
             Cp[i] = 0.0;
         }
         __syncthreads();
-        convolve_into(A.pool + A.ev[s].pool_off, ps.len, A.pmf_probs + A.pmf_off[k], m, Cp + oC);
+        {
+            const double *conv = A.convbuf + A.conv_off[pi];
+            for (int64_t j = threadIdx.x; j < nC; j += kAnThreads) Cp[oC + j] = conv[j];
+            __syncthreads();
+        }
         {
             const double expct = expected_mass(ps.mass, A.pmf_mass[k]);
             const double tot = range_sum(Cp, oC, oC + nC, red);
@@ -371,8 +389,11 @@ struct mcd_analytic {
     int32_t E = 0;
     AnArgs args{};
     std::vector<int32_t> level_off;    // non-origin levels: events level_ev[level_off[l] .. level_off[l+1])
-    std::vector<int32_t> level_smem;   // dynamic shared memory per level launch (bytes)
+    std::vector<int32_t> level_smem;   // dynamic shared memory per fold launch (bytes)
+    std::vector<int32_t> chunk_off;    // convolution chunks of each level: chunks[chunk_off[l] .. chunk_off[l+1])
     int32_t *d_level_ev = nullptr;
+    int2 *d_chunks = nullptr;
+    cudaGraphExec_t graph = nullptr;   // every level's two launches
     char *dmem = nullptr;
     int64_t bins = 0;                  // output pool size
     bool ran = false;
@@ -501,11 +522,13 @@ int mcd_analytic_create(const mcd_analytic_desc *d, mcd_analytic **out) {
         an = new mcd_analytic();
         an->E = E;
         std::vector<int32_t> level_ev;
+        std::vector<int2> chunks;
+        std::vector<int64_t> conv_off((size_t)std::max<int64_t>(P, 1), 0);
         an->level_off.push_back(0);
-        int64_t scratch_max = 0;
+        an->chunk_off.push_back(0);
+        int64_t scratch_max = 0, conv_max = 0;
         for (int32_t l = 1; l <= n_levels; ++l) {
-            int64_t scratch = 0;
-            int64_t smem_bins = 0;
+            int64_t scratch = 0, smem_bins = 0, conv = 0;
             for (int32_t e : by_level[l]) {
                 AnEv &r = ev[e];
                 if (r.gmax <= kAnSmemBins) {
@@ -515,9 +538,18 @@ int mcd_analytic_create(const mcd_analytic_desc *d, mcd_analytic **out) {
                     scratch += 5 * (int64_t)r.gmax;
                 }
                 level_ev.push_back(e);
+                for (int64_t p = tstart[e]; p < tstart[e] + tlen[e]; ++p) {  // each convolution's slot and chunks
+                    const int64_t n = ev[d->pred_src[p]].cap, m = d->pmf_off[d->pred_pmf[p] + 1] - d->pmf_off[d->pred_pmf[p]];
+                    const int64_t len = n == 1 ? m : (m == 1 ? n : n + m - 1);
+                    conv_off[p] = conv;
+                    conv += (len + 1) / 2 * 2;
+                    for (int64_t c = 0; c * kAnThreads < len; ++c) chunks.push_back(make_int2((int)p, (int)c));
+                }
             }
             scratch_max = std::max(scratch_max, scratch);
+            conv_max = std::max(conv_max, conv);
             an->level_off.push_back((int32_t)level_ev.size());
+            an->chunk_off.push_back((int32_t)chunks.size());
             an->level_smem.push_back((int32_t)(5 * smem_bins * (int64_t)sizeof(double)));
         }
         an->bins = pool;
@@ -530,8 +562,11 @@ int mcd_analytic_create(const mcd_analytic_desc *d, mcd_analytic **out) {
                      s_out = align_up((size_t)std::max(E, 1) * sizeof(AnOut), 256),
                      s_pool = align_up((size_t)std::max<int64_t>(pool, 1) * 8, 256),
                      s_scr = align_up((size_t)std::max<int64_t>(scratch_max, 1) * 8, 256),
-                     s_lev = align_up((size_t)std::max<size_t>(level_ev.size(), 1) * 4, 256), s_err = 256;
-        const size_t total = s_ev + 2 * s_pred + s_poff + 2 * s_pk + s_probs + s_out + s_pool + s_scr + s_lev + s_err;
+                     s_lev = align_up((size_t)std::max<size_t>(level_ev.size(), 1) * 4, 256), s_err = 256,
+                     s_coff = align_up(conv_off.size() * 8, 256), s_conv = align_up((size_t)std::max<int64_t>(conv_max, 1) * 8, 256),
+                     s_chunk = align_up(std::max<size_t>(chunks.size(), 1) * sizeof(int2), 256);
+        const size_t total = s_ev + 2 * s_pred + s_poff + 2 * s_pk + s_probs + s_out + s_pool + s_scr + s_lev + s_err +
+                             s_coff + s_conv + s_chunk;
         cuda_check(cudaMalloc(&an->dmem, total), "analytic allocation");
         char *p = an->dmem;
         auto put = [&](const void *src, size_t bytes, size_t slot) -> char * {
@@ -565,14 +600,32 @@ int mcd_analytic_create(const mcd_analytic_desc *d, mcd_analytic **out) {
         a.scratch = reinterpret_cast<double *>(p);
         p += s_scr;
         an->d_level_ev = reinterpret_cast<int32_t *>(put(level_ev.data(), level_ev.size() * 4, s_lev));
+        a.conv_off = reinterpret_cast<const int64_t *>(put(conv_off.data(), conv_off.size() * 8, s_coff));
+        a.convbuf = reinterpret_cast<double *>(p);
+        p += s_conv;
+        an->d_chunks = reinterpret_cast<int2 *>(put(chunks.data(), chunks.size() * sizeof(int2), s_chunk));
         a.err = reinterpret_cast<int32_t *>(p);
         cuda_check(cudaMemset(a.err, 0, 4), "analytic error flag");
         a.step = d->step;
         a.urule = d->underflow_rule;
         a.orule = d->overflow_rule;
-        cuda_check(cudaFuncSetAttribute(k_analytic_level, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cuda_check(cudaFuncSetAttribute(k_an_fold, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)(5 * kAnSmemBins * sizeof(double))),
                    "analytic shared memory");
+        // every level's launches, captured once into a graph
+        cuda_check(cudaStreamBeginCapture(an->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+        for (size_t l = 0; l + 1 < an->level_off.size(); ++l) {
+            const int32_t nc = an->chunk_off[l + 1] - an->chunk_off[l], ne = an->level_off[l + 1] - an->level_off[l];
+            if (nc > 0) k_an_conv<<<nc, kAnThreads, 0, an->stream>>>(an->args, an->d_chunks + an->chunk_off[l]);
+            if (ne > 0)
+                k_an_fold<<<ne, kAnThreads, an->level_smem[l], an->stream>>>(an->args, an->d_level_ev + an->level_off[l]);
+        }
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(an->stream, &g);
+        cuda_check(ce, "graph capture");
+        const cudaError_t ie = cudaGraphInstantiate(&an->graph, g, 0);
+        cudaGraphDestroy(g);
+        cuda_check(ie, "graph instantiate");
         *out = an;
     });
     if (rc != MCD_OK && an) mcd_analytic_destroy(an);
@@ -581,10 +634,9 @@ int mcd_analytic_create(const mcd_analytic_desc *d, mcd_analytic **out) {
 
 void mcd_analytic_destroy(mcd_analytic *an) {
     if (!an) return;
-    if (an->stream) {
-        cudaStreamSynchronize(an->stream);
-        cudaStreamDestroy(an->stream);
-    }
+    if (an->stream) cudaStreamSynchronize(an->stream);
+    if (an->graph) cudaGraphExecDestroy(an->graph);
+    if (an->stream) cudaStreamDestroy(an->stream);
     if (an->dmem) cudaFree(an->dmem);
     delete an;
 }
@@ -593,13 +645,7 @@ int mcd_analytic_run(mcd_analytic *an) {
     return guarded([&] {
         if (!an) throw McdError(MCD_ERR_INVALID, "null handle");
         cuda_check(cudaSetDevice(an->device), "cudaSetDevice");
-        for (size_t l = 0; l + 1 < an->level_off.size(); ++l) {
-            const int32_t n = an->level_off[l + 1] - an->level_off[l];
-            if (n == 0) continue;
-            k_analytic_level<<<n, kAnThreads, an->level_smem[l], an->stream>>>(an->args,
-                                                                              an->d_level_ev + an->level_off[l]);
-            cuda_check(cudaGetLastError(), "analytic launch");
-        }
+        cuda_check(cudaGraphLaunch(an->graph, an->stream), "analytic launch");
         cuda_check(cudaStreamSynchronize(an->stream), "analytic run");
         int32_t flags = 0;
         cuda_check(cudaMemcpy(&flags, an->args.err, 4, cudaMemcpyDeviceToHost), "analytic error flag");

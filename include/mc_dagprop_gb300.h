@@ -23,6 +23,7 @@
  *                             demo/monte_carlo.py:48-49)
  *   mcd_analytic_*            the analytic PMF propagator, src/mc_dagprop/analytic/
  *                             (pure Python in the reference)
+ *   mcd_delay_histograms      per-type delay inspection, demo/inspection.py:11-29
  *
  * Layouts.  "Sample-major" (host entry points) is the reference's SimResult
  * layout: one contiguous row per sample, realized[s*E + e], durations[s*L + l],
@@ -281,6 +282,21 @@ int mcd_server_submit(mcd_server *server, const mcd_dag_desc *desc, const mcd_ge
 int mcd_server_wait(mcd_server *server, int64_t ticket, double wait_ms, const mcd_stats *host, int32_t *done,
                     double *latency_ms);
 int mcd_server_counters(mcd_server *server, mcd_server_info *info);
+
+/* ---- Delay inspection ----
+ * Per-class histograms of sampled delays, durations[l] - base[l] (absolute) and
+ * (durations[l] - base[l]) / base[l] for base[l] != 0 (relative), over n samples:
+ * the reference's demo/inspection.py:11-29 (which lists the delays of every
+ * activity by type) without materialising the durations on the host.
+ * link_class[l]: class of link l in 0..n_classes-1 (-1: skipped); link_base[l]: its
+ * minimal duration.  ranges[c*4 .. c*4+3]: absolute lo, hi, relative lo, hi.
+ * Bin of x: 0 below lo, 1 + floor((x - lo) * n_bins / (hi - lo)) inside, n_bins + 1
+ * at or above hi.  counts[(c*2 + k)*(n_bins + 2) + bin] (k = 0 absolute, 1
+ * relative); moments[c*6 + k*3 + {0, 1, 2}] = count, sum, sum of squares.
+ * n_classes * 2 * (n_bins + 2) counters must fit 48 KB. */
+int mcd_delay_histograms(mcd_dag *dag, const int64_t *seeds, int64_t n, const int32_t *link_class,
+                         const double *link_base, int32_t n_classes, int32_t n_bins, const double *ranges,
+                         uint64_t *counts, double *moments);
 
 /* ---- Analytic PMF propagation ----
  * The reference's analytic engine (src/mc_dagprop/analytic/, pure Python there)

@@ -371,6 +371,20 @@ __device__ __forceinline__ long long to_ticks(long long b, int q) {
     return b < 0 ? -t : t;
 }
 
+// Sum over the warp of non-negative 64-bit tick counts: four 16-bit limbs summed
+// with one redux.sync each (a limb's sum stays below 2^21), then recombined -- the
+// exact sum, as long as it stays below 2^64 (the host's choice of tick keeps the
+// sum over all samples below 2^63).
+__device__ __forceinline__ long long warp_sum_ticks(long long d) {
+    const unsigned long long u = (unsigned long long)d;
+    const unsigned s0 = __reduce_add_sync(0xFFFFFFFFu, (unsigned)(u & 0xFFFFu));
+    const unsigned s1 = __reduce_add_sync(0xFFFFFFFFu, (unsigned)((u >> 16) & 0xFFFFu));
+    const unsigned s2 = __reduce_add_sync(0xFFFFFFFFu, (unsigned)((u >> 32) & 0xFFFFu));
+    const unsigned s3 = __reduce_add_sync(0xFFFFFFFFu, (unsigned)(u >> 48));
+    return (long long)((unsigned long long)s0 + ((unsigned long long)s1 << 16) + ((unsigned long long)s2 << 32) +
+                       ((unsigned long long)s3 << 48));
+}
+
 // One event's realized values of the tile into the per-event accumulators:
 // the tile's sum of (realized - earliest) with one 64-bit atomic, and the
 // histogram with one atomic per distinct bin of the warp.
@@ -383,8 +397,7 @@ __device__ __forceinline__ void accumulate_stats(const KArgs &a, const EvRec &ev
         const unsigned long long du = (unsigned long long)(d > 0 ? d : 0ll);
         bin = (int)__umul64hi(du, a.bin_mul);
         bin = bin > kHistBins - 1 ? kHistBins - 1 : bin;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xFFFFFFFFu, d, off);
+        d = warp_sum_ticks(d > 0 ? d : 0ll);  // realized >= earliest: d >= 0
         if ((threadIdx.x & 31) == 0 && d != 0) atomicAdd(&a.acc[ev.user], (unsigned long long)d);
     } else {
         const double dd = active ? __longlong_as_double(lbits) - __longlong_as_double(ev.init_bits) : 0.0;
@@ -405,8 +418,7 @@ __device__ __forceinline__ void accumulate_stats(const KArgs &a, const EvRec &ev
 // adjoint; the same integer accumulation as the statistics mean).
 __device__ __forceinline__ void accumulate_sum(const KArgs &a, const EvRec &ev, long long lbits, bool active) {
     long long d = active ? to_ticks(lbits, a.tick_q) - to_ticks(ev.init_bits, a.tick_q) : 0ll;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) d += __shfl_xor_sync(0xFFFFFFFFu, d, off);
+    d = warp_sum_ticks(d > 0 ? d : 0ll);  // realized >= earliest: d >= 0
     if ((threadIdx.x & 31) == 0 && d != 0) atomicAdd(&a.acc[ev.user], (unsigned long long)d);
 }
 

@@ -253,3 +253,35 @@ def test_reference_suite_bounds_and_known_answers(cuda):
     for res in sim.run_many(list(range(50))):
         assert res.realized[3] in (5.0 + 3.0 + 10 + 5.0 + d for d in (10, 20, 40, 50)) or res.realized[3] >= 22.0
         assert res.realized[5] == 100.0
+
+
+def test_unstaged_stage_tables_and_draws(cuda):
+    """An event with 3,000 predecessors: its stage's records exceed a staging buffer,
+    so they (and the empirical links' duration tables) are read from global memory.
+    Its draws still match the model at each link's (block, word), and the run is a
+    propagation of its own durations."""
+    from mcd_testlib import describe
+
+    n = 3000
+    kinds = [2, 4, 5, 3, 1]  # exp, emp abs, emp rel, gamma, constant
+    links = {(i, n): (i, 20.0 + i % 7, kinds[i % 5]) for i in range(n)}
+    flat = flat_from_lists([0.0] * (n + 1), links, [(n, [(i, i) for i in range(n)])], 1e12)
+    gen = SHARED_GEN[:5]
+    rc, info, _ = describe(flat, gen)
+    assert rc == 0 and info.n_stages >= 2
+    prop = propagator_from_flat(m, flat, gen)
+    seeds = np.arange(64, dtype=np.int64) * 31 + 7
+    real, dur, cause = prop.run_many_arrays(seeds)
+    r2, c2 = prop.propagate(dur)
+    assert np.array_equal(real.view(np.int64), r2.view(np.int64)) and np.array_equal(cause, c2)
+    block, word = prop.link_streams()
+    gmap = {g[1]: g for g in gen}
+    for l in range(0, n, 37):
+        g, base = gmap[kinds[l % 5]], float(flat["act_duration"][l])
+        if g[0].startswith("empirical"):
+            ref = PM.empirical_durations(seeds, l, base, g[2], g[3], g[0] == "empirical_relative",
+                                         block=block[l], word=max(0, word[l]))
+            assert np.array_equal(dur[:, l], ref), l
+        elif g[0] == "exponential":
+            ref = PM.exponential_durations(seeds, l, base, g[2], g[3], block=block[l], word=word[l])
+            np.testing.assert_allclose(dur[:, l], ref, rtol=2e-6)

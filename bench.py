@@ -577,7 +577,9 @@ def main():
     h = C.c_void_p(prop._handle())
     dev = torch.device("cuda", local)
     # per-rank disjoint seed ranges (weak scaling: every rank runs its own samples)
-    seeds = torch.arange(rank * S, (rank + 1) * S, dtype=torch.int64, device=dev)
+    from mc_dagprop_gb300 import replicas
+
+    seeds = torch.from_numpy(replicas.seed_range(rank, world, S)).to(dev)
     ld = S
     real = torch.empty((E, ld), dtype=torch.float64, device=dev)
     durs = torch.empty((L, ld), dtype=torch.float64, device=dev)
@@ -626,12 +628,9 @@ def main():
         raise RuntimeError(lib.mcd_last_error().decode())
     total_ms = t_start.elapsed_time(t_end)
     kernel_ms = [a.elapsed_time(b) for a, b in evs]
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = replicas.job_seconds(total_ms * 1e-3) * 1e3  # max over ranks
     units_per_step = S * L
-    value = units_per_step * world * args.steps / (total_ms * 1e-3)
+    value = replicas.job_throughput(units_per_step * args.steps, world, total_ms * 1e-3)
 
     # roofline of the dominant kernel (the only launch of a step)
     out_bytes = S * (8 * L + 8 * E + 4 * E)

@@ -19,8 +19,8 @@
 
 namespace mcd {
 
-// One CTA per tile of 32 samples; all warps split each stage's events, stages
-// from last to first.  Shared memory: [counts: window_slots x 32 uint32][stage
+// One CTA per tile of 32 samples; warps take each stage's events one at a time
+// from the stage's counter, stages from last to first.  Shared memory: [counts: window_slots x 32 uint32][stage
 // buffer 0][stage buffer 1][tables][2 mbarriers] -- the forward layout, whose
 // window rows are twice the size the counts need.
 __global__ void __launch_bounds__(768) k_adjoint(const KArgs a) {
@@ -29,15 +29,16 @@ __global__ void __launch_bounds__(768) k_adjoint(const KArgs a) {
     char *stage_buf0 = reinterpret_cast<char *>(smem + a.smem_stage_off);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + a.smem_bar_off);
     const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int NW = a.n_warps;
     const int64_t s = (int64_t)blockIdx.x * kTile + lane;
     const bool active = s < a.n;
     for (int i = threadIdx.x; i < a.window_slots * kTile; i += blockDim.x) cnt[i] = 0u;
+    int *stage_ctr = reinterpret_cast<int *>(bars + 2);
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        stage_ctr[0] = 0;
+        stage_ctr[1] = 0;
     }
     __syncthreads();
     const int NS = a.n_stages;
@@ -60,10 +61,17 @@ __global__ void __launch_bounds__(768) k_adjoint(const KArgs a) {
         const EvRec *sev = meta.y >= 0 ? reinterpret_cast<const EvRec *>(buf) : a.ev + meta.x;
         const PredRec *spred = meta.y >= 0 ? reinterpret_cast<const PredRec *>(buf + pred_boff)
                                            : a.pred + meta.z;
-        const int ib = __ldg(&a.wk_off[l * NW + warp]) - meta.x;
-        const int ie = __ldg(&a.wk_off[l * NW + warp + 1]) - meta.x;
-        for (int i = ib; i < ie; ++i) {
-            const EvRec ev = sev[i];
+        const int n_ev = meta.y >= 0 ? meta.y : -meta.y;
+        if (threadIdx.x == 0) stage_ctr[(j + 1) & 1] = 0;  // last used by stage j - 1, before the barrier
+        const uint32_t ctr = smem_u32(&stage_ctr[j & 1]);
+        // events one at a time from the stage's counter, the next taken ahead
+        int i_next = 0;
+        if (lane == 0) i_next = take_next(ctr);
+        i_next = __shfl_sync(0xFFFFFFFFu, i_next, 0);
+        while (i_next < n_ev) {
+            const int i = i_next;
+            if (lane == 0) i_next = take_next(ctr);
+            const EvRec ev = load_ev(sev + i);
             const int64_t o = (int64_t)ev.user * a.ld + s;
             const uint32_t code = active ? (uint32_t)a.adj_code[o] : kAdjNone;
             const float dfac = active ? a.adj_dfac[o] : 0.0f;
@@ -76,19 +84,27 @@ __global__ void __launch_bounds__(768) k_adjoint(const KArgs a) {
                 cnt[ev.slot * kTile + lane] = 0u;
             }
             if (!active) c = 0u;
-            long long ge = ((k == kAdjNone || clamped) ? (long long)c : 0ll) - (delayed ? 1ll : 0ll);
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) ge += __shfl_xor_sync(0xFFFFFFFFu, ge, off);
-            if (lane == 0 && ge != 0) atomicAdd(reinterpret_cast<unsigned long long *>(&a.grad_e[ev.user]),
-                                                (unsigned long long)ge);
-            if (k != kAdjNone && !clamped && c != 0u) {
-                const PredRec pr = spred[ev.pred_begin - meta.z + (int)k];
+            // this lane's share of d J / d earliest, >= -1: summed over the warp as ge + 1
+            const long long ge = ((k == kAdjNone || clamped) ? (long long)c : 0ll) - (delayed ? 1ll : 0ll);
+            const long long ge_sum = warp_sum_ticks(ge + 1) - 32;
+            if (lane == 0 && ge_sum != 0)
+                atomicAdd(reinterpret_cast<unsigned long long *>(&a.grad_e[ev.user]), (unsigned long long)ge_sum);
+            const bool wins = k != kAdjNone && !clamped && c != 0u;
+            const unsigned wmask = __ballot_sync(0xFFFFFFFFu, wins);
+            if (wins) {
+                const PredRec pr = load_pred(spred + (ev.pred_begin - meta.z + (int)k));
                 if (pr.src_slot >= 0) atomicAdd(&cnt[pr.src_slot * kTile + lane], c);
-                if (pr.link >= 0 && dfac != 0.0f) {
-                    const long long gl = __float2ll_rn((float)c * dfac * (float)(1 << kAdjDfacShift));
-                    atomicAdd(reinterpret_cast<unsigned long long *>(&a.grad_l[pr.link]), (unsigned long long)gl);
-                }
+                // lanes whose winner is the same predecessor add their link terms in one atomic
+                const long long gl = (pr.link >= 0 && dfac != 0.0f)
+                                         ? __float2ll_rn((float)c * dfac * (float)(1 << kAdjDfacShift))
+                                         : 0ll;
+                const unsigned grp = __match_any_sync(wmask, k);
+                long long sum = 0;
+                for (unsigned mm = grp; mm; mm &= mm - 1) sum += __shfl_sync(grp, gl, __ffs(mm) - 1);
+                if (lane == __ffs(grp) - 1 && pr.link >= 0 && sum != 0)
+                    atomicAdd(reinterpret_cast<unsigned long long *>(&a.grad_l[pr.link]), (unsigned long long)sum);
             }
+            i_next = __shfl_sync(0xFFFFFFFFu, i_next, 0);
         }
         __syncthreads();
         if (threadIdx.x == 0 && j + 2 < NS) stage_issue(a, l - 2, stage_buf0 + b * a.stage_bytes, &bars[b]);
@@ -111,10 +127,17 @@ __global__ void k_adjoint_finish(const long long *grad_e, const long long *grad_
     const double dn = (double)n;
     if (i < E && g_earliest) g_earliest[i] = (double)grad_e[i] / dn;
     if (i < L && g_base) g_base[i] = ldexp((double)grad_l[i], -kAdjDfacShift) / dn;
-    if (i == 0 && objective) {
-        double total = 0.0;
-        for (int e = 0; e < E; ++e) total += ldexp((double)(long long)acc[e], -q);
-        *objective = total / dn;
+    if (objective && blockIdx.x == gridDim.x - 1) {  // the objective: one block, a fixed summation order
+        __shared__ double part[256];
+        double t = 0.0;
+        for (int e = threadIdx.x; e < E; e += blockDim.x) t += ldexp((double)(long long)acc[e], -q);
+        part[threadIdx.x] = t;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) *objective = part[0] / dn;
     }
 }
 

@@ -532,7 +532,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--samples", type=int, default=19456)
-    ap.add_argument("--e2e-samples", type=int, default=4864)
+    ap.add_argument("--e2e-samples", type=int, default=7296)
     ap.add_argument("--layers", type=int, default=2000)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--workload", default="single", choices=["single", "batched", "gradient", "serving", "analytic"])
@@ -648,11 +648,12 @@ def main():
     e2e = None
     if rank == 0:
         n2 = args.e2e_samples
-        try:  # pinned host outputs: at most a quarter of the available host memory
+        try:  # pinned host outputs: at most a third of the available host memory
             with open("/proc/meminfo") as f:
                 avail = int(next(ln for ln in f if ln.startswith("MemAvailable")).split()[1]) * 1024
-            while n2 > 32 and n2 * (8 + 12 * E + 8 * L) > avail // 4:
-                n2 = n2 // 64 * 32
+            fit = avail // 3 // (8 + 12 * E + 8 * L)
+            if n2 > fit:  # whole half-wave chunks (2,432 samples on 152 SMs) where possible
+                n2 = max(32, fit // 2432 * 2432 if fit >= 2432 else fit // 32 * 32)
         except (OSError, StopIteration, ValueError):
             pass
         bufs = []

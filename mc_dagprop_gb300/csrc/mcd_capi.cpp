@@ -101,16 +101,15 @@ void check_device_error(mcd_dag *g) {
 namespace {
 
 // Samples per chunk for the host-buffer entry points, a multiple of 32, and the
-// number of chunk buffer sets (sample-minor rows + sample-major rows): one when
-// all n samples fit one chunk, else two, used alternately by the handle's two
-// streams.  A chunk is one launch in which every 32-sample tile walks the whole
-// DAG at one CTA per SM, so a chunk of half a wave of tiles leaves the other
-// half of the SMs to the previous chunk's transposes and copies: the host
-// transfer, the bound of these entry points, overlaps the next chunk's sampling.
-// Chunks also stay within a workspace of a quarter of the device memory not
-// otherwise in use (at most 32 GiB).
-int64_t host_chunk(const mcd_dag *g, int64_t n, int *sets) {
-    const double per_sample = 2.0 * (12.0 * g->h.E + 8.0 * g->h.L) + 8.0;
+// number of chunk buffer sets: one when all n samples fit one chunk, else two,
+// used alternately.  A chunk is one launch in which every 32-sample tile walks
+// the whole DAG at one CTA per SM; half a wave of tiles leaves the other half of
+// the SMs to the transfer of the previous chunk.  staged: some host buffer is
+// pageable, so its rows go through a sample-major device copy as well.  Chunks
+// stay within a workspace of a quarter of the device memory not otherwise in use
+// (at most 32 GiB).
+int64_t host_chunk(const mcd_dag *g, int64_t n, bool staged, int *sets) {
+    const double per_sample = (staged ? 2.0 : 1.0) * (12.0 * g->h.E + 8.0 * g->h.L) + 8.0;
     size_t free_b = 0, total_b = 0;
     cuda_check(cudaMemGetInfo(&free_b, &total_b), "device memory query");
     int sms = 0;
@@ -127,6 +126,43 @@ int64_t host_chunk(const mcd_dag *g, int64_t n, int *sets) {
     const int64_t c = std::min<int64_t>(half_wave, (int64_t)(budget / (2.0 * std::max(per_sample, 1.0))));
     return std::max<int64_t>(32, c / 32 * 32);
 }
+
+// The two-stream chunk pipeline of the host-buffer entry points.  The handle's
+// first stream computes chunk after chunk (uploads of given inputs, sampling and
+// propagation into a buffer set); the second moves each computed chunk to the
+// host (transposes, and copies for pageable buffers).  Chunk k's computation
+// waits only until the transfer of chunk k - sets has released its buffer set,
+// so after the first chunk the host link -- the bound -- does not wait for the
+// sampler.
+struct ChunkPipe {
+    cudaStream_t compute, transfer;
+    cudaEvent_t computed[2] = {}, moved[2] = {};
+    int sets;
+    ChunkPipe(mcd_dag *g, int sets_) : compute(g->stream[0]), transfer(g->stream[1]), sets(sets_) {
+        for (int k = 0; k < 2; ++k) {
+            cuda_check(cudaEventCreateWithFlags(&computed[k], cudaEventDisableTiming), "event create");
+            cuda_check(cudaEventCreateWithFlags(&moved[k], cudaEventDisableTiming), "event create");
+        }
+    }
+    ~ChunkPipe() {
+        for (int k = 0; k < 2; ++k) {
+            if (computed[k]) cudaEventDestroy(computed[k]);
+            if (moved[k]) cudaEventDestroy(moved[k]);
+        }
+    }
+    ChunkPipe(const ChunkPipe &) = delete;
+    ChunkPipe &operator=(const ChunkPipe &) = delete;
+    // before chunk idx's computation: its buffer set is free again
+    void begin_compute(int64_t idx) {
+        if (idx >= sets) cuda_check(cudaStreamWaitEvent(compute, moved[idx % sets], 0), "stream wait");
+    }
+    // after it: the transfer stream takes the chunk over
+    void begin_transfer(int64_t idx) {
+        cuda_check(cudaEventRecord(computed[idx % sets], compute), "event record");
+        cuda_check(cudaStreamWaitEvent(transfer, computed[idx % sets], 0), "stream wait");
+    }
+    void end_transfer(int64_t idx) { cuda_check(cudaEventRecord(moved[idx % sets], transfer), "event record"); }
+};
 
 // The device-side address of a host buffer a kernel may access directly
 // (pinned or registered memory, mapped under unified addressing), or null when
@@ -152,12 +188,12 @@ struct ChunkBufs {
 };
 
 // Carves `sets` chunk buffer sets of C samples out of the workspace (a single
-// set serves both slots).
-void carve(mcd_dag *g, int64_t C, int sets, ChunkBufs cb[2]) {
+// set serves both slots); the sample-major rows only when staged.
+void carve(mcd_dag *g, int64_t C, int sets, bool staged, ChunkBufs cb[2]) {
     const size_t E = (size_t)g->h.E, L = (size_t)g->h.L;
     const size_t sz_seed = align_up((size_t)C * 8, 256), sz_re = align_up(E * (size_t)C * 8, 256),
                  sz_du = align_up(L * (size_t)C * 8, 256), sz_ca = align_up(E * (size_t)C * 4, 256);
-    const size_t per = sz_seed + 2 * (sz_re + sz_du + sz_ca);
+    const size_t per = sz_seed + (staged ? 2 : 1) * (sz_re + sz_du + sz_ca);
     ensure_ws(g, (size_t)sets * per);
     for (int k = 0; k < 2; ++k) {
         char *p = g->ws + (size_t)(k % sets) * per;
@@ -169,11 +205,16 @@ void carve(mcd_dag *g, int64_t C, int sets, ChunkBufs cb[2]) {
         p += sz_du;
         cb[k].cause_minor = (int32_t *)p;
         p += sz_ca;
-        cb[k].real_major = (double *)p;
-        p += sz_re;
-        cb[k].dur_major = (double *)p;
-        p += sz_du;
-        cb[k].cause_major = (int32_t *)p;
+        if (staged) {
+            cb[k].real_major = (double *)p;
+            p += sz_re;
+            cb[k].dur_major = (double *)p;
+            p += sz_du;
+            cb[k].cause_major = (int32_t *)p;
+        } else {
+            cb[k].real_major = cb[k].dur_major = nullptr;
+            cb[k].cause_major = nullptr;
+        }
     }
 }
 
@@ -427,59 +468,56 @@ int mcd_run_many_host(mcd_dag *g, const int64_t *seeds, int64_t n, double *reali
         if (!seeds) throw McdError(MCD_ERR_INVALID, "null seeds");
         cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
         const int64_t E = g->h.E, L = g->h.L;
-        int sets = 1;
-        const int64_t C = host_chunk(g, n, &sets);
-        ChunkBufs cb[2];
-        carve(g, C, sets, cb);
         double *real_dv = device_view(realized), *dur_dv = device_view(durations);
         int32_t *cause_dv = device_view(cause);
-        // chunk k waits for chunk k - 2 (same buffers, same stream); the two streams
-        // start together, after work already queued on the handle's first stream
-        cudaEvent_t start;
-        cuda_check(cudaEventCreateWithFlags(&start, cudaEventDisableTiming), "event create");
-        cuda_check(cudaEventRecord(start, g->stream[0]), "event record");
-        cuda_check(cudaStreamWaitEvent(g->stream[1], start, 0), "stream wait");
-        cudaEventDestroy(start);
+        const bool staged = (realized && !real_dv) || (durations && !dur_dv) || (cause && !cause_dv);
+        int sets = 1;
+        const int64_t C = host_chunk(g, n, staged, &sets);
+        ChunkBufs cb[2];
+        carve(g, C, sets, staged, cb);
+        ChunkPipe pipe(g, sets);
         int64_t idx = 0;
         for (int64_t off = 0; off < n; off += C, ++idx) {
-            const int k = (int)(idx & 1);
-            cudaStream_t st = g->stream[k];
+            const ChunkBufs &b = cb[idx & 1];
             const int64_t m = std::min(C, n - off);
-            cuda_check(cudaMemcpyAsync(cb[k].seeds, seeds + off, (size_t)m * 8, cudaMemcpyHostToDevice, st),
+            pipe.begin_compute(idx);
+            cuda_check(cudaMemcpyAsync(b.seeds, seeds + off, (size_t)m * 8, cudaMemcpyHostToDevice, pipe.compute),
                        "seed upload");
             KArgs a = base_args(g);
-            a.seeds = cb[k].seeds;
+            a.seeds = b.seeds;
             a.n = m;
             a.ld = C;
-            a.realized = cb[k].real_minor;  // always: also the spill rows of a global window
-            a.durations = durations ? cb[k].dur_minor : nullptr;
-            a.cause = cause ? cb[k].cause_minor : nullptr;
-            cuda_check(launch_propagate(a, false, g->h.win_smem, false, st), "propagate launch");
+            a.realized = b.real_minor;  // always: also the spill rows of a global window
+            a.durations = durations ? b.dur_minor : nullptr;
+            a.cause = cause ? b.cause_minor : nullptr;
+            cuda_check(launch_propagate(a, false, g->h.win_smem, false, pipe.compute), "propagate launch");
+            pipe.begin_transfer(idx);
+            cudaStream_t st = pipe.transfer;
             if (real_dv) {
-                cuda_check(launch_transpose_f64(cb[k].real_minor, C, real_dv + off * E, E, E, m, st), "transpose");
+                cuda_check(launch_transpose_f64(b.real_minor, C, real_dv + off * E, E, E, m, st), "transpose");
             } else if (realized) {
-                cuda_check(launch_transpose_f64(cb[k].real_minor, C, cb[k].real_major, E, E, m, st), "transpose");
-                cuda_check(cudaMemcpyAsync(realized + off * E, cb[k].real_major, (size_t)(m * E) * 8,
+                cuda_check(launch_transpose_f64(b.real_minor, C, b.real_major, E, E, m, st), "transpose");
+                cuda_check(cudaMemcpyAsync(realized + off * E, b.real_major, (size_t)(m * E) * 8,
                                            cudaMemcpyDeviceToHost, st),
                            "realized download");
             }
             if (dur_dv) {
-                cuda_check(launch_transpose_f64(cb[k].dur_minor, C, dur_dv + off * L, L, L, m, st), "transpose");
+                cuda_check(launch_transpose_f64(b.dur_minor, C, dur_dv + off * L, L, L, m, st), "transpose");
             } else if (durations) {
-                cuda_check(launch_transpose_f64(cb[k].dur_minor, C, cb[k].dur_major, L, L, m, st), "transpose");
-                cuda_check(cudaMemcpyAsync(durations + off * L, cb[k].dur_major, (size_t)(m * L) * 8,
+                cuda_check(launch_transpose_f64(b.dur_minor, C, b.dur_major, L, L, m, st), "transpose");
+                cuda_check(cudaMemcpyAsync(durations + off * L, b.dur_major, (size_t)(m * L) * 8,
                                            cudaMemcpyDeviceToHost, st),
                            "durations download");
             }
             if (cause_dv) {
-                cuda_check(launch_transpose_i32(cb[k].cause_minor, C, cause_dv + off * E, E, E, m, st), "transpose");
+                cuda_check(launch_transpose_i32(b.cause_minor, C, cause_dv + off * E, E, E, m, st), "transpose");
             } else if (cause) {
-                cuda_check(launch_transpose_i32(cb[k].cause_minor, C, cb[k].cause_major, E, E, m, st),
-                           "transpose");
-                cuda_check(cudaMemcpyAsync(cause + off * E, cb[k].cause_major, (size_t)(m * E) * 4,
+                cuda_check(launch_transpose_i32(b.cause_minor, C, b.cause_major, E, E, m, st), "transpose");
+                cuda_check(cudaMemcpyAsync(cause + off * E, b.cause_major, (size_t)(m * E) * 4,
                                            cudaMemcpyDeviceToHost, st),
                            "cause download");
             }
+            pipe.end_transfer(idx);
         }
         check_device_error(g);
     });
@@ -493,56 +531,56 @@ int mcd_propagate_host(mcd_dag *g, const double *durations, int64_t n, double *r
         if (!durations && g->h.L > 0) throw McdError(MCD_ERR_INVALID, "null durations");
         cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
         const int64_t E = g->h.E, L = g->h.L;
-        int sets = 1;
-        const int64_t C = host_chunk(g, n, &sets);
-        ChunkBufs cb[2];
-        carve(g, C, sets, cb);
         const double *dur_dv = device_view(durations);
         double *real_dv = device_view(realized);
         int32_t *cause_dv = device_view(cause);
-        cudaEvent_t start;
-        cuda_check(cudaEventCreateWithFlags(&start, cudaEventDisableTiming), "event create");
-        cuda_check(cudaEventRecord(start, g->stream[0]), "event record");
-        cuda_check(cudaStreamWaitEvent(g->stream[1], start, 0), "stream wait");
-        cudaEventDestroy(start);
+        const bool staged = (L > 0 && !dur_dv) || (realized && !real_dv) || (cause && !cause_dv);
+        int sets = 1;
+        const int64_t C = host_chunk(g, n, staged, &sets);
+        ChunkBufs cb[2];
+        carve(g, C, sets, staged, cb);
+        ChunkPipe pipe(g, sets);
         int64_t idx = 0;
         for (int64_t off = 0; off < n; off += C, ++idx) {
-            const int k = (int)(idx & 1);
-            cudaStream_t st = g->stream[k];
+            const ChunkBufs &b = cb[idx & 1];
             const int64_t m = std::min(C, n - off);
+            pipe.begin_compute(idx);
+            cudaStream_t cs = pipe.compute;
             if (L > 0 && dur_dv) {
-                cuda_check(launch_transpose_f64(dur_dv + off * L, L, cb[k].dur_minor, C, m, L, st), "transpose");
+                cuda_check(launch_transpose_f64(dur_dv + off * L, L, b.dur_minor, C, m, L, cs), "transpose");
             } else if (L > 0) {
-                cuda_check(cudaMemcpyAsync(cb[k].dur_major, durations + off * L, (size_t)(m * L) * 8,
-                                           cudaMemcpyHostToDevice, st),
+                cuda_check(cudaMemcpyAsync(b.dur_major, durations + off * L, (size_t)(m * L) * 8,
+                                           cudaMemcpyHostToDevice, cs),
                            "durations upload");
-                cuda_check(launch_transpose_f64(cb[k].dur_major, L, cb[k].dur_minor, C, m, L, st), "transpose");
+                cuda_check(launch_transpose_f64(b.dur_major, L, b.dur_minor, C, m, L, cs), "transpose");
             }
             KArgs a = base_args(g);
             a.n = m;
             a.ld = C;
-            a.realized = cb[k].real_minor;
-            a.cause = cause ? cb[k].cause_minor : nullptr;
-            a.dur_in = cb[k].dur_minor;
+            a.realized = b.real_minor;
+            a.cause = cause ? b.cause_minor : nullptr;
+            a.dur_in = b.dur_minor;
             a.ld_in = C;
-            cuda_check(launch_propagate(a, true, g->h.win_smem, false, st), "propagate launch");
+            cuda_check(launch_propagate(a, true, g->h.win_smem, false, cs), "propagate launch");
+            pipe.begin_transfer(idx);
+            cudaStream_t st = pipe.transfer;
             if (real_dv) {
-                cuda_check(launch_transpose_f64(cb[k].real_minor, C, real_dv + off * E, E, E, m, st), "transpose");
+                cuda_check(launch_transpose_f64(b.real_minor, C, real_dv + off * E, E, E, m, st), "transpose");
             } else if (realized) {
-                cuda_check(launch_transpose_f64(cb[k].real_minor, C, cb[k].real_major, E, E, m, st), "transpose");
-                cuda_check(cudaMemcpyAsync(realized + off * E, cb[k].real_major, (size_t)(m * E) * 8,
+                cuda_check(launch_transpose_f64(b.real_minor, C, b.real_major, E, E, m, st), "transpose");
+                cuda_check(cudaMemcpyAsync(realized + off * E, b.real_major, (size_t)(m * E) * 8,
                                            cudaMemcpyDeviceToHost, st),
                            "realized download");
             }
             if (cause_dv) {
-                cuda_check(launch_transpose_i32(cb[k].cause_minor, C, cause_dv + off * E, E, E, m, st), "transpose");
+                cuda_check(launch_transpose_i32(b.cause_minor, C, cause_dv + off * E, E, E, m, st), "transpose");
             } else if (cause) {
-                cuda_check(launch_transpose_i32(cb[k].cause_minor, C, cb[k].cause_major, E, E, m, st),
-                           "transpose");
-                cuda_check(cudaMemcpyAsync(cause + off * E, cb[k].cause_major, (size_t)(m * E) * 4,
+                cuda_check(launch_transpose_i32(b.cause_minor, C, b.cause_major, E, E, m, st), "transpose");
+                cuda_check(cudaMemcpyAsync(cause + off * E, b.cause_major, (size_t)(m * E) * 4,
                                            cudaMemcpyDeviceToHost, st),
                            "cause download");
             }
+            pipe.end_transfer(idx);
         }
         check_device_error(g);
     });

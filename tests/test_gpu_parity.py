@@ -249,3 +249,40 @@ def test_host_paths_pinned_and_pageable_agree(cuda):
     assert_bits_equal(r2, real[-700:])
     assert_bits_equal(d2, dur[-700:])
     assert np.array_equal(c2, cause[-700:])
+
+
+def test_host_paths_mixed_pinned_pageable_and_absent_outputs(cuda):
+    """One call with a pinned, a pageable and an absent output (the chunk buffers then
+    hold sample-major staging rows too), over several chunks of the two-stream
+    pipeline, gives the bits of the all-pageable call."""
+    flat, gen = W.config1(seed=6, n_layers=16, width=40)
+    prop = propagator_from_flat(m, flat, gen)
+    h = C.c_void_p(prop._handle())
+    E, L = prop.node_count(), prop.activity_count()
+    n = 32 * 152 * 2 + 77  # five half-wave chunks on a 152-SM part
+    seeds = np.arange(100, 100 + n, dtype=np.int64)
+    real = np.empty((n, E)); dur = np.empty((n, L)); cause = np.empty((n, E), np.int32)
+    assert lib().mcd_run_many_host(h, ptr(seeds), n, ptr(real), ptr(dur), ptr(cause)) == MCD_OK, last_error()
+    bufs = [_pinned(n * E * 8), _pinned(n * L * 8)]
+    try:
+        pr = np.ctypeslib.as_array(C.cast(bufs[0], C.POINTER(C.c_double)), (n, E))
+        pd = np.ctypeslib.as_array(C.cast(bufs[1], C.POINTER(C.c_double)), (n, L))
+        pr.fill(-1.0)
+        d_pageable = np.full((n, L), -1.0)
+        assert lib().mcd_run_many_host(h, ptr(seeds), n, bufs[0], ptr(d_pageable), None) == MCD_OK, last_error()
+        assert_bits_equal(pr, real)
+        assert_bits_equal(d_pageable, dur)
+        # given pageable durations into a pinned realized row set and a pageable cause
+        pd[:] = dur
+        pr.fill(-1.0)
+        c_pageable = np.full((n, E), -9, np.int32)
+        assert lib().mcd_propagate_host(h, ptr(dur), n, bufs[0], ptr(c_pageable)) == MCD_OK, last_error()
+        assert_bits_equal(pr, real)
+        assert np.array_equal(c_pageable, cause)
+        # given pinned durations into pageable outputs
+        r_pageable = np.full((n, E), -1.0)
+        assert lib().mcd_propagate_host(h, bufs[1], n, ptr(r_pageable), None) == MCD_OK, last_error()
+        assert_bits_equal(r_pageable, real)
+    finally:
+        for b in bufs:
+            lib().mcd_host_free(b)

@@ -47,7 +47,7 @@
 extern "C" {
 #endif
 
-#define MCD_ABI_VERSION 1
+#define MCD_ABI_VERSION 2
 
 /* Status codes. */
 #define MCD_OK 0
@@ -115,18 +115,26 @@ typedef struct mcd_dag_info {
     int32_t smem_bytes;        /* shared memory per CTA */
     int32_t positive;          /* 1: all times non-negative and finite (cheaper comparisons) */
     int32_t tables_in_smem;    /* 1: distribution tables held in shared memory */
+    int32_t cache_hit;         /* 1: the compiled records are shared with an earlier live
+                                  handle of identical inputs (compiled-DAG cache) */
 } mcd_dag_info;
 
 /* Simulator::Simulator: validates, compiles to level-ordered CSR and uploads to
  * the current CUDA device.  The generator is copied; both inputs may be freed
- * afterwards.  Each handle owns one CUDA stream; a handle is not reentrant,
- * separate handles run concurrently. */
+ * afterwards.  Each handle owns its CUDA streams; a handle is not reentrant,
+ * separate handles run concurrently.  A handle created from inputs identical to
+ * those of a live handle on the same device (byte for byte: arrays, generator,
+ * n_warps) shares that handle's compiled, read-only device records instead of
+ * compiling again (the compiled-DAG cache; mcd_dag_options.no_cache opts out). */
 int mcd_dag_create(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag **out);
 /* Compile options (the same call with explicit choices). */
 #define MCD_WARPS_BATCH_CLASS (-1)
 typedef struct mcd_dag_options {
     int32_t n_warps; /* warps per CTA, 1..24; 0 = chosen from the DAG's level width;
                         MCD_WARPS_BATCH_CLASS = chosen, then rounded up to 2, 4, 8, 12 or 24 */
+    int32_t no_cache; /* 0: share the compiled records of a live handle created from
+                         identical inputs (same arrays, generator, n_warps and device);
+                         1: compile a private copy */
 } mcd_dag_options;
 int mcd_dag_create_ex(const mcd_dag_desc *desc, const mcd_generator *gen, const mcd_dag_options *opts,
                       mcd_dag **out);

@@ -1,15 +1,20 @@
 // mcd_capi.cpp -- the extern "C" entry points of include/mc_dagprop_gb300.h.
 //
-// Owns the compiled, device-resident DAG (one allocation), the handle's two CUDA
-// streams and a workspace for the host-buffer entry points, which run in
+// Owns the compiled, device-resident DAG images (one allocation each, shared by
+// handles of identical inputs through a content-keyed cache), each handle's two
+// CUDA streams and a workspace for the host-buffer entry points, which run in
 // chunks: copy seeds in, run the fused kernel into sample-minor rows, transpose
-// to the reference's sample-major SimResult layout, copy out -- two chunks in
-// flight on alternating streams so copies overlap compute.
+// to the reference's sample-major SimResult layout, copy out -- a compute
+// stream and a transfer stream, so the host link overlaps the sampling.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 
 #include "mcd_handle.hpp"
 
@@ -97,6 +102,15 @@ void check_device_error(mcd_dag *g) {
 }
 
 }  // namespace mcd
+
+DagImage::~DagImage() {
+    if (!dmem) return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(device);
+    cudaFree(dmem);
+    cudaSetDevice(prev);
+}
 
 namespace {
 
@@ -218,6 +232,154 @@ void carve(mcd_dag *g, int64_t C, int sets, bool staged, ChunkBufs cb[2]) {
     }
 }
 
+// ---- the compiled-DAG cache
+// Handles whose inputs (DAG arrays, generator, warps, device) are identical share
+// one device image.  The key is the inputs serialized byte for byte, in the order
+// the compiler reads them; a 64-bit hash picks the bucket and a full comparison
+// decides, so two different inputs never share an image.  The cache holds weak
+// references: an image lives as long as a handle uses it.
+
+void put_bytes(std::vector<unsigned char> &k, const void *p, size_t n) {
+    if (!n) return;
+    const size_t o = k.size();
+    k.resize(o + n);
+    std::memcpy(k.data() + o, p, n);
+}
+template <typename T>
+void put(std::vector<unsigned char> &k, const T &v) {
+    put_bytes(k, &v, sizeof(T));
+}
+
+// Serializes what compile_dag reads; false (no caching) where the arrays are not
+// well-formed enough to read safely -- compile_dag then reports the error.
+bool image_key(const mcd_dag_desc &d, const mcd_generator &gen, int32_t n_warps, int device,
+               std::vector<unsigned char> &k) {
+    if (d.n_events < 0 || d.n_activities < 0 || d.n_targets < 0) return false;
+    if ((d.n_events && !d.earliest) ||
+        (d.n_activities && (!d.act_idx || !d.act_duration || !d.act_type)) ||
+        (d.n_targets && (!d.target || !d.pred_offsets)))
+        return false;
+    const size_t E = (size_t)d.n_events, A = (size_t)d.n_activities, T = (size_t)d.n_targets;
+    int64_t P = 0;
+    for (size_t t = 0; t < T; ++t) {
+        const int64_t b = d.pred_offsets[t], e = d.pred_offsets[t + 1];
+        if (b < 0 || e < b) return false;
+        P += e - b;
+    }
+    if (P > 0 && (!d.pred_src || !d.pred_act)) return false;
+    size_t gen_bytes = 0;
+    for (const DistSpec &sp : gen.dists) gen_bytes += 48 + 8 * (sp.values.size() + sp.weights.size());
+    k.clear();
+    k.reserve(64 + E * 8 + A * 16 + T * 12 + (size_t)P * 8 + gen_bytes);
+    put(k, (int32_t)0x4D434401);  // key format
+    put(k, device);
+    put(k, n_warps);
+    for (const char *var : {"MCD_NO_SMEM_WINDOW", "MCD_WARPS"}) {  // compile_dag's environment overrides
+        const char *v = std::getenv(var);
+        put(k, (int64_t)(v ? (int64_t)std::strlen(v) : -1));
+        if (v) put_bytes(k, v, std::strlen(v));
+    }
+    put(k, d.n_events);
+    put_bytes(k, d.earliest, E * 8);
+    put(k, d.n_activities);
+    put_bytes(k, d.act_idx, A * 4);
+    put_bytes(k, d.act_duration, A * 8);
+    put_bytes(k, d.act_type, A * 4);
+    put(k, d.n_targets);
+    put_bytes(k, d.target, T * 4);
+    if (T) put_bytes(k, d.pred_offsets, (T + 1) * 8);
+    for (size_t t = 0; t < T; ++t) {
+        const int64_t b = d.pred_offsets[t], e = d.pred_offsets[t + 1];
+        put_bytes(k, d.pred_src + b, (size_t)(e - b) * 4);
+        put_bytes(k, d.pred_act + b, (size_t)(e - b) * 4);
+    }
+    put(k, d.max_delay);
+    put(k, gen.seed);
+    put(k, (int64_t)gen.dists.size());
+    for (const DistSpec &sp : gen.dists) {
+        put(k, sp.type);
+        put(k, sp.kind);
+        put(k, sp.p0);
+        put(k, sp.p1);
+        put(k, sp.p2);
+        put(k, (int64_t)sp.values.size());
+        put_bytes(k, sp.values.data(), sp.values.size() * 8);
+        put(k, (int64_t)sp.weights.size());
+        put_bytes(k, sp.weights.data(), sp.weights.size() * 8);
+    }
+    return true;
+}
+
+// 64-bit multiply-xorshift hash over 8-byte words (the tail zero-padded).
+uint64_t hash_bytes(const std::vector<unsigned char> &k) {
+    uint64_t h = 0x9E3779B97F4A7C15ull ^ (uint64_t)k.size();
+    const size_t nw = k.size() / 8;
+    for (size_t i = 0; i < nw; ++i) {
+        uint64_t w;
+        std::memcpy(&w, k.data() + 8 * i, 8);
+        h = (h ^ w) * 0xFF51AFD7ED558CCDull;
+        h ^= h >> 32;
+    }
+    uint64_t tail = 0;
+    std::memcpy(&tail, k.data() + 8 * nw, k.size() - 8 * nw);
+    h = (h ^ tail) * 0xC4CEB9FE1A85EC53ull;
+    return h ^ (h >> 29);
+}
+
+std::mutex g_cache_mu;
+std::unordered_multimap<uint64_t, std::weak_ptr<const DagImage>> g_cache;
+
+std::shared_ptr<const DagImage> cache_find(uint64_t hash, const std::vector<unsigned char> &key) {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    auto range = g_cache.equal_range(hash);
+    for (auto it = range.first; it != range.second; ++it)
+        if (auto img = it->second.lock())
+            if (img->key == key) return img;
+    return nullptr;
+}
+
+void cache_insert(uint64_t hash, const std::shared_ptr<const DagImage> &img) {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    for (auto it = g_cache.begin(); it != g_cache.end();)  // drop the entries of freed images
+        it = it->second.expired() ? g_cache.erase(it) : std::next(it);
+    g_cache.emplace(hash, img);
+}
+
+// One device allocation holding the compiled records, uploaded from the host copies.
+void upload_image(DagImage &im) {
+    const HostDag &h = im.h;
+    const size_t s_ev = align_up(h.ev.size() * sizeof(EvRec), 256),
+                 s_pred = align_up(h.pred.size() * sizeof(PredRec), 256),
+                 s_aux = align_up(h.aux.size() * sizeof(LinkRec), 256),
+                 s_tables = align_up(tables_bytes(h), 256),
+                 s_vals = align_up(h.vals.size() * sizeof(double), 256),
+                 s_wk = align_up(h.wk_off.size() * sizeof(int32_t), 256),
+                 s_meta = align_up(h.stage_meta.size() * sizeof(int32_t), 256),
+                 s_times = align_up(h.earliest.size() * sizeof(double), 256);
+    im.dbytes = s_ev + s_pred + s_aux + s_tables + s_vals + s_wk + s_meta + 2 * s_times;
+    cuda_check(cudaMalloc(&im.dmem, std::max<size_t>(im.dbytes, 256)), "compiled DAG allocation");
+    char *p = im.dmem;
+    auto place = [&](auto *&dst, const auto &vec, size_t sz) {
+        dst = reinterpret_cast<std::remove_reference_t<decltype(dst)>>(p);
+        if (!vec.empty())
+            cuda_check(cudaMemcpy(p, vec.data(), vec.size() * sizeof(vec[0]), cudaMemcpyHostToDevice),
+                       "compiled DAG upload");
+        p += sz;
+    };
+    place(im.d_ev, h.ev, s_ev);
+    place(im.d_pred, h.pred, s_pred);
+    place(im.d_aux, h.aux, s_aux);
+    {
+        const std::vector<unsigned char> tb = tables_block(h);
+        place(im.d_dist, tb, s_tables);
+    }
+    place(im.d_vals, h.vals, s_vals);
+    place(im.d_wk, h.wk_off, s_wk);
+    place(im.d_stage_meta, h.stage_meta, s_meta);
+    place(im.d_earliest, h.earliest, s_times);
+    place(im.d_ub, h.ub, s_times);
+}
+
 }  // namespace
 
 extern "C" {
@@ -292,43 +454,35 @@ int mcd_dag_create_ex(const mcd_dag_desc *desc, const mcd_generator *gen, const 
         const int32_t nw = opts ? opts->n_warps : 0;
         if (nw < kBatchClassWarps || nw > kMaxWarps)
             throw McdError(MCD_ERR_INVALID, "n_warps must be -1 (batch class), 0 (automatic) or 1..24");
-        g = new mcd_dag();
-        compile_dag(*desc, *gen, g->h, nw);
-        cuda_check(cudaGetDevice(&g->device), "cudaGetDevice");
+        const bool use_cache = !(opts && opts->no_cache);
+        int dev = -1;
+        if (cudaGetDevice(&dev) != cudaSuccess) {  // reported after validation, as before
+            (void)cudaGetLastError();
+            dev = -1;
+        }
+        std::vector<unsigned char> key;
+        uint64_t hash = 0;
+        std::shared_ptr<const DagImage> img;
+        bool hit = false;
+        if (use_cache && dev >= 0 && image_key(*desc, *gen, nw, dev, key)) {
+            hash = hash_bytes(key);
+            img = cache_find(hash, key);
+            hit = img != nullptr;
+        }
+        if (!img) {
+            auto fresh = std::make_shared<DagImage>();
+            compile_dag(*desc, *gen, fresh->h, nw);
+            cuda_check(cudaGetDevice(&fresh->device), "cudaGetDevice");
+            upload_image(*fresh);
+            if (!key.empty()) fresh->key = std::move(key);
+            img = fresh;
+            if (!img->key.empty()) cache_insert(hash, img);
+        }
+        g = new mcd_dag(img);
+        g->cache_hit = hit;
         for (int k = 0; k < 2; ++k)
             cuda_check(cudaStreamCreateWithFlags(&g->stream[k], cudaStreamNonBlocking), "stream create");
-        const HostDag &h = g->h;
-        const size_t s_ev = align_up(h.ev.size() * sizeof(EvRec), 256),
-                     s_pred = align_up(h.pred.size() * sizeof(PredRec), 256),
-                     s_aux = align_up(h.aux.size() * sizeof(LinkRec), 256),
-                     s_tables = align_up(tables_bytes(h), 256),
-                     s_vals = align_up(h.vals.size() * sizeof(double), 256),
-                     s_wk = align_up(h.wk_off.size() * sizeof(int32_t), 256),
-                     s_meta = align_up(h.stage_meta.size() * sizeof(int32_t), 256),
-                     s_times = align_up(h.earliest.size() * sizeof(double), 256), s_err = 256;
-        g->dbytes = s_ev + s_pred + s_aux + s_tables + s_vals + s_wk + s_meta + 2 * s_times + s_err;
-        cuda_check(cudaMalloc(&g->dmem, g->dbytes), "compiled DAG allocation");
-        char *p = g->dmem;
-        auto place = [&](auto *&dst, const auto &vec, size_t sz) {
-            dst = reinterpret_cast<std::remove_reference_t<decltype(dst)>>(p);
-            if (!vec.empty())
-                cuda_check(cudaMemcpy(p, vec.data(), vec.size() * sizeof(vec[0]), cudaMemcpyHostToDevice),
-                           "compiled DAG upload");
-            p += sz;
-        };
-        place(g->d_ev, h.ev, s_ev);
-        place(g->d_pred, h.pred, s_pred);
-        place(g->d_aux, h.aux, s_aux);
-        {
-            const std::vector<unsigned char> tb = tables_block(h);
-            place(g->d_dist, tb, s_tables);
-        }
-        place(g->d_vals, h.vals, s_vals);
-        place(g->d_wk, h.wk_off, s_wk);
-        place(g->d_stage_meta, h.stage_meta, s_meta);
-        place(g->d_earliest, h.earliest, s_times);
-        place(g->d_ub, h.ub, s_times);
-        g->d_err = reinterpret_cast<int32_t *>(p);
+        cuda_check(cudaMalloc(&g->d_err, 256), "error flag allocation");
         cuda_check(cudaMemset(g->d_err, 0, sizeof(int32_t)), "error flag init");
         *out = g;
     });
@@ -351,9 +505,9 @@ void mcd_dag_destroy(mcd_dag *g) {
             cudaStreamDestroy(g->stream[k]);
         }
     if (g->ws) cudaFree(g->ws);
-    if (g->dmem) cudaFree(g->dmem);
+    if (g->d_err) cudaFree(g->d_err);
     cudaSetDevice(prev);
-    delete g;
+    delete g;  // the image goes with its last handle
 }
 
 int32_t mcd_dag_node_count(const mcd_dag *g) { return g ? g->h.E : -1; }
@@ -381,6 +535,7 @@ int mcd_dag_get_info(const mcd_dag *g, mcd_dag_info *info) {
         fill_info(g->h, info);
         info->device = g->device;
         info->device_bytes = (int64_t)g->dbytes;
+        info->cache_hit = g->cache_hit ? 1 : 0;
     });
 }
 

@@ -349,6 +349,7 @@ class Propagator {
         d["smem_bytes"] = i.smem_bytes;
         d["positive"] = (bool)i.positive;
         d["tables_in_smem"] = (bool)i.tables_in_smem;
+        d["cache_hit"] = (bool)i.cache_hit;
         return d;
     }
     mcd_dag *handle() const { return dag_.get(); }

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <numeric>
 #include <string>
 
@@ -132,12 +133,13 @@ int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0,
         if (B->n_items > (int64_t)INT32_MAX) throw McdError(MCD_ERR_INVALID, "too many work items");
         const size_t E = (size_t)B->total_E;
         const size_t s_acc = align_up(E * 8, 256), s_hist = align_up(E * kHistStride * 4, 256), s_ctr = 256,
-                     s_out = align_up(5 * E * 8, 256), s_args = align_up((size_t)n_dags * sizeof(KArgs), 256),
+                     s_out = align_up(5 * E * 8, 256), s_te = align_up(E * 8, 256),
+                     s_args = align_up((size_t)n_dags * sizeof(KArgs), 256),
                      s_fargs = align_up((size_t)n_dags * sizeof(FArgs), 256),
                      s_items = align_up(items.size() * 4, 256),
                      s_scr = align_up((size_t)grid_global * max_E_global * kTile * 8, 256);
         B->zero_bytes = s_acc + s_hist + s_ctr;
-        cuda_check(cudaMalloc(&B->dmem, B->zero_bytes + s_out + s_args + s_fargs + s_items + s_scr),
+        cuda_check(cudaMalloc(&B->dmem, B->zero_bytes + s_out + s_te + s_args + s_fargs + s_items + s_scr),
                    "batch allocation");
         char *p = B->dmem;
         auto *acc = reinterpret_cast<unsigned long long *>(p);
@@ -146,6 +148,8 @@ int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0,
         p += B->zero_bytes;
         B->out = reinterpret_cast<double *>(p);
         p += s_out;
+        auto *d_te = reinterpret_cast<long long *>(p);
+        p += s_te;
         auto *d_args = reinterpret_cast<KArgs *>(p);
         p += s_args;
         B->d_fargs = reinterpret_cast<FArgs *>(p);
@@ -156,6 +160,7 @@ int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0,
         // per-DAG kernel and finish arguments
         std::vector<KArgs> ka((size_t)n_dags);
         std::vector<FArgs> fa((size_t)n_dags);
+        std::vector<long long> te(E);  // every DAG's earliest in ticks of its statistics
         for (int32_t i = 0; i < n_dags; ++i) {
             mcd_dag *g = B->dags[i];
             const StatsParams sp = stats_params(g->h, B->n[i]);
@@ -169,8 +174,14 @@ int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0,
             a.bin_mul = sp.bin_mul;
             a.hist_inv_w = sp.inv_w;
             a.acc = acc + B->ev_off[i];
+            a.te = d_te + B->ev_off[i];
             a.hist = B->hist + (size_t)B->ev_off[i] * kHistStride;
             ka[i] = a;
+            for (int32_t e = 0; e < g->h.E; ++e) {
+                long long b;
+                std::memcpy(&b, &g->h.earliest[(size_t)e], 8);
+                te[(size_t)B->ev_off[i] + e] = sp.fixed ? ticks_of(b, sp.q) : 0ll;
+            }
             FArgs f{};
             f.acc = a.acc;
             f.hist = a.hist;
@@ -190,6 +201,7 @@ int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0,
         cuda_check(cudaMemcpy(d_args, ka.data(), ka.size() * sizeof(KArgs), cudaMemcpyHostToDevice), "upload");
         cuda_check(cudaMemcpy(B->d_fargs, fa.data(), fa.size() * sizeof(FArgs), cudaMemcpyHostToDevice), "upload");
         cuda_check(cudaMemcpy(d_items, items.data(), items.size() * 4, cudaMemcpyHostToDevice), "upload");
+        if (E) cuda_check(cudaMemcpy(d_te, te.data(), E * 8, cudaMemcpyHostToDevice), "upload");
         for (size_t k = 0; k < B->launches.size(); ++k) {
             Launch &L = B->launches[k];
             L.args.dags = d_args;

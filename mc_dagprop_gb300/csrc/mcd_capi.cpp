@@ -21,6 +21,7 @@
 namespace mcd {
 cudaError_t launch_propagate(const KArgs &a, bool given, bool win_smem, bool stats, cudaStream_t st);
 cudaError_t launch_stats_finish(const FArgs &f, cudaStream_t st);
+cudaError_t launch_event_ticks(const double *earliest, int32_t E, int32_t q, long long *te, cudaStream_t st);
 cudaError_t noalloc_scratch(void **ptr, size_t *bytes);
 cudaError_t launch_transpose_f64(const double *in, int64_t ld_in, double *out, int64_t ld_out, int64_t rows,
                                  int64_t cols, cudaStream_t st);
@@ -755,12 +756,16 @@ static void stats_device(mcd_dag *g, const int64_t *seeds, int64_t seed0, int64_
         C = std::max<int64_t>(32, std::min<int64_t>(n, (int64_t)((512ull << 20) / std::max<size_t>(E * 8, 1)) / 32 * 32));
         scratch_bytes = align_up(E * (size_t)C * 8, 256);
     }
-    const size_t acc_bytes = align_up(E * 8, 256), hist_bytes = align_up(E * kHistStride * 4, 256);
-    ensure_ws(g, acc_bytes + hist_bytes + scratch_bytes);
+    const size_t acc_bytes = align_up(E * 8, 256), hist_bytes = align_up(E * kHistStride * 4, 256),
+                 te_bytes = align_up(E * 8, 256);
+    ensure_ws(g, acc_bytes + hist_bytes + te_bytes + scratch_bytes);
     auto *acc = reinterpret_cast<unsigned long long *>(g->ws);
     auto *hist = reinterpret_cast<uint32_t *>(g->ws + acc_bytes);
-    double *scratch = scratch_bytes ? reinterpret_cast<double *>(g->ws + acc_bytes + hist_bytes) : nullptr;
+    auto *te = reinterpret_cast<long long *>(g->ws + acc_bytes + hist_bytes);
+    double *scratch =
+        scratch_bytes ? reinterpret_cast<double *>(g->ws + acc_bytes + hist_bytes + te_bytes) : nullptr;
     cuda_check(cudaMemsetAsync(g->ws, 0, acc_bytes + hist_bytes, st), "accumulator reset");
+    if (sp.fixed) cuda_check(launch_event_ticks(g->d_earliest, h.E, sp.q, te, st), "earliest ticks");
     for (int64_t off = 0; off < n; off += C) {
         const int64_t m = std::min(C, n - off);
         KArgs a = base_args(g);
@@ -774,6 +779,7 @@ static void stats_device(mcd_dag *g, const int64_t *seeds, int64_t seed0, int64_
         a.bin_mul = sp.bin_mul;
         a.hist_inv_w = sp.inv_w;
         a.acc = acc;
+        a.te = te;
         a.hist = hist;
         cuda_check(launch_propagate(a, false, h.win_smem, true, st), "statistics launch");
     }
@@ -870,17 +876,20 @@ int mcd_stats_device_noalloc(mcd_dag *g, const int64_t *seeds, int64_t seed0, in
         size_t cap = 0;
         cuda_check(noalloc_scratch(&base, &cap), "fixed scratch lookup");
         const size_t E = (size_t)h.E;
-        const size_t acc_bytes = align_up(E * 8, 256), hist_bytes = align_up(E * kHistStride * 4, 256);
-        if (h.E > MCD_NOALLOC_MAX_EVENTS || acc_bytes + hist_bytes > cap)
+        const size_t acc_bytes = align_up(E * 8, 256), hist_bytes = align_up(E * kHistStride * 4, 256),
+                     te_bytes = align_up(E * 8, 256);
+        if (h.E > MCD_NOALLOC_MAX_EVENTS || acc_bytes + hist_bytes + te_bytes > cap)
             throw McdError(MCD_ERR_INVALID, "mcd_stats_device_noalloc supports at most " +
                                                 std::to_string(MCD_NOALLOC_MAX_EVENTS) + " events; this DAG has " +
                                                 std::to_string(h.E));
         cudaStream_t st = stream ? (cudaStream_t)stream : g->stream[0];
         auto *acc = reinterpret_cast<unsigned long long *>(base);
         auto *hist = reinterpret_cast<uint32_t *>(static_cast<char *>(base) + acc_bytes);
+        auto *te = reinterpret_cast<long long *>(static_cast<char *>(base) + acc_bytes + hist_bytes);
         // the array keeps the previous call's counts: start from zero
         cuda_check(cudaMemsetAsync(base, 0, acc_bytes + hist_bytes, st), "fixed scratch reset");
         const StatsParams sp = stats_params(h, n);
+        if (sp.fixed) cuda_check(launch_event_ticks(g->d_earliest, h.E, sp.q, te, st), "earliest ticks");
         KArgs a = base_args(g);
         a.seeds = seeds;
         a.seed0 = seed0;
@@ -891,6 +900,7 @@ int mcd_stats_device_noalloc(mcd_dag *g, const int64_t *seeds, int64_t seed0, in
         a.bin_mul = sp.bin_mul;
         a.hist_inv_w = sp.inv_w;
         a.acc = acc;
+        a.te = te;
         a.hist = hist;
         cuda_check(launch_propagate(a, false, true, true, st), "statistics launch");
         FArgs f{};

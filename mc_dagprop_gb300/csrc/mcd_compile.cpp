@@ -817,8 +817,9 @@ std::vector<unsigned char> tables_block(const HostDag &h) {
     return b;
 }
 
-// Ticks of 2^-q seconds: every |time| * 2^q must stay below 2^62, and the sum
-// over n samples of (realized - earliest) * 2^q below 2^63.
+// Ticks of 2^-q seconds: every |time| * 2^q must stay below 2^62, one sample's
+// (realized - earliest) * 2^q below 2^53 (the kernels sum a warp's counts in two
+// 27-bit limbs), and the sum over n samples below 2^63.
 StatsParams stats_params(const HostDag &h, int64_t n) {
     StatsParams p;
     const double span = std::max(h.max_span, 0.0);
@@ -827,6 +828,7 @@ StatsParams stats_params(const HostDag &h, int64_t n) {
         const int lg_span = (int)std::ceil(std::log2(std::max(span, 1e-300) * 1.001 + 1e-300));
         const int lg_n = (int)std::ceil(std::log2((double)std::max<int64_t>(n, 2)));
         int q = std::min(61 - lg_abs, 62 - lg_n - std::max(lg_span, -1000));
+        q = std::min(q, 53 - std::max(lg_span, -1000));
         q = std::min(q, 1000);
         if (q >= -60) {
             p.fixed = 1;

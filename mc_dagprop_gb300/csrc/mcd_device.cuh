@@ -359,46 +359,44 @@ __device__ __forceinline__ bool stage_wait(uint64_t *bar, uint32_t parity, int32
 }
 
 // ---------------------------------------------------------------- statistics helpers
-// x * 2^q truncated toward zero, from the bits of a finite double x with
-// |x| * 2^q < 2^62 (the host picks q so that every realized time qualifies).
-__device__ __forceinline__ long long to_ticks(long long b, int q) {
-    const int e = (int)((b >> 52) & 0x7FF);
-    const long long m = (b & 0xFFFFFFFFFFFFFll) | (e ? (1ll << 52) : 0ll);
-    const int sh = (e ? e : 1) - 1075 + q;
-    long long t;
-    if (sh >= 0) t = m << sh;
-    else t = sh > -63 ? (m >> -sh) : 0ll;
-    return b < 0 ? -t : t;
+// Statistics tick count of a realized time (ticks_of).  POSITIVE: the time is
+// non-negative and finite, and |x| * 2^q < 2^62 makes every shift of the
+// mantissa m a right shift of m << 10 (below 2^63): one variable shift.
+template <bool POSITIVE>
+__device__ __forceinline__ long long tick_count(long long b, int q) {
+    if (!POSITIVE) return ticks_of(b, q);
+    const int e = (int)(b >> 52);
+    const long long m = (b & 0xFFFFFFFFFFFFFll) | ((long long)(e != 0) << 52);
+    const int r = 1085 - q - (e ? e : 1);
+    return r < 64 ? (long long)((unsigned long long)(m << 10) >> r) : 0ll;
 }
 
-// Sum over the warp of non-negative 64-bit tick counts: four 16-bit limbs summed
-// with one redux.sync each (a limb's sum stays below 2^21), then recombined -- the
-// exact sum, as long as it stays below 2^64 (the host's choice of tick keeps the
-// sum over all samples below 2^63).
+// Sum over the warp of non-negative 64-bit tick counts below 2^54: two 27-bit
+// limbs summed with one redux.sync each (a limb's sum stays below 2^32), then
+// recombined -- the exact sum.  The host's choice of tick keeps every per-sample
+// count below 2^54 (and the sum over all samples below 2^63).
 __device__ __forceinline__ long long warp_sum_ticks(long long d) {
     const unsigned long long u = (unsigned long long)d;
-    const unsigned s0 = __reduce_add_sync(0xFFFFFFFFu, (unsigned)(u & 0xFFFFu));
-    const unsigned s1 = __reduce_add_sync(0xFFFFFFFFu, (unsigned)((u >> 16) & 0xFFFFu));
-    const unsigned s2 = __reduce_add_sync(0xFFFFFFFFu, (unsigned)((u >> 32) & 0xFFFFu));
-    const unsigned s3 = __reduce_add_sync(0xFFFFFFFFu, (unsigned)(u >> 48));
-    return (long long)((unsigned long long)s0 + ((unsigned long long)s1 << 16) + ((unsigned long long)s2 << 32) +
-                       ((unsigned long long)s3 << 48));
+    const unsigned s0 = __reduce_add_sync(0xFFFFFFFFu, (unsigned)(u & 0x7FFFFFFu));
+    const unsigned s1 = __reduce_add_sync(0xFFFFFFFFu, (unsigned)(u >> 27));
+    return (long long)((unsigned long long)s0 + ((unsigned long long)s1 << 27));
 }
 
 // One event's realized values of the tile into the per-event accumulators:
 // the tile's sum of (realized - earliest) with one 64-bit atomic, and the
-// histogram with one atomic per distinct bin of the warp.
-__device__ __forceinline__ void accumulate_stats(const KArgs &a, const EvRec &ev, long long lbits, bool active,
-                                                 unsigned active_mask) {
+// histogram with one atomic per distinct bin of the warp.  te: the event's
+// earliest in ticks (KArgs::te), loaded when the event started.
+template <bool POSITIVE>
+__device__ __forceinline__ void accumulate_stats(const KArgs &a, const EvRec &ev, long long lbits, long long te,
+                                                 bool active, unsigned active_mask) {
     int bin;
     if (a.stats_fixed) {
-        const long long te = to_ticks(ev.init_bits, a.tick_q);
-        long long d = active ? to_ticks(lbits, a.tick_q) - te : 0ll;
-        const unsigned long long du = (unsigned long long)(d > 0 ? d : 0ll);
-        bin = (int)__umul64hi(du, a.bin_mul);
+        // realized >= earliest and ticks are monotone: d >= 0
+        const long long d = active ? tick_count<POSITIVE>(lbits, a.tick_q) - te : 0ll;
+        bin = (int)__umul64hi((unsigned long long)d, a.bin_mul);
         bin = bin > kHistBins - 1 ? kHistBins - 1 : bin;
-        d = warp_sum_ticks(d > 0 ? d : 0ll);  // realized >= earliest: d >= 0
-        if ((threadIdx.x & 31) == 0 && d != 0) atomicAdd(&a.acc[ev.user], (unsigned long long)d);
+        const long long s = warp_sum_ticks(d);
+        if ((threadIdx.x & 31) == 0 && s != 0) atomicAdd(&a.acc[ev.user], (unsigned long long)s);
     } else {
         const double dd = active ? __longlong_as_double(lbits) - __longlong_as_double(ev.init_bits) : 0.0;
         const double x = dd * a.hist_inv_w;
@@ -416,10 +414,11 @@ __device__ __forceinline__ void accumulate_stats(const KArgs &a, const EvRec &ev
 
 // The tile's sum of (realized - earliest) ticks into a.acc (objective of the
 // adjoint; the same integer accumulation as the statistics mean).
-__device__ __forceinline__ void accumulate_sum(const KArgs &a, const EvRec &ev, long long lbits, bool active) {
-    long long d = active ? to_ticks(lbits, a.tick_q) - to_ticks(ev.init_bits, a.tick_q) : 0ll;
-    d = warp_sum_ticks(d > 0 ? d : 0ll);  // realized >= earliest: d >= 0
-    if ((threadIdx.x & 31) == 0 && d != 0) atomicAdd(&a.acc[ev.user], (unsigned long long)d);
+template <bool POSITIVE>
+__device__ __forceinline__ void accumulate_sum(const KArgs &a, const EvRec &ev, long long lbits, long long te,
+                                               bool active) {
+    const long long s = warp_sum_ticks(active ? tick_count<POSITIVE>(lbits, a.tick_q) - te : 0ll);
+    if ((threadIdx.x & 31) == 0 && s != 0) atomicAdd(&a.acc[ev.user], (unsigned long long)s);
 }
 
 // ---------------------------------------------------------------- stage bodies
@@ -467,6 +466,9 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec 
         const int i = i_next;
         if (lane == 0) i_next = take_next(ctr);
         const EvRec ev = load_ev(sev + i);
+        // the event's earliest in ticks, needed after its predecessors (the load's
+        // latency hides behind them)
+        const long long te = (STATS || ADJ) && a.stats_fixed ? __ldg(a.te + ev.user) : 0ll;
         // POSITIVE: keys are the bits themselves (init_key == init_bits, ub_key == ub_bits),
         // so one 64-bit value carries both
         long long lk = POSITIVE ? ev.init_bits : ev.init_key, lbits = ev.init_bits;
@@ -512,10 +514,10 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec 
         if (!POSITIVE && ub_key < lk) lbits = ev.ub_bits;
         const double real = __longlong_as_double(lbits);
         if (WIN_SMEM && ev.slot >= 0) win[ev.slot * kTile + lane] = real;
-        if (STATS) accumulate_stats(a, ev, lbits, t.active, t.active_mask);
+        if (STATS) accumulate_stats<POSITIVE>(a, ev, lbits, te, t.active, t.active_mask);
         if (ADJ) {
             const bool delayed = lk > (POSITIVE ? ev.init_bits : ev.init_key);  // realized > earliest
-            accumulate_sum(a, ev, lbits, t.active);
+            accumulate_sum<POSITIVE>(a, ev, lbits, te, t.active);
             if (t.active) {
                 const int64_t o = (int64_t)ev.user * a.ld + t.s;
                 a.adj_code[o] = (uint16_t)(win_code | (delayed ? kAdjDelayed : 0u));

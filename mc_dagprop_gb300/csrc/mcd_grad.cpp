@@ -9,6 +9,7 @@
 
 namespace mcd {
 cudaError_t launch_adjoint(const KArgs &a, cudaStream_t st);
+cudaError_t launch_event_ticks(const double *earliest, int32_t E, int32_t q, long long *te, cudaStream_t st);
 cudaError_t launch_adjoint_finish(const long long *grad_e, const long long *grad_l, const unsigned long long *acc,
                                   int32_t E, int32_t L, int64_t n, int32_t q, double *g_earliest, double *g_base,
                                   double *objective, cudaStream_t st);
@@ -36,8 +37,8 @@ extern "C" int mcd_gradient_host(mcd_dag *g, int64_t seed0, int64_t n, double *o
         C = std::max<int64_t>(32, std::min<int64_t>(C / 32 * 32, (n + 31) / 32 * 32));
         const size_t s_code = align_up(E * (size_t)C * 2, 256), s_dfac = align_up(E * (size_t)C * 4, 256),
                      s_acc = align_up(E * 8, 256), s_ge = align_up(E * 8, 256), s_gl = align_up(L * 8 + 8, 256),
-                     s_out = align_up((E + L + 1) * 8, 256);
-        ensure_ws(g, s_code + s_dfac + s_acc + s_ge + s_gl + s_out);
+                     s_out = align_up((E + L + 1) * 8, 256), s_te = align_up(E * 8, 256);
+        ensure_ws(g, s_code + s_dfac + s_acc + s_ge + s_gl + s_out + s_te);
         char *p = g->ws;
         auto *code = reinterpret_cast<uint16_t *>(p);
         p += s_code;
@@ -49,6 +50,8 @@ extern "C" int mcd_gradient_host(mcd_dag *g, int64_t seed0, int64_t n, double *o
         cuda_check(cudaMemsetAsync(p, 0, s_acc + s_ge + s_gl, st), "accumulator reset");
         p += s_acc + s_ge + s_gl;
         auto *out = reinterpret_cast<double *>(p);
+        auto *te = reinterpret_cast<long long *>(p + s_out);
+        cuda_check(launch_event_ticks(g->d_earliest, h.E, sp.q, te, st), "earliest ticks");
         for (int64_t off = 0; off < n; off += C) {
             KArgs a = base_args(g);
             a.seeds = nullptr;
@@ -58,6 +61,7 @@ extern "C" int mcd_gradient_host(mcd_dag *g, int64_t seed0, int64_t n, double *o
             a.stats_fixed = 1;
             a.tick_q = sp.q;
             a.acc = acc;
+            a.te = te;
             a.adj_code = code;
             a.adj_dfac = dfac;
             a.grad_e = ge;

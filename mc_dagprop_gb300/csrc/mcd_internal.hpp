@@ -8,7 +8,26 @@
 
 #include <cstdint>
 
+#if defined(__CUDACC__)
+#define MCD_HD __host__ __device__
+#else
+#define MCD_HD
+#endif
+
 namespace mcd {
+
+// x * 2^q truncated toward zero, from the bits b of a finite double x with
+// |x| * 2^q < 2^62: the statistics tick count of a time.  The host builds the
+// per-run table of earliest ticks with this same definition the kernels use.
+MCD_HD inline long long ticks_of(long long b, int q) {
+    const int e = (int)((b >> 52) & 0x7FF);
+    const long long m = (b & 0xFFFFFFFFFFFFFll) | (e ? (1ll << 52) : 0ll);
+    const int sh = (e ? e : 1) - 1075 + q;
+    long long t;
+    if (sh >= 0) t = m << sh;
+    else t = sh > -63 ? (m >> -sh) : 0ll;
+    return b < 0 ? -t : t;
+}
 
 // Delay kinds as the kernels see them.  FIXED covers links whose duration does
 // not vary between samples: unmapped types, gaps in the link index space and the
@@ -169,6 +188,7 @@ struct KArgs {
     unsigned long long bin_mul;   // bin = mulhi64(delta_ticks, bin_mul)
     double hist_inv_w;            // FP64 fallback: 256 / max_delay, 0 when not finite
     unsigned long long *acc;      // [E] sum of delta ticks (fixed) or FP64 sum bits (fallback)
+    const long long *te;          // [E] ticks_of(earliest, tick_q), caller order (fixed ticks only)
     uint32_t *hist;               // [E][kHistStride]
     // adjoint
     uint16_t *adj_code;           // [E][ld] winner position and flags (forward), read backward

@@ -13,28 +13,71 @@
 
 namespace mcd {
 
-// Quantile at probability p of one event from its histogram: rank p*(n-1) as
-// numpy's default ("linear") takes it, atoms exact, samples spread evenly
-// inside a bin.
-__device__ double hist_quantile(const uint32_t *h, int64_t n, double p, double lo, double hi, double w) {
+// One warp per event.  Lane j holds bins 8j .. 8j+7 and their running count from
+// a warp scan (exact integers), so finding the bin of a quantile is a ballot, not a
+// 256-step loop.
+constexpr int kBinsPerLane = kHistBins / 32;
+static_assert(kHistBins == 32 * kBinsPerLane && kBinsPerLane == 8, "two 16-byte loads per lane");
+
+// Quantile at probability p from the lane's bins: rank p*(n-1) as numpy's default
+// ("linear") takes it, atoms exact, samples spread evenly inside a bin.
+// below: the count before this lane's first bin, on-time atom included.
+__device__ double warp_quantile(const uint32_t (&c)[kBinsPerLane], uint32_t below, uint32_t c_lo, uint32_t c_hi,
+                                int64_t n, double p, double lo, double hi, double w) {
+    const int lane = threadIdx.x & 31;
     const double k = p * (double)(n - 1);
-    const double c_lo = h[kBinLo], c_hi = h[kBinHi];
-    if (k < c_lo) return lo;
-    if (k >= (double)n - c_hi) return hi;
-    double cum = c_lo;
-    for (int b = 0; b < kHistBins; ++b) {
-        const double c = h[b];
-        if (c > 0.0 && k < cum + c) {
-            const double v = lo + ((double)b + (k - cum + 0.5) / c) * w;
-            return v < hi ? v : hi;
+    if (k < (double)c_lo) return lo;
+    if (k >= (double)n - (double)c_hi) return hi;
+    // the first bin whose cumulative count (on-time atom included) exceeds k
+    uint32_t cum = below;
+    int found = -1;
+    uint32_t cum_before = 0;
+#pragma unroll
+    for (int j = 0; j < kBinsPerLane; ++j) {
+        if (found < 0 && (double)(cum + c[j]) > k) {
+            found = j;
+            cum_before = cum;
         }
-        cum += c;
+        cum += c[j];
     }
-    return hi;
+    const unsigned hit = __ballot_sync(0xFFFFFFFFu, found >= 0);
+    if (!hit) return hi;
+    const int src = __ffs(hit) - 1;
+    const int j = __shfl_sync(0xFFFFFFFFu, found, src);
+    const uint32_t cb = __shfl_sync(0xFFFFFFFFu, cum_before, src);
+    uint32_t cj = 0;
+#pragma unroll
+    for (int t = 0; t < kBinsPerLane; ++t)
+        if (t == j) cj = c[t];
+    cj = __shfl_sync(0xFFFFFFFFu, cj, src);
+    const int bin = src * kBinsPerLane + j;
+    const double v = lo + ((double)bin + (k - (double)cb + 0.5) / (double)cj) * w;
+    (void)lane;
+    return v < hi ? v : hi;
 }
 
-__device__ __forceinline__ void finish_event(const FArgs &f, int e) {
+__device__ __forceinline__ void finish_event_warp(const FArgs &f, int e) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t *h = f.hist + (int64_t)e * kHistStride;
+    const uint4 a = reinterpret_cast<const uint4 *>(h)[2 * lane];
+    const uint4 b = reinterpret_cast<const uint4 *>(h)[2 * lane + 1];
+    const uint32_t c[kBinsPerLane] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    const uint32_t c_lo = h[kBinLo], c_hi = h[kBinHi];
+    uint32_t mine = 0;
+#pragma unroll
+    for (int j = 0; j < kBinsPerLane; ++j) mine += c[j];
+    uint32_t incl = mine;  // inclusive scan over lanes (the counts sum to at most n <= 2^31)
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t o = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= d) incl += o;
+    }
+    const uint32_t below = c_lo + incl - mine;
     const double lo = f.earliest[e], hi = f.ub[e];
+    const double p50 = warp_quantile(c, below, c_lo, c_hi, f.n, 0.50, lo, hi, f.bin_w);
+    const double p90 = warp_quantile(c, below, c_lo, c_hi, f.n, 0.90, lo, hi, f.bin_w);
+    const double p99 = warp_quantile(c, below, c_lo, c_hi, f.n, 0.99, lo, hi, f.bin_w);
+    if (lane != 0) return;
     const double n = (double)f.n;
     if (f.mean) {
         double sum;
@@ -42,25 +85,30 @@ __device__ __forceinline__ void finish_event(const FArgs &f, int e) {
         else sum = __longlong_as_double((long long)f.acc[e]);
         f.mean[e] = lo + sum / n;
     }
-    const uint32_t *h = f.hist + (int64_t)e * kHistStride;
-    if (f.p50) f.p50[e] = hist_quantile(h, f.n, 0.50, lo, hi, f.bin_w);
-    if (f.p90) f.p90[e] = hist_quantile(h, f.n, 0.90, lo, hi, f.bin_w);
-    if (f.p99) f.p99[e] = hist_quantile(h, f.n, 0.99, lo, hi, f.bin_w);
-    if (f.p_on_time) f.p_on_time[e] = (double)h[kBinLo] / n;
+    if (f.p50) f.p50[e] = p50;
+    if (f.p90) f.p90[e] = p90;
+    if (f.p99) f.p99[e] = p99;
+    if (f.p_on_time) f.p_on_time[e] = (double)c_lo / n;
 }
 
-__global__ void k_stats_finish(const FArgs f) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < f.E) finish_event(f, e);
+__global__ void __launch_bounds__(256) k_stats_finish(const FArgs f) {
+    const int e = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (e < f.E) finish_event_warp(f, e);
 }
 
 // The finish of every DAG of a batch in one launch: blockIdx.y selects the DAG.
-__global__ void k_batch_finish(const FArgs *__restrict__ fs, int32_t n_dags) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) k_batch_finish(const FArgs *__restrict__ fs, int32_t n_dags) {
+    const int e = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     for (int32_t d = (int32_t)blockIdx.y; d < n_dags; d += (int32_t)gridDim.y) {
         const FArgs &f = fs[d];
-        if (e < f.E) finish_event(f, e);
+        if (e < f.E) finish_event_warp(f, e);
     }
+}
+
+// Every event's earliest in ticks of 2^-q seconds (KArgs::te) for one run.
+__global__ void k_event_ticks(const double *__restrict__ earliest, int32_t E, int32_t q, long long *__restrict__ te) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x)
+        te[e] = ticks_of(__double_as_longlong(earliest[e]), q);
 }
 
 // ---------------------------------------------------------------- layout change
@@ -115,11 +163,11 @@ cudaError_t launch_propagate(const KArgs &a, bool given, bool win_smem, bool sta
 
 // ---------------------------------------------------------------- fixed scratch
 // Device scratch for mcd_stats_device_noalloc: the per-event accumulators
-// (8 bytes of sum + kHistStride 32-bit counters per event) of callers that
-// cannot allocate device memory.  32 MiB, held by every GPU that loads this
-// library until the process exits.  Host code must not use the symbol as an
+// (8 bytes of sum, kHistStride 32-bit counters and 8 bytes of earliest ticks per
+// event) of callers that cannot allocate device memory.  34 MiB, held by every
+// GPU that loads this library until the process exits.  Host code must not use the symbol as an
 // address; noalloc_scratch() below looks the device address up.
-constexpr size_t kNoAllocScratchBytes = 32ull << 20;
+constexpr size_t kNoAllocScratchBytes = 34ull << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 // Device address of g_noalloc_scratch on the current device, looked up once per
@@ -147,13 +195,20 @@ cudaError_t noalloc_scratch(void **ptr, size_t *bytes) {
 cudaError_t launch_batch_finish(const FArgs *fs, int32_t n_dags, int32_t max_events, cudaStream_t st) {
     if (n_dags <= 0 || max_events <= 0) return cudaSuccess;
     const unsigned gy = (unsigned)(n_dags < 65535 ? n_dags : 65535);  // grid y limit; the kernel strides
-    k_batch_finish<<<dim3((unsigned)((max_events + 255) / 256), gy), 256, 0, st>>>(fs, n_dags);
+    k_batch_finish<<<dim3((unsigned)((max_events + 7) / 8), gy), 256, 0, st>>>(fs, n_dags);  // a warp per event
+    return cudaGetLastError();
+}
+
+cudaError_t launch_event_ticks(const double *earliest, int32_t E, int32_t q, long long *te, cudaStream_t st) {
+    if (E <= 0) return cudaSuccess;
+    const int blocks = (E + 255) / 256;
+    k_event_ticks<<<blocks < 4096 ? blocks : 4096, 256, 0, st>>>(earliest, E, q, te);
     return cudaGetLastError();
 }
 
 cudaError_t launch_stats_finish(const FArgs &f, cudaStream_t st) {
     if (f.E <= 0) return cudaSuccess;
-    k_stats_finish<<<(unsigned)((f.E + 255) / 256), 256, 0, st>>>(f);
+    k_stats_finish<<<(unsigned)((f.E + 7) / 8), 256, 0, st>>>(f);  // a warp per event
     return cudaGetLastError();
 }
 

@@ -52,7 +52,7 @@ enum State : int { Q_COMPILE = 0, Q_READY = 1, Q_RUNNING = 2, Q_DONE = 3, Q_FAIL
 // Offsets of one request's device block: compiled records, then the
 // accumulators (zeroed at upload), then the statistics.
 struct Layout {
-    size_t ev, pred, aux, tables, vals, wk, meta, earliest, ub, err, acc, hist, out, total;
+    size_t ev, pred, aux, tables, vals, wk, meta, earliest, ub, te, err, acc, hist, out, total;
 };
 
 Layout layout_of(const HostDag &h) {
@@ -72,6 +72,7 @@ Layout layout_of(const HostDag &h) {
     L.meta = take(h.stage_meta.size() * 4);
     L.earliest = take((size_t)h.E * 8);
     L.ub = take((size_t)h.E * 8);
+    L.te = take((size_t)h.E * 8);
     L.err = take(4);
     L.acc = take((size_t)h.E * 8);
     L.hist = take((size_t)h.E * kHistStride * 4);
@@ -191,6 +192,7 @@ void request_args(Request *r) {
     a.bin_mul = sp.bin_mul;
     a.hist_inv_w = sp.inv_w;
     a.acc = reinterpret_cast<unsigned long long *>(b + L.acc);
+    a.te = reinterpret_cast<const long long *>(b + L.te);
     a.hist = reinterpret_cast<uint32_t *>(b + L.hist);
     FArgs &f = r->fa;
     f = FArgs{};
@@ -254,6 +256,15 @@ void upload_request(const mcd_server *S, Request *r, cudaStream_t st, Staging &s
     put(L.meta, h.stage_meta.data(), h.stage_meta.size() * 4);
     put(L.earliest, h.earliest.data(), (size_t)h.E * 8);
     put(L.ub, h.ub.data(), (size_t)h.E * 8);
+    {  // earliest in ticks of the request's statistics
+        const StatsParams sp = stats_params(h, r->n);
+        auto *te = reinterpret_cast<long long *>(stage.p + L.te);
+        for (int32_t e = 0; e < h.E; ++e) {
+            long long b;
+            std::memcpy(&b, &h.earliest[(size_t)e], 8);
+            te[e] = sp.fixed ? ticks_of(b, sp.q) : 0ll;
+        }
+    }
     cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&r->dblock), r->bytes, st), "request allocation");
     char *b = r->dblock;
     cuda_check(cudaMemcpyAsync(b, stage.p, L.err, cudaMemcpyHostToDevice, st), "request upload");  // records

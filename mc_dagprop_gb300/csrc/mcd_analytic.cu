@@ -4,7 +4,7 @@
 // A PMF is (first value, probabilities) on the context's step grid.  Events are
 // processed level by level (longest path from a source), two launches a level:
 // k_an_conv computes every convolution of the level, its outputs split into
-// chunks of 256 across CTAs (the FP64 multiply-adds are the bulk of the work);
+// chunks of 64 across CTAs (the FP64 multiply-adds are the bulk of the work);
 // k_an_fold then takes one event per CTA:
 //   convolution along each incoming activity       _pmf.py:107-125
 //   maximum over the predecessors, pairwise in      _pmf.py:127-148
@@ -34,7 +34,10 @@
 namespace mcd {
 namespace {
 
-constexpr int kAnThreads = 256;
+constexpr int kAnThreads = 128;
+// Outputs (and threads) per convolution CTA: small CTAs spread a level's
+// multiply-adds evenly over the SMs (several CTAs per SM, no partial last wave).
+constexpr int kConvChunk = 64;
 constexpr int64_t kAnSmemBins = 4096;  // 5 arrays x 4096 doubles = 160 KB of shared memory
 
 // Kernel-reported errors (the reference raises ValueError in each case).
@@ -92,53 +95,93 @@ __device__ __forceinline__ double expected_mass(double m1, double m2) {  // _pmf
     return (close12(m1, 1.0) && close12(m2, 1.0)) ? 1.0 : m1 * m2;
 }
 
-// Sum over the block (every thread gets the result).
-__device__ double block_sum(double v, double *red) {
+constexpr int kAnWarps = kAnThreads / 32;
+
+// Block-wide sums with one barrier each.  The FP64 pipe (2 lanes per clock per
+// SM) and the chain of dependent phases bound this kernel, so a sum is a warp
+// shuffle tree, one barrier, and every thread adding the few warp totals itself.
+// Warps post their totals to one of two slot sets, alternately: a call never
+// overwrites totals a slower thread may still be reading from the call before it
+// (the barrier of the call in between separates them).  Every thread of the
+// block must make the same sequence of calls.
+struct BlockRed {
+    double *slots;  // [2][2][kAnWarps]
+    int parity;
+    __device__ double2 sum2(double x, double y) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
-    const int w = threadIdx.x >> 5;
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) red[w] = v;
-    __syncthreads();
-    double t = 0.0;
-    for (int i = 0; i < kAnThreads / 32; ++i) t += red[i];
-    return t;
+        for (int o = 16; o > 0; o >>= 1) {
+            x += __shfl_xor_sync(0xFFFFFFFFu, x, o);
+            y += __shfl_xor_sync(0xFFFFFFFFu, y, o);
+        }
+        double *sl = slots + parity * 2 * kAnWarps;
+        parity ^= 1;
+        const int w = threadIdx.x >> 5;
+        if ((threadIdx.x & 31) == 0) {
+            sl[w] = x;
+            sl[kAnWarps + w] = y;
+        }
+        __syncthreads();
+        double tx = 0.0, ty = 0.0;
+#pragma unroll
+        for (int i = 0; i < kAnWarps; ++i) {
+            tx += sl[i];
+            ty += sl[kAnWarps + i];
+        }
+        return make_double2(tx, ty);
+    }
+    __device__ double sum(double x) { return sum2(x, 0.0).x; }
+};
+
+// The first index >= lo this thread owns under the strided mapping (index i
+// belongs to thread i mod kAnThreads).  Every elementwise phase uses that
+// mapping, so a phase that only touches its own elements needs no barrier.
+__device__ __forceinline__ int64_t own_from(int64_t lo) {
+    const int64_t r = ((int64_t)threadIdx.x - lo) % kAnThreads;
+    return lo + (r < 0 ? r + kAnThreads : r);
 }
 
-__device__ double range_sum(const double *x, int64_t lo, int64_t hi, double *red) {
-    double s = 0.0;
-    for (int64_t i = lo + threadIdx.x; i < hi; i += kAnThreads) s += x[i];
-    return block_sum(s, red);
-}
-
-__device__ void range_scale(double *x, int64_t lo, int64_t hi, double f) {
-    for (int64_t i = lo + threadIdx.x; i < hi; i += kAnThreads) x[i] *= f;
-    __syncthreads();
-}
-
-// In-place inclusive prefix sum of x[0, n): contiguous chunks per thread.
-__device__ void block_scan(double *x, int64_t n, double *red) {
+// Inclusive prefix sums ox = cumsum(x[0, n)), oy = cumsum(y[0, n)), each thread
+// scanning one contiguous chunk of both; two barriers.  x and y must be complete
+// (a barrier after their last writes); the closing barrier lets callers read any
+// element of ox and oy.
+__device__ void block_scan2(const double *x, const double *y, double *ox, double *oy, int64_t n, BlockRed &r) {
     const int64_t chunk = (n + kAnThreads - 1) / kAnThreads;
     const int64_t a0 = (int64_t)threadIdx.x * chunk, a = a0 < n ? a0 : n, b = a + chunk < n ? a + chunk : n;
-    double local = 0.0;
-    for (int64_t i = a; i < b; ++i) local += x[i];
-    // exclusive scan of the thread totals
-    double incl = local;
+    double lx = 0.0, ly = 0.0;
+    for (int64_t i = a; i < b; ++i) {
+        lx += x[i];
+        ly += y[i];
+    }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double ix = lx, iy = ly;  // inclusive within the warp
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const double y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= o) incl += y;
+        const double ux = __shfl_up_sync(0xFFFFFFFFu, ix, o), uy = __shfl_up_sync(0xFFFFFFFFu, iy, o);
+        if (lane >= o) {
+            ix += ux;
+            iy += uy;
+        }
+    }
+    double ex = __shfl_up_sync(0xFFFFFFFFu, ix, 1), ey = __shfl_up_sync(0xFFFFFFFFu, iy, 1);
+    if (lane == 0) ex = ey = 0.0;
+    double *sl = r.slots + r.parity * 2 * kAnWarps;
+    r.parity ^= 1;
+    if (lane == 31) {
+        sl[w] = ix;
+        sl[kAnWarps + w] = iy;
     }
     __syncthreads();
-    if (lane == 31) red[w] = incl;
-    __syncthreads();
-    double base = 0.0;
-    for (int i = 0; i < w; ++i) base += red[i];
-    double run = base + incl - local;
+    double bx = 0.0, by = 0.0;
+    for (int i = 0; i < w; ++i) {
+        bx += sl[i];
+        by += sl[kAnWarps + i];
+    }
+    double rx = bx + ex, ry = by + ey;
     for (int64_t i = a; i < b; ++i) {
-        run += x[i];
-        x[i] = run;
+        rx += x[i];
+        ox[i] = rx;
+        ry += y[i];
+        oy[i] = ry;
     }
     __syncthreads();
 }
@@ -148,13 +191,13 @@ __device__ __forceinline__ int64_t round_half_even(double x) { return (int64_t)r
 // Length of the convolution of a pred PMF of n entries with an activity PMF of m.
 __device__ __forceinline__ int64_t conv_len(int64_t n, int64_t m) { return n == 1 ? m : (m == 1 ? n : n + m - 1); }
 
-// One chunk of 256 outputs of one convolution: chunks[blockIdx.x] = (predecessor
-// entry, chunk index).  Chunks past the convolution's actual length exit.
-__global__ void __launch_bounds__(kAnThreads) k_an_conv(const AnArgs A, const int2 *__restrict__ chunks) {
+// One chunk of kConvChunk outputs of one convolution: chunks[blockIdx.x] =
+// (predecessor entry, chunk index).  Chunks past the convolution's actual length exit.
+__global__ void __launch_bounds__(kConvChunk) k_an_conv(const AnArgs A, const int2 *__restrict__ chunks) {
     const int2 c = chunks[blockIdx.x];
     const int32_t s = A.pred_src[c.x], k = A.pred_pmf[c.x];
     const int64_t n = A.out[s].len, m = A.pmf_off[k + 1] - A.pmf_off[k];
-    const int64_t j = (int64_t)c.y * kAnThreads + threadIdx.x;
+    const int64_t j = (int64_t)c.y * kConvChunk + threadIdx.x;
     if (j >= conv_len(n, m)) return;
     const double *p = A.pool + A.ev[s].pool_off, *q = A.pmf_probs + A.pmf_off[k];
     double v;
@@ -173,7 +216,8 @@ __global__ void __launch_bounds__(kAnThreads) k_an_conv(const AnArgs A, const in
 
 __global__ void __launch_bounds__(kAnThreads) k_an_fold(const AnArgs A, const int32_t *__restrict__ level_ev) {
     extern __shared__ __align__(16) double sm[];
-    __shared__ double red[kAnThreads / 32];
+    __shared__ double slots[4 * kAnWarps];
+    BlockRed red{slots, 0};
     const int32_t e = level_ev[blockIdx.x];
     const AnEv ev = A.ev[e];
     const int64_t G = ev.gmax;
@@ -185,7 +229,7 @@ __global__ void __launch_bounds__(kAnThreads) k_an_fold(const AnArgs A, const in
         if (threadIdx.x == 0) atomicOr(A.err, (code)); \
     } while (0)
 
-    // ---- predecessor 0: R = pred0 (*) activity0
+    // ---- predecessor 0: R = pred0 (*) activity0, rescaled to its expected mass
     double fX;
     int64_t nX;
     double mR;
@@ -200,12 +244,21 @@ __global__ void __launch_bounds__(kAnThreads) k_an_fold(const AnArgs A, const in
             return;
         }
         const double *conv = A.convbuf + A.conv_off[ev.pred_begin];
-        for (int64_t j = threadIdx.x; j < nX; j += kAnThreads) X[j] = conv[j];
-        __syncthreads();
+        double part = 0.0;
+        for (int64_t j = threadIdx.x; j < nX; j += kAnThreads) {
+            const double v = conv[j];
+            X[j] = v;
+            part += v;
+        }
+        const double tot = red.sum(part);
         const double expct = expected_mass(ps.mass, A.pmf_mass[k]);
-        const double tot = range_sum(X, 0, nX, red);
-        if (tot > 0.0 && !close12(tot, expct)) range_scale(X, 0, nX, expct / tot);
-        mR = range_sum(X, 0, nX, red);
+        mR = tot;
+        if (tot > 0.0 && !close12(tot, expct)) {
+            const double f = expct / tot;
+            part = 0.0;
+            for (int64_t j = threadIdx.x; j < nX; j += kAnThreads) part += (X[j] *= f);
+            mR = red.sum(part);
+        }
     }
     // ---- later predecessors: R = max(R, pred_k (*) activity_k)
     for (int32_t pi = ev.pred_begin + 1; pi < ev.pred_end; ++pi) {
@@ -223,41 +276,48 @@ __global__ void __launch_bounds__(kAnThreads) k_an_fold(const AnArgs A, const in
             fail(n > G ? AN_ERR_CAPACITY : AN_ERR_GRID);
             return;
         }
+        // both operands on the common grid; the convolution rescaled to its expected mass
+        const double *conv = A.convbuf + A.conv_off[pi];
+        double part = 0.0;
         for (int64_t i = threadIdx.x; i < n; i += kAnThreads) {
             Rp[i] = (i >= oR && i < oR + nX) ? X[i - oR] : 0.0;
-            Cp[i] = 0.0;
+            const double c = (i >= oC && i < oC + nC) ? conv[i - oC] : 0.0;
+            Cp[i] = c;
+            part += c;
         }
-        __syncthreads();
-        {
-            const double *conv = A.convbuf + A.conv_off[pi];
-            for (int64_t j = threadIdx.x; j < nC; j += kAnThreads) Cp[oC + j] = conv[j];
-            __syncthreads();
+        const double totC = red.sum(part);
+        const double expctC = expected_mass(ps.mass, A.pmf_mass[k]);
+        double mC = totC;
+        if (totC > 0.0 && !close12(totC, expctC)) {
+            const double f = expctC / totC;
+            part = 0.0;
+            for (int64_t i = own_from(oC); i < oC + nC; i += kAnThreads) part += (Cp[i] *= f);
+            mC = red.sum(part);
         }
-        {
-            const double expct = expected_mass(ps.mass, A.pmf_mass[k]);
-            const double tot = range_sum(Cp, oC, oC + nC, red);
-            if (tot > 0.0 && !close12(tot, expct)) range_scale(Cp, oC, oC + nC, expct / tot);
-        }
-        const double mC = range_sum(Cp, 0, n, red);
+        // max(R, C) by cumulative sums: P(max = x) = r(x) C(x) + c(x) R(x - 1); the
+        // last sum's barrier completed Rp and Cp
+        block_scan2(Rp, Cp, cR, cC, n, red);
+        part = 0.0;
         for (int64_t i = threadIdx.x; i < n; i += kAnThreads) {
-            cR[i] = Rp[i];
-            cC[i] = Cp[i];
+            const double v = fma(Rp[i], cC[i], Cp[i] * (i > 0 ? cR[i - 1] : 0.0));
+            X[i] = v;
+            part += v;
         }
-        __syncthreads();
-        block_scan(cR, n, red);
-        block_scan(cC, n, red);
-        for (int64_t i = threadIdx.x; i < n; i += kAnThreads)
-            X[i] = fma(Rp[i], cC[i], Cp[i] * (i > 0 ? cR[i - 1] : 0.0));
-        __syncthreads();
         fX = lo;
         nX = n;
+        const double tot = red.sum(part);
         const double expct = expected_mass(mR, mC);
-        const double tot = range_sum(X, 0, nX, red);
-        if (tot > 0.0 && !close12(tot, expct)) range_scale(X, 0, nX, expct / tot);
-        mR = range_sum(X, 0, nX, red);
+        mR = tot;
+        if (tot > 0.0 && !close12(tot, expct)) {
+            const double f = expct / tot;
+            part = 0.0;
+            for (int64_t i = threadIdx.x; i < nX; i += kAnThreads) part += (X[i] *= f);
+            mR = red.sum(part);
+        }
     }
 
-    // ---- clipping to [lower, upper] under the flow rules (_propagator.py:158-265)
+    // ---- clipping to [lower, upper] under the flow rules (_propagator.py:158-265);
+    // from here on every thread touches only its own elements of X
     const double lower = (double)ev.lower, upper = (double)ev.upper;
     if (ev.lower > ev.upper) {
         fail(AN_ERR_BOUNDS);
@@ -266,7 +326,18 @@ __global__ void __launch_bounds__(kAnThreads) k_an_fold(const AnArgs A, const in
     int64_t ka = (int64_t)ceil((lower - fX) / step), kb = (int64_t)floor((upper - fX) / step) + 1;
     ka = ka < 0 ? 0 : (ka > nX ? nX : ka);
     kb = kb > nX ? nX : (kb < ka ? ka : kb);
-    double u = range_sum(X, 0, ka, red), o = range_sum(X, kb, nX, red);
+    double u, o;
+    {
+        double pu = 0.0, po = 0.0;
+        for (int64_t i = threadIdx.x; i < nX; i += kAnThreads) {
+            if (i < ka) pu += X[i];
+            else if (i >= kb) po += X[i];
+        }
+        const double2 uo = red.sum2(pu, po);
+        u = uo.x;
+        o = uo.y;
+    }
+    const bool own_ka = ka < nX && own_from(ka) == ka, own_last = kb > 0 && own_from(kb - 1) == kb - 1;
     // kept values: X[ka, kb) at fX + i * step, or one value `single_v` with mass `single_p`
     bool single = false;
     double single_v = 0.0, single_p = 0.0;
@@ -274,8 +345,7 @@ __global__ void __launch_bounds__(kAnThreads) k_an_fold(const AnArgs A, const in
     double red_u = 0.0, red_o = 0.0;
     if (A.urule == MCD_RULE_TRUNCATE && u > 0.0) {
         if (nk > 0 && close_default(fX + step * (double)ka, lower)) {
-            if (threadIdx.x == 0) X[ka] += u;
-            __syncthreads();
+            if (own_ka) X[ka] += u;
         } else if (nk == 0) {
             single = true;
             single_v = lower;
@@ -294,10 +364,7 @@ __global__ void __launch_bounds__(kAnThreads) k_an_fold(const AnArgs A, const in
         const double last = single ? single_v : fX + step * (double)(kb - 1);
         if (any && close_default(last, upper)) {
             if (single) single_p += o;
-            else {
-                if (threadIdx.x == 0) X[kb - 1] += o;
-                __syncthreads();
-            }
+            else if (own_last) X[kb - 1] += o;
         } else if (!any) {
             single = true;
             single_v = upper;
@@ -311,9 +378,14 @@ __global__ void __launch_bounds__(kAnThreads) k_an_fold(const AnArgs A, const in
         red_o = o;
         o = 0.0;
     }
+    auto kept_sum = [&]() {
+        double part = 0.0;
+        for (int64_t i = own_from(ka); i < kb; i += kAnThreads) part += X[i];
+        return red.sum(part);
+    };
     const double redist = red_u + red_o;
     if (redist > 0.0) {
-        const double inside = single ? single_p : range_sum(X, ka, kb, red);
+        const double inside = single ? single_p : kept_sum();
         if (inside == 0.0) {
             single = true;
             single_v = lower;
@@ -321,8 +393,7 @@ __global__ void __launch_bounds__(kAnThreads) k_an_fold(const AnArgs A, const in
         } else if (single) {
             single_p = single_p + redist * (single_p / inside);
         } else {
-            for (int64_t i = ka + threadIdx.x; i < kb; i += kAnThreads) X[i] = X[i] + redist * (X[i] / inside);
-            __syncthreads();
+            for (int64_t i = own_from(ka); i < kb; i += kAnThreads) X[i] = X[i] + redist * (X[i] / inside);
         }
     }
     if (!single && nk == 0) {
@@ -330,26 +401,40 @@ __global__ void __launch_bounds__(kAnThreads) k_an_fold(const AnArgs A, const in
         return;
     }
     const double target = fmax(0.0, 1.0 - (u + o));
+    double total;
     {
-        const double s_in = single ? single_p : range_sum(X, ka, kb, red);
+        const double s_in = single ? single_p : kept_sum();
         if (s_in > 0.0) {
-            if (single) single_p = (single_p / s_in) * target;
-            else {
-                for (int64_t i = ka + threadIdx.x; i < kb; i += kAnThreads) X[i] = (X[i] / s_in) * target;
-                __syncthreads();
+            if (single) {
+                single_p = (single_p / s_in) * target;
+                total = single_p;
+            } else {
+                double part = 0.0;
+                for (int64_t i = own_from(ka); i < kb; i += kAnThreads) part += (X[i] = (X[i] / s_in) * target);
+                total = red.sum(part);
             }
-        } else if (target > 0.0) {
-            single = true;
-            single_v = lower;
-            single_p = target;
+        } else {
+            if (target > 0.0) {
+                single = true;
+                single_v = lower;
+                single_p = target;
+            }
+            total = single ? single_p : s_in;
         }
     }
+    double mass = total;
     {
-        const double total = (single ? single_p : range_sum(X, ka, kb, red)) + u + o;
-        if (!close12(total, 1.0)) {
-            const double corr = total > 0.0 ? 1.0 / total : 1.0;
-            if (single) single_p *= corr;
-            else range_scale(X, ka, kb, corr);
+        const double all = total + u + o;
+        if (!close12(all, 1.0)) {
+            const double corr = all > 0.0 ? 1.0 / all : 1.0;
+            if (single) {
+                single_p *= corr;
+                mass = single_p;
+            } else {
+                double part = 0.0;
+                for (int64_t i = own_from(ka); i < kb; i += kAnThreads) part += (X[i] *= corr);
+                mass = red.sum(part);
+            }
         }
     }
     // ---- output
@@ -362,9 +447,8 @@ __global__ void __launch_bounds__(kAnThreads) k_an_fold(const AnArgs A, const in
     if (single) {
         if (threadIdx.x == 0) dst[0] = single_p;
     } else {
-        for (int64_t i = threadIdx.x; i < nk; i += kAnThreads) dst[i] = X[ka + i];
+        for (int64_t i = own_from(ka); i < kb; i += kAnThreads) dst[i - ka] = X[i];
     }
-    const double mass = single ? single_p : range_sum(X, ka, kb, red);
     if (threadIdx.x == 0) {
         AnOut r;
         r.first = single ? single_v : fX + step * (double)ka;
@@ -543,7 +627,7 @@ int mcd_analytic_create(const mcd_analytic_desc *d, mcd_analytic **out) {
                     const int64_t len = n == 1 ? m : (m == 1 ? n : n + m - 1);
                     conv_off[p] = conv;
                     conv += (len + 1) / 2 * 2;
-                    for (int64_t c = 0; c * kAnThreads < len; ++c) chunks.push_back(make_int2((int)p, (int)c));
+                    for (int64_t c = 0; c * kConvChunk < len; ++c) chunks.push_back(make_int2((int)p, (int)c));
                 }
             }
             scratch_max = std::max(scratch_max, scratch);
@@ -616,7 +700,7 @@ int mcd_analytic_create(const mcd_analytic_desc *d, mcd_analytic **out) {
         cuda_check(cudaStreamBeginCapture(an->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
         for (size_t l = 0; l + 1 < an->level_off.size(); ++l) {
             const int32_t nc = an->chunk_off[l + 1] - an->chunk_off[l], ne = an->level_off[l + 1] - an->level_off[l];
-            if (nc > 0) k_an_conv<<<nc, kAnThreads, 0, an->stream>>>(an->args, an->d_chunks + an->chunk_off[l]);
+            if (nc > 0) k_an_conv<<<nc, kConvChunk, 0, an->stream>>>(an->args, an->d_chunks + an->chunk_off[l]);
             if (ne > 0)
                 k_an_fold<<<ne, kAnThreads, an->level_smem[l], an->stream>>>(an->args, an->d_level_ev + an->level_off[l]);
         }

@@ -4,7 +4,8 @@
 // A PMF is (first value, probabilities) on the context's step grid.  Events are
 // processed level by level (longest path from a source), two launches a level:
 // k_an_conv computes every convolution of the level, its outputs split into
-// chunks of 64 across CTAs (the FP64 multiply-adds are the bulk of the work);
+// one-warp chunks of 8 dealt out costliest first across the warps (the FP64
+// multiply-adds are the bulk of the work);
 // k_an_fold then takes one event per CTA:
 //   convolution along each incoming activity       _pmf.py:107-125
 //   maximum over the predecessors, pairwise in      _pmf.py:127-148
@@ -35,9 +36,10 @@ namespace mcd {
 namespace {
 
 constexpr int kAnThreads = 128;
-// Outputs (and threads) per convolution CTA: small CTAs spread a level's
-// multiply-adds evenly over the SMs (several CTAs per SM, no partial last wave).
-constexpr int kConvChunk = 64;
+// Outputs (and threads) per convolution chunk and CTA, and convolution CTAs per SM.
+constexpr int kConvLanes = 4;                 // lanes per output
+constexpr int kConvOuts = 32 / kConvLanes;    // outputs per chunk (one warp)
+constexpr int kConvWarpsPerSm = 16;
 constexpr int64_t kAnSmemBins = 4096;  // 5 arrays x 4096 doubles = 160 KB of shared memory
 
 // Kernel-reported errors (the reference raises ValueError in each case).
@@ -191,27 +193,40 @@ __device__ __forceinline__ int64_t round_half_even(double x) { return (int64_t)r
 // Length of the convolution of a pred PMF of n entries with an activity PMF of m.
 __device__ __forceinline__ int64_t conv_len(int64_t n, int64_t m) { return n == 1 ? m : (m == 1 ? n : n + m - 1); }
 
-// One chunk of kConvChunk outputs of one convolution: chunks[blockIdx.x] =
-// (predecessor entry, chunk index).  Chunks past the convolution's actual length exit.
-__global__ void __launch_bounds__(kConvChunk) k_an_conv(const AnArgs A, const int2 *__restrict__ chunks) {
-    const int2 c = chunks[blockIdx.x];
+// One chunk of kConvOuts outputs of one convolution (predecessor entry c.x, chunk
+// index c.y), computed by one warp: kConvLanes lanes per output split its terms
+// and add their partial sums with shuffles.  A warp's FP64 multiply-adds issue at
+// the SM sub-partition's FP64 rate (a warp instruction per 64 clocks), so chunks
+// are kept small: the last chunks of a level then finish soon after the others.
+// Operands are read through the L1 cache (every chunk of a convolution reads the
+// same activity PMF and overlapping windows of the predecessor's).
+__device__ void conv_chunk(const AnArgs &A, int2 c) {
     const int32_t s = A.pred_src[c.x], k = A.pred_pmf[c.x];
     const int64_t n = A.out[s].len, m = A.pmf_off[k + 1] - A.pmf_off[k];
-    const int64_t j = (int64_t)c.y * kConvChunk + threadIdx.x;
-    if (j >= conv_len(n, m)) return;
+    const int lane = threadIdx.x & 31, sub = lane % kConvLanes;
+    const int64_t len = conv_len(n, m), j = (int64_t)c.y * kConvOuts + lane / kConvLanes;
     const double *p = A.pool + A.ev[s].pool_off, *q = A.pmf_probs + A.pmf_off[k];
-    double v;
-    if (n == 1) {
-        v = q[j] * p[0];
-    } else if (m == 1) {
-        v = p[j] * q[0];
-    } else {
-        const int64_t i0 = j - (m - 1) > 0 ? j - (m - 1) : 0, i1 = j < n - 1 ? j : n - 1;
-        double acc = 0.0;
-        for (int64_t i = i0; i <= i1; ++i) acc = fma(p[i], q[j - i], acc);
-        v = acc;
+    double *out = A.convbuf + A.conv_off[c.x];
+    if (n == 1 || m == 1) {  // the reference's scaled copies (_pmf.py:111-116)
+        if (j < len && sub == 0) out[j] = n == 1 ? __ldg(q + j) * __ldg(p) : __ldg(p + j) * __ldg(q);
+        return;
     }
-    A.convbuf[A.conv_off[c.x] + j] = v;
+    double acc = 0.0;
+    if (j < len) {
+        const int64_t i0 = j - (m - 1) > 0 ? j - (m - 1) : 0, i1 = j < n - 1 ? j : n - 1;
+        for (int64_t i = i0 + sub; i <= i1; i += kConvLanes) acc = fma(__ldg(p + i), __ldg(q + (j - i)), acc);
+    }
+#pragma unroll
+    for (int o = 1; o < kConvLanes; o <<= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+    if (j < len && sub == 0) out[j] = acc;
+}
+
+// Every convolution of a level.  A level's chunks differ in cost (a chunk at a
+// convolution's edge has few terms); the host lists them costliest first and each
+// warp takes every gridDim.x-th, so the warps' loads come out nearly equal without
+// a shared counter (one counter's atomics serialise at its L2 slice).
+__global__ void __launch_bounds__(32) k_an_conv(const AnArgs A, const int2 *__restrict__ chunks, int32_t n_chunks) {
+    for (int32_t ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) conv_chunk(A, chunks[ci]);
 }
 
 __global__ void __launch_bounds__(kAnThreads) k_an_fold(const AnArgs A, const int32_t *__restrict__ level_ev) {
@@ -613,6 +628,7 @@ int mcd_analytic_create(const mcd_analytic_desc *d, mcd_analytic **out) {
         int64_t scratch_max = 0, conv_max = 0;
         for (int32_t l = 1; l <= n_levels; ++l) {
             int64_t scratch = 0, smem_bins = 0, conv = 0;
+            std::vector<std::pair<int64_t, int2>> level_chunks;  // (estimated multiply-adds, chunk)
             for (int32_t e : by_level[l]) {
                 AnEv &r = ev[e];
                 if (r.gmax <= kAnSmemBins) {
@@ -627,9 +643,17 @@ int mcd_analytic_create(const mcd_analytic_desc *d, mcd_analytic **out) {
                     const int64_t len = n == 1 ? m : (m == 1 ? n : n + m - 1);
                     conv_off[p] = conv;
                     conv += (len + 1) / 2 * 2;
-                    for (int64_t c = 0; c * kConvChunk < len; ++c) chunks.push_back(make_int2((int)p, (int)c));
+                    for (int64_t c = 0; c * kConvOuts < len; ++c) {
+                        const int64_t jm = c * kConvOuts + kConvOuts / 2;  // the chunk's middle output
+                        const int64_t terms = (n == 1 || m == 1) ? 1
+                                                                 : (std::min(jm, n - 1) - std::max<int64_t>(0, jm - (m - 1)) + 1);
+                        level_chunks.emplace_back(std::max<int64_t>(terms, 1) * kConvOuts, make_int2((int)p, (int)c));
+                    }
                 }
             }
+            std::stable_sort(level_chunks.begin(), level_chunks.end(),
+                             [](const auto &x, const auto &y) { return x.first > y.first; });
+            for (const auto &lc : level_chunks) chunks.push_back(lc.second);
             scratch_max = std::max(scratch_max, scratch);
             conv_max = std::max(conv_max, conv);
             an->level_off.push_back((int32_t)level_ev.size());
@@ -696,11 +720,15 @@ int mcd_analytic_create(const mcd_analytic_desc *d, mcd_analytic **out) {
         cuda_check(cudaFuncSetAttribute(k_an_fold, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)(5 * kAnSmemBins * sizeof(double))),
                    "analytic shared memory");
+        int sms = 0;
+        cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, an->device), "device query");
         // every level's launches, captured once into a graph
         cuda_check(cudaStreamBeginCapture(an->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
         for (size_t l = 0; l + 1 < an->level_off.size(); ++l) {
             const int32_t nc = an->chunk_off[l + 1] - an->chunk_off[l], ne = an->level_off[l + 1] - an->level_off[l];
-            if (nc > 0) k_an_conv<<<nc, kConvChunk, 0, an->stream>>>(an->args, an->d_chunks + an->chunk_off[l]);
+            if (nc > 0)
+                k_an_conv<<<std::min(nc, sms * kConvWarpsPerSm), 32, 0, an->stream>>>(
+                    an->args, an->d_chunks + an->chunk_off[l], nc);
             if (ne > 0)
                 k_an_fold<<<ne, kAnThreads, an->level_smem[l], an->stream>>>(an->args, an->d_level_ev + an->level_off[l]);
         }

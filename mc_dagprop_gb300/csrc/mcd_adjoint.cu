@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(768) k_adjoint(const KArgs a) {
             const int i = i_next;
             if (lane == 0) i_next = take_next(ctr);
             const EvRec ev = load_ev(sev + i);
-            const int64_t o = (int64_t)ev.user * a.ld + s;
+            const int64_t o = (int64_t)row_off(ev.user, (uint32_t)a.ld) + s;
             const uint32_t code = active ? (uint32_t)a.adj_code[o] : kAdjNone;
             const float dfac = active ? a.adj_dfac[o] : 0.0f;
             const uint32_t k = code & kAdjNone;

@@ -292,8 +292,8 @@ __device__ __forceinline__ EvRec load_ev(const EvRec *p) {
     r.pred_begin = a.z;
     r.pred_end = a.w;
     r.init_bits = (int64_t)(((uint64_t)(uint32_t)b.y << 32) | (uint32_t)b.x);
-    r.init_key = (int64_t)(((uint64_t)(uint32_t)b.w << 32) | (uint32_t)b.z);
-    r.ub_bits = (int64_t)(((uint64_t)(uint32_t)c.y << 32) | (uint32_t)c.x);
+    r.ub_bits = (int64_t)(((uint64_t)(uint32_t)b.w << 32) | (uint32_t)b.z);
+    r.init_key = (int64_t)(((uint64_t)(uint32_t)c.y << 32) | (uint32_t)c.x);
     r.ub_key = (int64_t)(((uint64_t)(uint32_t)c.w << 32) | (uint32_t)c.z);
     return r;
 }
@@ -422,6 +422,10 @@ __device__ __forceinline__ void accumulate_sum(const KArgs &a, const EvRec &ev, 
 }
 
 // ---------------------------------------------------------------- stage bodies
+// Offset of row `row` (>= 0) in rows of ld elements: one 32 x 32 -> 64-bit
+// multiply (leading dimensions are below 2^32, checked by the host).
+__device__ __forceinline__ uint64_t row_off(int32_t row, uint32_t ld) { return (uint64_t)(uint32_t)row * ld; }
+
 // A tile's per-lane state: its sample, seed, and output columns.
 struct TileCtx {
     int lane;
@@ -430,10 +434,11 @@ struct TileCtx {
     unsigned active_mask;
     uint64_t seed;
     double *rows;              // global realized rows (window off chip, or output), or null
-    int64_t rows_ld, rcol;
+    uint32_t rows_ld;
+    int64_t rcol;
     double *dcol;              // durations output column of this lane (null: none, or inactive)
     int32_t *ccol;             // cause_event output column of this lane (null: none, or inactive)
-    int64_t ld;                // leading dimension of the outputs
+    uint32_t ld;               // leading dimension of the outputs
 };
 
 // Lane 0 takes the next event index of a stage from its shared-memory counter.
@@ -482,15 +487,15 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec 
             double dur;
             float dfac = 0.0f;
             if (GIVEN) {
-                dur = (t.active && pr.link >= 0) ? __ldg(&a.dur_in[(int64_t)pr.link * a.ld_in + t.s]) : 0.0;
+                dur = (t.active && pr.link >= 0) ? __ldg(&a.dur_in[row_off(pr.link, (uint32_t)a.ld_in) + t.s]) : 0.0;
             } else {
                 dur = link_duration<STAGED>(a, pr.kd, pr.v, pr.dvo, (uint32_t)pr.block, (uint32_t)pr.link, t.seed,
                                             grp, smem, l, dfac);
-                if (!STATS && !ADJ && (pr.kd & KD_WRITE) && t.dcol) t.dcol[(int64_t)pr.link * t.ld] = dur;
+                if (!STATS && !ADJ && (pr.kd & KD_WRITE) && t.dcol) t.dcol[row_off(pr.link, t.ld)] = dur;
             }
             // with the window on chip every source has a slot (the compiler checks it)
             const double src = WIN_SMEM ? win[pr.src_slot * kTile + lane]
-                                        : (t.active ? t.rows[(int64_t)pr.src_user * t.rows_ld + t.rcol] : 0.0);
+                                        : (t.active ? t.rows[row_off(pr.src_user, t.rows_ld) + t.rcol] : 0.0);
             const double tt = src + dur;  // the one FP64 add of the edge (_core.cpp:341)
             long long tb = __double_as_longlong(tt);
             long long tk = order_key<POSITIVE>(tb);
@@ -519,13 +524,13 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec 
             const bool delayed = lk > (POSITIVE ? ev.init_bits : ev.init_key);  // realized > earliest
             accumulate_sum<POSITIVE>(a, ev, lbits, te, t.active);
             if (t.active) {
-                const int64_t o = (int64_t)ev.user * a.ld + t.s;
+                const int64_t o = (int64_t)row_off(ev.user, (uint32_t)a.ld) + t.s;
                 a.adj_code[o] = (uint16_t)(win_code | (delayed ? kAdjDelayed : 0u));
                 a.adj_dfac[o] = win_dfac;
             }
         }
-        if (t.active && t.rows) t.rows[(int64_t)ev.user * t.rows_ld + t.rcol] = real;
-        if (!STATS && !ADJ && t.ccol) t.ccol[(int64_t)ev.user * t.ld] = cause;
+        if (t.active && t.rows) t.rows[row_off(ev.user, t.rows_ld) + t.rcol] = real;
+        if (!STATS && !ADJ && t.ccol) t.ccol[row_off(ev.user, t.ld)] = cause;
         i_next = __shfl_sync(0xFFFFFFFFu, i_next, 0);
     }
 }
@@ -568,9 +573,9 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
     t.seed = 0;
     if (!GIVEN && t.active) t.seed = a.seeds ? (uint64_t)a.seeds[t.s] : (uint64_t)(a.seed0 + t.s);
     t.rows = rows;
-    t.rows_ld = rows_ld;
+    t.rows_ld = (uint32_t)rows_ld;
     t.rcol = rows_tile_local ? (int64_t)t.lane : t.s;
-    t.ld = a.ld;
+    t.ld = (uint32_t)a.ld;
     t.dcol = (!STATS && !ADJ && !GIVEN && a.durations && t.active) ? a.durations + t.s : nullptr;
     t.ccol = (!STATS && !ADJ && a.cause && t.active) ? a.cause + t.s : nullptr;
 
@@ -638,7 +643,7 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
             U4 own;  // an unreferenced link owns its block
             const double dur =
                 link_duration<false>(a, lr.kd, lr.v, -1, (uint32_t)lr.link, (uint32_t)lr.link, t.seed, own, smem, 0, dfac);
-            if (t.dcol) t.dcol[(int64_t)lr.link * t.ld] = dur;
+            if (t.dcol) t.dcol[row_off(lr.link, t.ld)] = dur;
         }
     }
     return true;

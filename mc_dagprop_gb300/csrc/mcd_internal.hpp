@@ -60,8 +60,10 @@ struct alignas(16) EvRec {
     int32_t pred_begin;  // range in the PredRec array
     int32_t pred_end;
     int64_t init_bits;   // earliest (bits): the running max starts here (_core.cpp:336)
-    int64_t init_key;    // order key of earliest; INT64_MAX when earliest is NaN
     int64_t ub_bits;     // earliest + max_delay (bits), evaluated on the host (_core.cpp:334)
+    // (the keys last: with all times non-negative and finite the bits are the keys,
+    // and the kernels skip this third 16-byte load)
+    int64_t init_key;    // order key of earliest; INT64_MAX when earliest is NaN
     int64_t ub_key;      // order key of ub; INT64_MAX when ub is NaN (std::min then keeps t)
 };
 

@@ -29,7 +29,7 @@
  * layout: one contiguous row per sample, realized[s*E + e], durations[s*L + l],
  * cause_event[s*E + e].  "Sample-minor" (device entry points) is the GPU layout:
  * one row per event / link with samples contiguous, realized[e*ld + s],
- * durations[l*ld + s], cause_event[e*ld + s], n_samples <= ld < 2^32.
+ * durations[l*ld + s], cause_event[e*ld + s], n_samples <= ld < 2^29.
  *
  * Random numbers.  Each sample s is identified by a 64-bit seed; delays are drawn
  * from Philox4x32-10 keyed by that seed with the link index in the counter, so a

@@ -573,7 +573,7 @@ int mcd_run_device(mcd_dag *g, const int64_t *seeds, int64_t n, double *realized
                    int32_t *cause, int64_t ld, void *stream) {
     return guarded([&] {
         if (!g) throw McdError(MCD_ERR_INVALID, "null handle");
-        if (n < 0 || ld < n || ld > (int64_t)UINT32_MAX) throw McdError(MCD_ERR_INVALID, "need 0 <= n <= ld < 2^32");
+        if (n < 0 || ld < n || ld >= ((int64_t)1 << 29)) throw McdError(MCD_ERR_INVALID, "need 0 <= n <= ld < 2^29");
         if (n > 0 && !seeds) throw McdError(MCD_ERR_INVALID, "null seeds");
         cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
         cudaStream_t st = stream ? (cudaStream_t)stream : g->stream[0];
@@ -596,8 +596,8 @@ int mcd_propagate_device(mcd_dag *g, const double *dur, int64_t ld_in, int64_t n
                          int32_t *cause, int64_t ld, void *stream) {
     return guarded([&] {
         if (!g) throw McdError(MCD_ERR_INVALID, "null handle");
-        if (n < 0 || ld < n || ld_in < n || ld > (int64_t)UINT32_MAX || ld_in > (int64_t)UINT32_MAX)
-            throw McdError(MCD_ERR_INVALID, "need 0 <= n <= ld, ld_in < 2^32");
+        if (n < 0 || ld < n || ld_in < n || ld >= ((int64_t)1 << 29) || ld_in >= ((int64_t)1 << 29))
+            throw McdError(MCD_ERR_INVALID, "need 0 <= n <= ld, ld_in < 2^29");
         if (n > 0 && g->h.L > 0 && !dur) throw McdError(MCD_ERR_INVALID, "null durations");
         cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
         cudaStream_t st = stream ? (cudaStream_t)stream : g->stream[0];

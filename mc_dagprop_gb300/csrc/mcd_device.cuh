@@ -426,6 +426,14 @@ __device__ __forceinline__ void accumulate_sum(const KArgs &a, const EvRec &ev, 
 // multiply (leading dimensions are below 2^32, checked by the host).
 __device__ __forceinline__ uint64_t row_off(int32_t row, uint32_t ld) { return (uint64_t)(uint32_t)row * ld; }
 
+// Element `row` (>= 0) of a column whose rows are ld_bytes apart: one 32 x 32-bit
+// multiply-add onto the 64-bit column address (row pitches below 2^32 bytes: the
+// host keeps leading dimensions below 2^29).
+template <typename T>
+__device__ __forceinline__ T *at_row(T *col, int32_t row, uint32_t ld_bytes) {
+    return reinterpret_cast<T *>(reinterpret_cast<uintptr_t>(col) + (uint64_t)(uint32_t)row * ld_bytes);
+}
+
 // A tile's per-lane state: its sample, seed, and output columns.
 struct TileCtx {
     int lane;
@@ -433,12 +441,14 @@ struct TileCtx {
     bool active;               // s < n
     unsigned active_mask;
     uint64_t seed;
-    double *rows;              // global realized rows (window off chip, or output), or null
-    uint32_t rows_ld;
-    int64_t rcol;
+    double *rcol;              // this lane's column of the global realized rows (window off chip, or
+                               // output), or null
+    uint32_t rows_ld8;         // their row pitch in bytes
     double *dcol;              // durations output column of this lane (null: none, or inactive)
     int32_t *ccol;             // cause_event output column of this lane (null: none, or inactive)
-    uint32_t ld;               // leading dimension of the outputs
+    uint32_t ld8, ld4;         // row pitches of the outputs in bytes (doubles, int32)
+    const double *dincol;      // given durations: this lane's column (GIVEN)
+    uint32_t ld_in8;
 };
 
 // Lane 0 takes the next event index of a stage from its shared-memory counter.
@@ -487,15 +497,15 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec 
             double dur;
             float dfac = 0.0f;
             if (GIVEN) {
-                dur = (t.active && pr.link >= 0) ? __ldg(&a.dur_in[row_off(pr.link, (uint32_t)a.ld_in) + t.s]) : 0.0;
+                dur = (t.active && pr.link >= 0) ? __ldg(at_row(t.dincol, pr.link, t.ld_in8)) : 0.0;
             } else {
                 dur = link_duration<STAGED>(a, pr.kd, pr.v, pr.dvo, (uint32_t)pr.block, (uint32_t)pr.link, t.seed,
                                             grp, smem, l, dfac);
-                if (!STATS && !ADJ && (pr.kd & KD_WRITE) && t.dcol) t.dcol[row_off(pr.link, t.ld)] = dur;
+                if (!STATS && !ADJ && (pr.kd & KD_WRITE) && t.dcol) *at_row(t.dcol, pr.link, t.ld8) = dur;
             }
             // with the window on chip every source has a slot (the compiler checks it)
             const double src = WIN_SMEM ? win[pr.src_slot * kTile + lane]
-                                        : (t.active ? t.rows[row_off(pr.src_user, t.rows_ld) + t.rcol] : 0.0);
+                                        : (t.active ? *at_row(t.rcol, pr.src_user, t.rows_ld8) : 0.0);
             const double tt = src + dur;  // the one FP64 add of the edge (_core.cpp:341)
             long long tb = __double_as_longlong(tt);
             long long tk = order_key<POSITIVE>(tb);
@@ -529,8 +539,8 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec 
                 a.adj_dfac[o] = win_dfac;
             }
         }
-        if (t.active && t.rows) t.rows[row_off(ev.user, t.rows_ld) + t.rcol] = real;
-        if (!STATS && !ADJ && t.ccol) t.ccol[row_off(ev.user, t.ld)] = cause;
+        if (t.active && t.rcol) *at_row(t.rcol, ev.user, t.rows_ld8) = real;
+        if (!STATS && !ADJ && t.ccol) *at_row(t.ccol, ev.user, t.ld4) = cause;
         i_next = __shfl_sync(0xFFFFFFFFu, i_next, 0);
     }
 }
@@ -572,10 +582,12 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
     t.active_mask = __ballot_sync(0xFFFFFFFFu, t.active);
     t.seed = 0;
     if (!GIVEN && t.active) t.seed = a.seeds ? (uint64_t)a.seeds[t.s] : (uint64_t)(a.seed0 + t.s);
-    t.rows = rows;
-    t.rows_ld = (uint32_t)rows_ld;
-    t.rcol = rows_tile_local ? (int64_t)t.lane : t.s;
-    t.ld = (uint32_t)a.ld;
+    t.rcol = rows ? rows + (rows_tile_local ? (int64_t)t.lane : t.s) : nullptr;
+    t.rows_ld8 = (uint32_t)rows_ld * 8u;
+    t.ld8 = (uint32_t)a.ld * 8u;
+    t.ld4 = (uint32_t)a.ld * 4u;
+    t.dincol = GIVEN ? a.dur_in + t.s : nullptr;
+    t.ld_in8 = (uint32_t)a.ld_in * 8u;
     t.dcol = (!STATS && !ADJ && !GIVEN && a.durations && t.active) ? a.durations + t.s : nullptr;
     t.ccol = (!STATS && !ADJ && a.cause && t.active) ? a.cause + t.s : nullptr;
 
@@ -643,7 +655,7 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
             U4 own;  // an unreferenced link owns its block
             const double dur =
                 link_duration<false>(a, lr.kd, lr.v, -1, (uint32_t)lr.link, (uint32_t)lr.link, t.seed, own, smem, 0, dfac);
-            if (t.dcol) t.dcol[row_off(lr.link, t.ld)] = dur;
+            if (t.dcol) *at_row(t.dcol, lr.link, t.ld8) = dur;
         }
     }
     return true;

@@ -621,7 +621,20 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
         if (a.n_stages > 1) stage_issue(a, 1, stage_buf0 + a.stage_bytes, &bars[1]);
     }
 
+    // a stage's metadata is loaded one stage ahead: its latency then hides behind
+    // the previous stage's events instead of stalling every warp at the stage start
+    const int4 *smeta = reinterpret_cast<const int4 *>(a.stage_meta);
+    int4 meta_next = make_int4(0, 0, 0, 0), mv_next = make_int4(0, 0, 0, 0);
+    if (a.n_stages > 0) {
+        meta_next = __ldg(smeta);
+        mv_next = __ldg(smeta + 1);
+    }
     for (int l = 0; l < a.n_stages; ++l) {
+        const int4 meta = meta_next, mv = mv_next;
+        if (l + 1 < a.n_stages) {
+            meta_next = __ldg(smeta + 2 * (l + 1));
+            mv_next = __ldg(smeta + 2 * (l + 1) + 1);
+        }
         const int b = l & 1;
         const bool ok = stage_wait(&bars[b], (uint32_t)((l >> 1) & 1), a.err);
         if (__syncthreads_or(!ok)) {  // a copy that never landed: drain, then leave together
@@ -630,8 +643,6 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
             __syncthreads();
             return false;
         }
-        const int4 meta = __ldg(reinterpret_cast<const int4 *>(a.stage_meta) + 2 * l);
-        const int4 mv = __ldg(reinterpret_cast<const int4 *>(a.stage_meta) + 2 * l + 1);
         if (threadIdx.x == 0) stage_ctr[(l + 1) & 1] = 0;  // last used by stage l - 1, before the barrier
         const uint32_t ctr = smem_u32(&stage_ctr[l & 1]);
         if (meta.y >= 0) {  // records in the staging buffer (shared memory)

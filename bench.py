@@ -410,8 +410,10 @@ def run_gradient(args):
         "config": {"workload": "10,000 events (100 layers x 100), five delay kinds, gradient of "
                                "mean_s sum_e (realized - earliest) w.r.t. every earliest and minimal_duration",
                    "samples": n, "links": L, "objective": g["objective"]},
-        "fd_check": {"coordinates": len(errs), "step_s": h, "max_rel_err": float(np.max(errs)),
-                     "median_rel_err": float(np.median(errs)), "metric": "|fd - adjoint| / (1 + |fd|)"},
+        "fd_check": {"coordinates": len(errs), "step_s": h,
+                     "max_rel_err": float(np.max(errs)) if errs else None,
+                     "median_rel_err": float(np.median(errs)) if errs else None,
+                     "metric": "|fd - adjoint| / (1 + |fd|)"},
     }))
     return 0
 

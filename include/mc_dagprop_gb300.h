@@ -205,7 +205,7 @@ int mcd_stats_device(mcd_dag *dag, const int64_t *seeds, int64_t seed0, int64_t 
  * another allocator (a framework's caching allocator that has reserved the
  * device), or an allocation would synchronise the device inside their
  * latency-critical loop.  This entry point keeps the per-event accumulators in a
- * fixed 32 MiB device array that the library holds on every GPU it is loaded on
+ * fixed 34 MiB device array that the library holds on every GPU it is loaded on
  * until the process exits, so it supports DAGs of at most MCD_NOALLOC_MAX_EVENTS
  * events whose propagation window fits in shared memory (larger ones fail with
  * MCD_ERR_INVALID).  Inputs, outputs and the compiled DAG are the caller's, as in

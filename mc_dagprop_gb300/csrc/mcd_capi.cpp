@@ -858,7 +858,7 @@ int mcd_stats_host(mcd_dag *g, const int64_t *seeds, int64_t seed0, int64_t n, c
 }
 
 // Statistics without any device allocation: the per-event accumulators live in
-// the library's fixed 32 MiB device array instead of the handle's workspace.
+// the library's fixed 34 MiB device array instead of the handle's workspace.
 // For callers that cannot allocate (their device memory belongs to another
 // allocator, or a cudaMalloc would stall their latency-critical loop).  The
 // first call on a device looks the array's address up; calls share the array,

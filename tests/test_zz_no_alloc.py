@@ -4,7 +4,7 @@ Some callers cannot call cudaMalloc: their GPU memory already belongs to another
 allocator (for example a framework's caching allocator that has reserved the
 device), or an allocation would synchronise the device in the middle of their
 latency-critical loop.  For them the library keeps the statistics accumulators
-in one fixed 32 MiB device array (DAGs up to MCD_NOALLOC_MAX_EVENTS events).
+in one fixed 34 MiB device array (DAGs up to MCD_NOALLOC_MAX_EVENTS events).
 
 This test calls the entry point through the C ABI, twice in a row on the same
 handle (the array keeps the previous call's contents, so the second call checks

@@ -40,7 +40,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUD
 
 HOST_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 
-SOURCES_CU = ["mcd_kernels.cu", "mcd_prop_sample.cu", "mcd_prop_given.cu", "mcd_adjoint.cu", "mcd_analytic.cu", "mcd_inspect.cu"]
+SOURCES_CU = ["mcd_kernels.cu", "mcd_prop_sample.cu", "mcd_prop_sample_gt.cu", "mcd_prop_given.cu", "mcd_adjoint.cu",
+              "mcd_analytic.cu", "mcd_inspect.cu"]
 SOURCES_CPP = ["mcd_compile.cpp", "mcd_capi.cpp", "mcd_batch.cpp", "mcd_grad.cpp", "mcd_server.cpp"]
 HEADERS = ["mcd_internal.hpp", "mcd_host.hpp", "mcd_device.cuh", "mcd_handle.hpp"]
 

@@ -254,7 +254,11 @@ __device__ __forceinline__ double sampled_duration(const KArgs &a, int32_t kd, d
 // duration table (STAGED; otherwise the table is in KArgs::vals).  Every table
 // address is derived here from the kernel arguments, so that the propagation
 // loop keeps no table pointers live.
-template <bool STAGED>
+// TS: where the tables block is -- kTablesGlobal, kTablesSmem (fixed for the
+// kernel: one copy of the samplers, no branch per edge), or kTablesEither
+// (KArgs::tables_in_smem decides per launch or per DAG).
+enum : int { kTablesGlobal = 0, kTablesSmem = 1, kTablesEither = 2 };
+template <bool STAGED, int TS>
 __device__ __forceinline__ double link_duration(const KArgs &a, int32_t kd, double v, int32_t dvo, uint32_t block,
                                                 uint32_t link, uint64_t seed, U4 &grp, const unsigned char *smem,
                                                 int stage, float &dfac) {
@@ -262,7 +266,8 @@ __device__ __forceinline__ double link_duration(const KArgs &a, int32_t kd, doub
         dfac = __int_as_float(dvo);
         return v;
     }
-    if (a.tables_in_smem) return sampled_duration<STAGED, true>(a, kd, v, dvo, block, link, seed, grp, smem, stage, dfac);
+    if (TS == kTablesSmem || (TS == kTablesEither && a.tables_in_smem))
+        return sampled_duration<STAGED, true>(a, kd, v, dvo, block, link, seed, grp, smem, stage, dfac);
     return sampled_duration<STAGED, false>(a, kd, v, dvo, block, link, seed, grp, smem, stage, dfac);
 }
 
@@ -466,7 +471,7 @@ __device__ __forceinline__ int take_next(uint32_t ctr) {
 // staging buffer in shared memory; otherwise into global memory.  pred0: the
 // stage's first predecessor record (the records' pred_begin/pred_end are
 // global indices).
-template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ, bool STAGED>
+template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ, bool STAGED, int TS>
 __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec *sev, const PredRec *spred, int pred0,
                                              int n_ev, uint32_t ctr, const TileCtx &t, unsigned char *smem,
                                              U4 &grp) {
@@ -499,7 +504,7 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec 
             if (GIVEN) {
                 dur = (t.active && pr.link >= 0) ? __ldg(at_row(t.dincol, pr.link, t.ld_in8)) : 0.0;
             } else {
-                dur = link_duration<STAGED>(a, pr.kd, pr.v, pr.dvo, (uint32_t)pr.block, (uint32_t)pr.link, t.seed,
+                dur = link_duration<STAGED, TS>(a, pr.kd, pr.v, pr.dvo, (uint32_t)pr.block, (uint32_t)pr.link, t.seed,
                                             grp, smem, l, dfac);
                 if (!STATS && !ADJ && (pr.kd & KD_WRITE) && t.dcol) *at_row(t.dcol, pr.link, t.ld8) = dur;
             }
@@ -567,7 +572,7 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec 
 // ADJ: the forward half of the adjoint: per event and sample, the winning
 // predecessor's position, clamp and delay flags and d(duration)/d(base) go to
 // a.adj_code / a.adj_dfac, and (realized - earliest) to the objective sum.
-template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ = false>
+template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ = false, int TS = kTablesEither>
 __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, double *rows, int64_t rows_ld,
                                                bool rows_tile_local, unsigned char *smem, uint64_t *bars,
                                                bool reuse) {
@@ -647,11 +652,11 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
         const uint32_t ctr = smem_u32(&stage_ctr[l & 1]);
         if (meta.y >= 0) {  // records in the staging buffer (shared memory)
             const unsigned char *buf = smem + a.smem_stage_off + b * a.stage_bytes;
-            stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, true>(
+            stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, true, TS>(
                 a, l, reinterpret_cast<const EvRec *>(buf), reinterpret_cast<const PredRec *>(buf + mv.z), meta.z,
                 meta.y, ctr, t, smem, grp);
         } else {  // a stage whose records exceed the buffer is read from global memory
-            stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, false>(a, l, a.ev + meta.x, a.pred + meta.z, meta.z,
+            stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, false, TS>(a, l, a.ev + meta.x, a.pred + meta.z, meta.z,
                                                                        -meta.y, ctr, t, smem, grp);
         }
         __syncthreads();
@@ -665,21 +670,23 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
             float dfac;
             U4 own;  // an unreferenced link owns its block
             const double dur =
-                link_duration<false>(a, lr.kd, lr.v, -1, (uint32_t)lr.link, (uint32_t)lr.link, t.seed, own, smem, 0, dfac);
+                link_duration<false, TS>(a, lr.kd, lr.v, -1, (uint32_t)lr.link, (uint32_t)lr.link, t.seed, own, smem, 0, dfac);
             if (t.dcol) *at_row(t.dcol, lr.link, t.ld8) = dur;
         }
     }
     return true;
 }
 
-// One CTA per tile of 32 samples.
-template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE>
+// One CTA per tile of 32 samples.  TS: the tables block's place (kTablesGlobal or
+// kTablesSmem; the host launches the instantiation that matches the DAG).
+template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, int TS>
 __global__ void __launch_bounds__(768) k_propagate(const KArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     double *rows = a.realized ? a.realized : a.scratch;  // global realized rows
     if (STATS && WIN_SMEM) rows = nullptr;
-    propagate_tile<GIVEN, WIN_SMEM, STATS, POSITIVE>(a, (int64_t)blockIdx.x, rows, a.ld, false, smem,
-                                                     reinterpret_cast<uint64_t *>(smem + a.smem_bar_off), false);
+    propagate_tile<GIVEN, WIN_SMEM, STATS, POSITIVE, false, TS>(a, (int64_t)blockIdx.x, rows, a.ld, false, smem,
+                                                                reinterpret_cast<uint64_t *>(smem + a.smem_bar_off),
+                                                                false);
 }
 
 }  // namespace mcd

@@ -51,15 +51,23 @@ static void (*batch_kernel(bool win_smem, bool positive))(const BatchArgs) {
     return positive ? k_batch_stats<false, true> : k_batch_stats<false, false>;
 }
 
+cudaError_t launch_prop_sample_gt(const KArgs &a, bool win_smem, bool stats, bool positive, dim3 grid, dim3 block,
+                                  size_t smem, cudaStream_t st);
+
+// DAGs whose tables block sits in shared memory (all but those with very large
+// empirical tables) run these; the others the kTablesGlobal instantiations of
+// mcd_prop_sample_gt.cu.
 cudaError_t launch_prop_sample(const KArgs &a, bool win_smem, bool stats, bool positive, dim3 grid, dim3 block,
                                size_t smem, cudaStream_t st) {
+    if (!a.tables_in_smem) return launch_prop_sample_gt(a, win_smem, stats, positive, grid, block, smem, st);
+    constexpr int S = kTablesSmem;
     void (*fn)(const KArgs);
     if (stats) {
-        if (positive) fn = win_smem ? k_propagate<false, true, true, true> : k_propagate<false, false, true, true>;
-        else fn = win_smem ? k_propagate<false, true, true, false> : k_propagate<false, false, true, false>;
+        if (positive) fn = win_smem ? k_propagate<false, true, true, true, S> : k_propagate<false, false, true, true, S>;
+        else fn = win_smem ? k_propagate<false, true, true, false, S> : k_propagate<false, false, true, false, S>;
     } else {
-        if (positive) fn = win_smem ? k_propagate<false, true, false, true> : k_propagate<false, false, false, true>;
-        else fn = win_smem ? k_propagate<false, true, false, false> : k_propagate<false, false, false, false>;
+        if (positive) fn = win_smem ? k_propagate<false, true, false, true, S> : k_propagate<false, false, false, true, S>;
+        else fn = win_smem ? k_propagate<false, true, false, false, S> : k_propagate<false, false, false, false, S>;
     }
     const cudaError_t e = raise_smem_limit((const void *)fn, smem);
     if (e != cudaSuccess) return e;

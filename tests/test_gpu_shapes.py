@@ -132,3 +132,33 @@ def test_zero_samples_and_empty_seed_lists(cuda):
     r, d, c = prop.run_many_arrays(np.zeros(0, np.int64))
     assert r.shape == (0, prop.node_count()) and d.shape == (0, prop.activity_count()) and c.shape == r.shape
     assert prop.run_many([]) == []
+
+
+def test_tables_in_global_memory(cuda):
+    """Distribution tables too large for shared memory (a 1,000-bin empirical table)
+    run the kernels that read them from global memory: bit-exact propagation of the
+    sampled durations, durations that are the reference's base + value, and draw
+    frequencies that follow the weights."""
+    rng = np.random.default_rng(77)
+    values = np.arange(1000, dtype=np.float64) * 0.5
+    weights = rng.random(1000) + 0.05
+    gen = [("empirical_absolute", 1, values, weights), ("exponential", 2, 0.2, 4.0)]
+    flat = W.layered_dag(3, 20, 30, 2, [1, 2], 100.0)
+    prop = propagator_from_flat(m, flat, gen)
+    assert prop.info()["tables_in_smem"] is False
+    sim = oracle.OracleSim(flat, gen)
+    seeds = np.arange(20_000, dtype=np.int64)
+    r, d, c = prop.run_many_arrays(seeds)
+    ro, co = sim.propagate_given(d)
+    assert np.array_equal(_bits(r), _bits(ro))
+    assert np.array_equal(c, co)
+    emp = np.asarray(flat["act_type"]) == 1
+    idx = np.asarray(flat["act_idx"])[emp]
+    base = np.asarray(flat["act_duration"])[emp]
+    delay = d[:, idx] - base[None, :]
+    k = np.rint(delay / 0.5).astype(np.int64)
+    assert np.all((k >= 0) & (k < 1000))
+    assert np.array_equal(_bits(d[:, idx]), _bits(base[None, :] + values[k]))  # base + v, as the reference adds
+    freq = np.bincount(k.ravel(), minlength=1000) / k.size
+    p = weights / weights.sum()
+    assert np.max(np.abs(freq - p)) < 8 * np.sqrt(p.max() / k.size)

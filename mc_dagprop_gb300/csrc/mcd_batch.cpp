@@ -4,7 +4,8 @@
 // (longest-processing-time order), consumed by a persistent grid of CTAs that
 // fills every SM whatever the DAGs' sizes -- a plain per-DAG launch of a DAG
 // with 1,000 samples keeps 32 CTAs busy and leaves the rest of the GPU idle.
-// DAGs are grouped by kernel variant (window on chip or not, positive times or
+// DAGs are grouped by kernel variant (window on chip or not, tables in shared
+// memory or not, positive times or
 // not); each group is one launch with its own queue.  Each run is one CUDA
 // graph: reset the accumulators and the queue heads, the persistent statistics
 // launches, the batched finish.  The graph is recorded on the first run and
@@ -20,9 +21,10 @@
 #include "mcd_handle.hpp"
 
 namespace mcd {
-cudaError_t launch_batch_stats(const BatchArgs &b, bool win_smem, bool positive, int n_warps, size_t smem, int grid,
+cudaError_t launch_batch_stats(const BatchArgs &b, bool win_smem, bool positive, bool tsmem, int n_warps, size_t smem,
+                               int grid,
                                cudaStream_t st);
-cudaError_t batch_blocks_per_sm(bool win_smem, bool positive, int n_warps, size_t smem, int *out);
+cudaError_t batch_blocks_per_sm(bool win_smem, bool positive, bool tsmem, int n_warps, size_t smem, int *out);
 cudaError_t launch_batch_finish(const FArgs *fs, int32_t n_dags, int32_t max_events, cudaStream_t st);
 }  // namespace mcd
 
@@ -31,7 +33,7 @@ using namespace mcd;
 namespace {
 // One persistent launch: the DAGs of one kernel variant.
 struct Launch {
-    bool win_smem = true, positive = true;
+    bool win_smem = true, positive = true, tsmem = true;
     std::vector<int32_t> dags;
     size_t smem = 0;
     int grid = 1;
@@ -91,12 +93,13 @@ int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0,
             B->ev_off[i + 1] = B->ev_off[i] + h.E;
             Launch *L = nullptr;
             for (Launch &x : B->launches)
-                if (x.win_smem == h.win_smem && x.positive == h.positive) L = &x;
+                if (x.win_smem == h.win_smem && x.positive == h.positive && x.tsmem == h.tables_in_smem) L = &x;
             if (!L) {
                 B->launches.emplace_back();
                 L = &B->launches.back();
                 L->win_smem = h.win_smem;
                 L->positive = h.positive;
+                L->tsmem = h.tables_in_smem;
             }
             L->dags.push_back(i);
             L->smem = std::max(L->smem, (size_t)h.smem_total);
@@ -113,7 +116,8 @@ int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0,
         B->grid = 0;
         for (Launch &L : B->launches) {
             int per_sm = 0;
-            cuda_check(batch_blocks_per_sm(L.win_smem, L.positive, B->n_warps, L.smem, &per_sm), "occupancy query");
+            cuda_check(batch_blocks_per_sm(L.win_smem, L.positive, L.tsmem, B->n_warps, L.smem, &per_sm),
+                       "occupancy query");
             L.grid = std::max(1, per_sm) * std::max(1, sms);
             B->grid += L.grid;
             std::stable_sort(L.dags.begin(), L.dags.end(), [&](int32_t x, int32_t y) { return cost(x) > cost(y); });
@@ -241,7 +245,8 @@ int mcd_batch_run(mcd_batch *B) {
             cudaError_t e = cudaMemsetAsync(B->dmem, 0, B->zero_bytes, B->stream);
             for (const Launch &L : B->launches)
                 if (e == cudaSuccess)
-                    e = launch_batch_stats(L.args, L.win_smem, L.positive, B->n_warps, L.smem, L.grid, B->stream);
+                    e = launch_batch_stats(L.args, L.win_smem, L.positive, L.tsmem, B->n_warps, L.smem, L.grid,
+                                           B->stream);
             if (e == cudaSuccess)
                 e = launch_batch_finish(B->d_fargs, (int32_t)B->dags.size(), B->max_E, B->stream);
             cudaGraph_t graph = nullptr;
@@ -270,7 +275,7 @@ int mcd_batch_occupancy(int32_t n_warps, int64_t smem_bytes, int32_t *blocks_per
             smem_bytes > (int64_t)kSmemMax)
             throw McdError(MCD_ERR_INVALID, "bad arguments");
         int per_sm = 0;
-        cuda_check(batch_blocks_per_sm(true, true, n_warps, (size_t)smem_bytes, &per_sm), "occupancy query");
+        cuda_check(batch_blocks_per_sm(true, true, true, n_warps, (size_t)smem_bytes, &per_sm), "occupancy query");
         *blocks_per_sm = per_sm;
     });
 }

@@ -8,13 +8,14 @@ namespace mcd {
 // Persistent statistics kernel over a batch of DAGs: each CTA takes (DAG, tile)
 // items from an atomic work queue (ordered longest first by the host) until the
 // queue is empty.  No CTA waits on another: the queue head is a plain counter.
-// One instantiation per (window on chip, positive times): every DAG of a launch
-// shares both, so only one propagation variant is inlined (fewer registers).
+// One instantiation per (window on chip, positive times, tables in shared memory):
+// every DAG of a launch shares all three, so only one propagation variant is
+// inlined (fewer registers, one copy of the samplers).
 // DAGs whose window is not on chip use per-CTA scratch rows (32 samples each).
 // Each DAG has its own shared-memory layout; the barrier pair and the stage
 // counters live outside all of them, in static shared memory, so they never
 // move between items.
-template <bool WIN_SMEM, bool POSITIVE>
+template <bool WIN_SMEM, bool POSITIVE, bool TSMEM>
 __global__ void __launch_bounds__(768, 1) k_batch_stats(const BatchArgs b) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ KArgs s_args;
@@ -32,23 +33,27 @@ __global__ void __launch_bounds__(768, 1) k_batch_stats(const BatchArgs b) {
         const KArgs &a = s_args;
         // a layout larger than the launch's shared memory, or of another variant: never touch it
         if (a.smem_total > b.smem_bytes || (a.win_smem != 0) != WIN_SMEM || (a.positive != 0) != POSITIVE ||
-            a.n_warps * 32 != (int)blockDim.x) {
+            (a.tables_in_smem != 0) != TSMEM || a.n_warps * 32 != (int)blockDim.x) {
             if (threadIdx.x == 0) atomicOr(a.err, ERR_LAYOUT);
             __syncthreads();
             continue;
         }
         double *rows = WIN_SMEM ? nullptr : b.scratch + (int64_t)blockIdx.x * b.scratch_stride;
-        const bool ok = propagate_tile<false, WIN_SMEM, true, POSITIVE>(a, it.y, rows, WIN_SMEM ? 0 : kTile, true,
-                                                                         smem, s_bars, reuse);
+        const bool ok = propagate_tile<false, WIN_SMEM, true, POSITIVE, false, TSMEM ? kTablesSmem : kTablesGlobal>(
+            a, it.y, rows, WIN_SMEM ? 0 : kTile, true, smem, s_bars, reuse);
         reuse = true;
         if (!ok) return;
         __syncthreads();  // s_args / s_item are rewritten by the next item
     }
 }
 
-static void (*batch_kernel(bool win_smem, bool positive))(const BatchArgs) {
-    if (win_smem) return positive ? k_batch_stats<true, true> : k_batch_stats<true, false>;
-    return positive ? k_batch_stats<false, true> : k_batch_stats<false, false>;
+static void (*batch_kernel(bool win_smem, bool positive, bool tsmem))(const BatchArgs) {
+    if (tsmem) {
+        if (win_smem) return positive ? k_batch_stats<true, true, true> : k_batch_stats<true, false, true>;
+        return positive ? k_batch_stats<false, true, true> : k_batch_stats<false, false, true>;
+    }
+    if (win_smem) return positive ? k_batch_stats<true, true, false> : k_batch_stats<true, false, false>;
+    return positive ? k_batch_stats<false, true, false> : k_batch_stats<false, false, false>;
 }
 
 cudaError_t launch_prop_sample_gt(const KArgs &a, bool win_smem, bool stats, bool positive, dim3 grid, dim3 block,
@@ -76,9 +81,9 @@ cudaError_t launch_prop_sample(const KArgs &a, bool win_smem, bool stats, bool p
 }
 
 // Persistent batch launch: one CTA per SM slot, `blocks_per_sm` of them per SM.
-cudaError_t launch_batch_stats(const BatchArgs &b, bool win_smem, bool positive, int n_warps, size_t smem, int grid,
-                               cudaStream_t st) {
-    void (*fn)(const BatchArgs) = batch_kernel(win_smem, positive);
+cudaError_t launch_batch_stats(const BatchArgs &b, bool win_smem, bool positive, bool tsmem, int n_warps, size_t smem,
+                               int grid, cudaStream_t st) {
+    void (*fn)(const BatchArgs) = batch_kernel(win_smem, positive, tsmem);
     const cudaError_t e = raise_smem_limit((const void *)fn, smem);
     if (e != cudaSuccess) return e;
     fn<<<grid, n_warps * 32, smem, st>>>(b);
@@ -86,8 +91,8 @@ cudaError_t launch_batch_stats(const BatchArgs &b, bool win_smem, bool positive,
 }
 
 // CTAs of the batch kernel that fit on one SM at this block size and shared memory.
-cudaError_t batch_blocks_per_sm(bool win_smem, bool positive, int n_warps, size_t smem, int *out) {
-    void (*fn)(const BatchArgs) = batch_kernel(win_smem, positive);
+cudaError_t batch_blocks_per_sm(bool win_smem, bool positive, bool tsmem, int n_warps, size_t smem, int *out) {
+    void (*fn)(const BatchArgs) = batch_kernel(win_smem, positive, tsmem);
     const cudaError_t e = raise_smem_limit((const void *)fn, smem);
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, fn, n_warps * 32, smem);

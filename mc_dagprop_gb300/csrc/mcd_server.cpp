@@ -9,7 +9,7 @@
 //     stream: uploads run in parallel, off the scheduler.
 //   - Requests are batched by class: equal warps per CTA, equal CTAs per SM for
 //     their shared-memory layout (so no request lowers another's occupancy) and
-//     the same kernel variant (positive times or not).
+//     the same kernel variant (positive times or not, tables in shared memory or not).
 //   - One scheduler thread, whenever one of its stream slots is free, launches
 //     the uploaded requests of the class of the oldest waiting request as one
 //     batch (the persistent k_batch_stats over (request, tile) items, then the
@@ -36,9 +36,10 @@
 #include "mcd_handle.hpp"
 
 namespace mcd {
-cudaError_t launch_batch_stats(const BatchArgs &b, bool win_smem, bool positive, int n_warps, size_t smem, int grid,
+cudaError_t launch_batch_stats(const BatchArgs &b, bool win_smem, bool positive, bool tsmem, int n_warps, size_t smem,
+                               int grid,
                                cudaStream_t st);
-cudaError_t batch_blocks_per_sm(bool win_smem, bool positive, int n_warps, size_t smem, int *out);
+cudaError_t batch_blocks_per_sm(bool win_smem, bool positive, bool tsmem, int n_warps, size_t smem, int *out);
 cudaError_t launch_batch_finish(const FArgs *fs, int32_t n_dags, int32_t max_events, cudaStream_t st);
 }  // namespace mcd
 
@@ -329,7 +330,8 @@ void compile_loop(mcd_server *S) {
             if ((int64_t)r->bytes > S->opt.memory_budget)
                 throw McdError(MCD_ERR_INVALID, "request needs more device memory than the server's budget");
             int per_sm = 0;
-            cuda_check(batch_blocks_per_sm(true, r->h.positive, r->h.n_warps, (size_t)r->h.smem_total, &per_sm),
+            cuda_check(batch_blocks_per_sm(true, r->h.positive, r->h.tables_in_smem, r->h.n_warps,
+                                           (size_t)r->h.smem_total, &per_sm),
                        "occupancy query");
             r->per_sm = std::max(1, per_sm);
             r->tile_cost = (double)r->h.pred.size() + 2.0 * r->h.E;
@@ -460,7 +462,8 @@ void launch_batch(mcd_server *S, Slot &slot, std::vector<Request *> &batch) {
     ba.smem_bytes = (int32_t)smem;
     const int32_t nw = batch[0]->h.n_warps;
     const int grid = batch[0]->per_sm * S->sms;  // the class's CTAs per SM, on every SM
-    cuda_check(launch_batch_stats(ba, true, batch[0]->h.positive, nw, smem, grid, st), "batch launch");
+    cuda_check(launch_batch_stats(ba, true, batch[0]->h.positive, batch[0]->h.tables_in_smem, nw, smem, grid, st),
+               "batch launch");
     cuda_check(launch_batch_finish(reinterpret_cast<const FArgs *>(slot.meta_dev + s_ka), (int32_t)nb, max_E, st),
                "batch finish");
     size_t pos = 0;
@@ -508,10 +511,11 @@ std::vector<Request *> take_class(mcd_server *S) {
     if (S->ready.empty()) return batch;
     const Request *first = S->ready.front();
     const int32_t nw = first->h.n_warps, per_sm = first->per_sm;
-    const bool positive = first->h.positive;
+    const bool positive = first->h.positive, tsmem = first->h.tables_in_smem;
     std::deque<Request *> rest;
     for (Request *r : S->ready) {
         if (r->h.n_warps == nw && r->per_sm == per_sm && r->h.positive == positive &&
+            r->h.tables_in_smem == tsmem &&
             (S->opt.max_batch <= 0 || (int32_t)batch.size() < S->opt.max_batch))
             batch.push_back(r);
         else

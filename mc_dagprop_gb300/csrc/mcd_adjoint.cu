@@ -111,11 +111,11 @@ __global__ void __launch_bounds__(768) k_adjoint(const KArgs a) {
     }
 }
 
-template <bool POSITIVE>
+template <bool POSITIVE, int TS>
 __global__ void __launch_bounds__(768) k_adjoint_forward(const KArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
-    propagate_tile<false, true, false, POSITIVE, true>(a, (int64_t)blockIdx.x, nullptr, a.ld, false, smem,
-                                                       reinterpret_cast<uint64_t *>(smem + a.smem_bar_off), false);
+    propagate_tile<false, true, false, POSITIVE, true, TS>(a, (int64_t)blockIdx.x, nullptr, a.ld, false, smem,
+                                                           reinterpret_cast<uint64_t *>(smem + a.smem_bar_off), false);
 }
 
 // grad_earliest[e] = grad_e[e] / n, grad_base[l] = grad_l[l] 2^-20 / n, and the
@@ -145,7 +145,9 @@ cudaError_t launch_adjoint(const KArgs &a, cudaStream_t st) {
     if (a.n <= 0) return cudaSuccess;
     const dim3 grid((unsigned)((a.n + kTile - 1) / kTile)), block((unsigned)(a.n_warps * 32));
     const size_t smem = (size_t)a.smem_total;
-    void (*fwd)(const KArgs) = a.positive ? k_adjoint_forward<true> : k_adjoint_forward<false>;
+    void (*fwd)(const KArgs);
+    if (a.tables_in_smem) fwd = a.positive ? k_adjoint_forward<true, kTablesSmem> : k_adjoint_forward<false, kTablesSmem>;
+    else fwd = a.positive ? k_adjoint_forward<true, kTablesGlobal> : k_adjoint_forward<false, kTablesGlobal>;
     cudaError_t e = raise_smem_limit((const void *)fwd, smem);
     if (e != cudaSuccess) return e;
     fwd<<<grid, block, smem, st>>>(a);

@@ -130,29 +130,39 @@ def _capi():
     return lib
 
 
-def cpu_baseline(flat, gen, seconds=10.0, kind="port"):
+def cpu_baseline(flat, gen, seconds=10.0, kind="port", single_core_seconds=0.0):
     """The reference's algorithm on all host cores: one simulator per thread,
     contiguous seed chunks (the reference's multithreading pattern), full outputs
-    into a reused buffer; repeated until `seconds` have passed."""
+    into a reused buffer; repeated until `seconds` have passed.  With
+    single_core_seconds > 0, also one thread alone for that long."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
     threads = os.cpu_count() or 1
     sim = oracle.OracleSim(flat, gen)
-    per_call = 8 * threads
     L = sim.activity_count()
-    done = 0
-    t0 = time.perf_counter()
-    while True:
-        seeds = np.arange(done, done + per_call, dtype=np.int64)
-        sim.run_many(seeds, threads=threads)
-        done += per_call
-        if time.perf_counter() - t0 >= seconds:
-            break
-    dt = time.perf_counter() - t0
-    return {"value": done * L / dt, "unit": METRIC, "cores": threads, "kind": kind,
-            "sample": f"{done} samples of the same DAG ({done * L:.3g} sample-edges) in {dt:.1f} s, "
-                      f"calls of {per_call} samples, full outputs"}
+
+    def timed(n_threads, secs):
+        per_call = 8 * n_threads
+        done = 0
+        t0 = time.perf_counter()
+        while True:
+            seeds = np.arange(done, done + per_call, dtype=np.int64)
+            sim.run_many(seeds, threads=n_threads)
+            done += per_call
+            if time.perf_counter() - t0 >= secs:
+                break
+        return done, time.perf_counter() - t0, per_call
+
+    done, dt, per_call = timed(threads, seconds)
+    out = {"value": done * L / dt, "unit": METRIC, "cores": threads, "kind": kind,
+           "sample": f"{done} samples of the same DAG ({done * L:.3g} sample-edges) in {dt:.1f} s, "
+                     f"calls of {per_call} samples, full outputs"}
+    if single_core_seconds > 0:
+        d1, t1, _ = timed(1, single_core_seconds)
+        out["single_core"] = {"value": d1 * L / t1, "cores": 1,
+                              "sample": f"{d1} samples ({d1 * L:.3g} sample-edges) in {t1:.1f} s on one thread"}
+    return out
 
 
 def run_reference_arm(args):
@@ -686,7 +696,7 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(flat, gen, seconds=float(os.environ.get("MCD_CPU_SECONDS", "10")))
+        cpu = cpu_baseline(flat, gen, seconds=float(os.environ.get("MCD_CPU_SECONDS", "10")), single_core_seconds=4.0)
 
     if rank == 0:
         print(json.dumps({

@@ -381,6 +381,30 @@ void upload_image(DagImage &im) {
     place(im.d_ub, h.ub, s_times);
 }
 
+// One output of a computed chunk to the host: sample-minor rows [rows][C] go to
+// sample-major host rows [n][rows] from sample `off` on, transposed straight
+// into pinned memory (dv: its device address) or, for a pageable buffer, into
+// sample-major device rows and copied.
+cudaError_t launch_transpose(const double *in, int64_t ld_in, double *out, int64_t ld_out, int64_t rows, int64_t cols,
+                             cudaStream_t st) {
+    return launch_transpose_f64(in, ld_in, out, ld_out, rows, cols, st);
+}
+cudaError_t launch_transpose(const int32_t *in, int64_t ld_in, int32_t *out, int64_t ld_out, int64_t rows,
+                             int64_t cols, cudaStream_t st) {
+    return launch_transpose_i32(in, ld_in, out, ld_out, rows, cols, st);
+}
+template <typename T>
+void move_rows(const T *minor, int64_t C, T *dv, T *host, T *major, int64_t rows, int64_t off, int64_t m,
+               cudaStream_t st, const char *what) {
+    if (dv) {
+        cuda_check(launch_transpose(minor, C, dv + off * rows, rows, rows, m, st), "transpose");
+    } else if (host) {
+        cuda_check(launch_transpose(minor, C, major, rows, rows, m, st), "transpose");
+        cuda_check(cudaMemcpyAsync(host + off * rows, major, (size_t)(m * rows) * sizeof(T), cudaMemcpyDeviceToHost, st),
+                   what);
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -649,31 +673,9 @@ int mcd_run_many_host(mcd_dag *g, const int64_t *seeds, int64_t n, double *reali
             a.cause = cause ? b.cause_minor : nullptr;
             cuda_check(launch_propagate(a, false, g->h.win_smem, false, pipe.compute), "propagate launch");
             pipe.begin_transfer(idx);
-            cudaStream_t st = pipe.transfer;
-            if (real_dv) {
-                cuda_check(launch_transpose_f64(b.real_minor, C, real_dv + off * E, E, E, m, st), "transpose");
-            } else if (realized) {
-                cuda_check(launch_transpose_f64(b.real_minor, C, b.real_major, E, E, m, st), "transpose");
-                cuda_check(cudaMemcpyAsync(realized + off * E, b.real_major, (size_t)(m * E) * 8,
-                                           cudaMemcpyDeviceToHost, st),
-                           "realized download");
-            }
-            if (dur_dv) {
-                cuda_check(launch_transpose_f64(b.dur_minor, C, dur_dv + off * L, L, L, m, st), "transpose");
-            } else if (durations) {
-                cuda_check(launch_transpose_f64(b.dur_minor, C, b.dur_major, L, L, m, st), "transpose");
-                cuda_check(cudaMemcpyAsync(durations + off * L, b.dur_major, (size_t)(m * L) * 8,
-                                           cudaMemcpyDeviceToHost, st),
-                           "durations download");
-            }
-            if (cause_dv) {
-                cuda_check(launch_transpose_i32(b.cause_minor, C, cause_dv + off * E, E, E, m, st), "transpose");
-            } else if (cause) {
-                cuda_check(launch_transpose_i32(b.cause_minor, C, b.cause_major, E, E, m, st), "transpose");
-                cuda_check(cudaMemcpyAsync(cause + off * E, b.cause_major, (size_t)(m * E) * 4,
-                                           cudaMemcpyDeviceToHost, st),
-                           "cause download");
-            }
+            move_rows(b.real_minor, C, real_dv, realized, b.real_major, E, off, m, pipe.transfer, "realized download");
+            move_rows(b.dur_minor, C, dur_dv, durations, b.dur_major, L, off, m, pipe.transfer, "durations download");
+            move_rows(b.cause_minor, C, cause_dv, cause, b.cause_major, E, off, m, pipe.transfer, "cause download");
             pipe.end_transfer(idx);
         }
         check_device_error(g);
@@ -720,23 +722,8 @@ int mcd_propagate_host(mcd_dag *g, const double *durations, int64_t n, double *r
             a.ld_in = C;
             cuda_check(launch_propagate(a, true, g->h.win_smem, false, cs), "propagate launch");
             pipe.begin_transfer(idx);
-            cudaStream_t st = pipe.transfer;
-            if (real_dv) {
-                cuda_check(launch_transpose_f64(b.real_minor, C, real_dv + off * E, E, E, m, st), "transpose");
-            } else if (realized) {
-                cuda_check(launch_transpose_f64(b.real_minor, C, b.real_major, E, E, m, st), "transpose");
-                cuda_check(cudaMemcpyAsync(realized + off * E, b.real_major, (size_t)(m * E) * 8,
-                                           cudaMemcpyDeviceToHost, st),
-                           "realized download");
-            }
-            if (cause_dv) {
-                cuda_check(launch_transpose_i32(b.cause_minor, C, cause_dv + off * E, E, E, m, st), "transpose");
-            } else if (cause) {
-                cuda_check(launch_transpose_i32(b.cause_minor, C, b.cause_major, E, E, m, st), "transpose");
-                cuda_check(cudaMemcpyAsync(cause + off * E, b.cause_major, (size_t)(m * E) * 4,
-                                           cudaMemcpyDeviceToHost, st),
-                           "cause download");
-            }
+            move_rows(b.real_minor, C, real_dv, realized, b.real_major, E, off, m, pipe.transfer, "realized download");
+            move_rows(b.cause_minor, C, cause_dv, cause, b.cause_major, E, off, m, pipe.transfer, "cause download");
             pipe.end_transfer(idx);
         }
         check_device_error(g);

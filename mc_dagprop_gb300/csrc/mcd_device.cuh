@@ -15,7 +15,8 @@
 // 32-bit integer logic, so FP64 is spent only where bit-exactness needs it: the
 // one IEEE add per edge of the reference's loop (_core.cpp:341).  Comparisons
 // run on 64-bit integer order keys that order doubles like the IEEE operators;
-// sampled durations base * (1 + X) are formed with integer mantissa products.
+// a sampled duration base * (1 + X) is one FP64 multiply by the double equal to
+// the float 1 + X, that double built with integer operations.
 //
 // Delays come from Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random
 // numbers: as easy as 1, 2, 3", SC'11) in counter mode: the counter holds the
@@ -272,7 +273,8 @@ __device__ __forceinline__ double link_duration(const KArgs &a, int32_t kd, doub
 }
 
 // ---------------------------------------------------------------- records
-// Record reads as 16-byte vector loads (two for a predecessor, three for an event).
+// Record reads as 16-byte vector loads (two for a predecessor; three for an event,
+// two where the order keys go unused: the compiler drops the third).
 __device__ __forceinline__ PredRec load_pred(const PredRec *p) {
     const int4 a = reinterpret_cast<const int4 *>(p)[0];
     const int4 b = reinterpret_cast<const int4 *>(p)[1];

@@ -5,8 +5,8 @@
 // fills every SM whatever the DAGs' sizes -- a plain per-DAG launch of a DAG
 // with 1,000 samples keeps 32 CTAs busy and leaves the rest of the GPU idle.
 // DAGs are grouped by kernel variant (window on chip or not, tables in shared
-// memory or not, positive times or
-// not); each group is one launch with its own queue.  Each run is one CUDA
+// memory or not, positive times or not); each group is one launch with its own
+// queue.  Each run is one CUDA
 // graph: reset the accumulators and the queue heads, the persistent statistics
 // launches, the batched finish.  The graph is recorded on the first run and
 // replayed afterwards.

@@ -1,7 +1,8 @@
-// mcd_kernels.cu -- launch dispatch, statistics finish and layout kernels.
+// mcd_kernels.cu -- launch dispatch, statistics finish, earliest-tick tables and
+// layout kernels.
 //
 // The propagation kernel itself (k_propagate, mcd_device.cuh) is instantiated in
-// mcd_prop_sample.cu and mcd_prop_given.cu.
+// mcd_prop_sample.cu, mcd_prop_sample_gt.cu and mcd_prop_given.cu.
 #include <cuda_runtime.h>
 
 #include <cstdint>

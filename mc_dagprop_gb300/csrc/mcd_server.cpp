@@ -9,7 +9,8 @@
 //     stream: uploads run in parallel, off the scheduler.
 //   - Requests are batched by class: equal warps per CTA, equal CTAs per SM for
 //     their shared-memory layout (so no request lowers another's occupancy) and
-//     the same kernel variant (positive times or not, tables in shared memory or not).
+//     the same kernel variant (positive times or not, tables in shared memory or
+//     not).
 //   - One scheduler thread, whenever one of its stream slots is free, launches
 //     the uploaded requests of the class of the oldest waiting request as one
 //     batch (the persistent k_batch_stats over (request, tile) items, then the

@@ -180,6 +180,12 @@ int mcd_propagate_device(mcd_dag *dag, const double *durations, int64_t ld_in, i
                          int32_t *cause_event, int64_t ld, void *stream);
 /* Synchronises the handle's stream and reports a latched kernel error, if any. */
 int mcd_dag_check(mcd_dag *dag);
+/* Self-test of the kernels' bounded waits (no reference counterpart): a kernel
+ * waits on a barrier that nothing completes, with a short poll limit, on the
+ * current device.  On return *timed_out is 1 when the wait gave up and latched its
+ * error flag, *kernel_returned 1 when the kernel then ran to its end; the CUDA
+ * context stays usable. */
+int mcd_selftest_bounded_wait(int32_t *timed_out, int32_t *kernel_returned);
 
 /* ---- Per-event statistics (the full sample matrix never leaves the chip) ----
  * For each event over n samples: mean of realized (FP64, accumulated exactly as

@@ -22,6 +22,7 @@ namespace mcd {
 cudaError_t launch_propagate(const KArgs &a, bool given, bool win_smem, bool stats, cudaStream_t st);
 cudaError_t launch_stats_finish(const FArgs &f, cudaStream_t st);
 cudaError_t launch_event_ticks(const double *earliest, int32_t E, int32_t q, long long *te, cudaStream_t st);
+cudaError_t launch_wait_selftest(int32_t *err, uint32_t limit, cudaStream_t st);
 cudaError_t noalloc_scratch(void **ptr, size_t *bytes);
 cudaError_t launch_transpose_f64(const double *in, int64_t ld_in, double *out, int64_t ld_out, int64_t rows,
                                  int64_t cols, cudaStream_t st);
@@ -582,6 +583,26 @@ int mcd_dag_describe(const mcd_dag_desc *desc, const mcd_generator *gen, mcd_dag
         fill_info(h, info);
         info->device = -1;
         info->device_bytes = -1;
+    });
+}
+
+int mcd_selftest_bounded_wait(int32_t *timed_out, int32_t *kernel_returned) {
+    return guarded([&] {
+        if (!timed_out || !kernel_returned) throw McdError(MCD_ERR_INVALID, "null argument");
+        int32_t *d = nullptr;
+        cudaStream_t st = nullptr;
+        int32_t flags = 0;
+        cudaError_t e = cudaMalloc(&d, sizeof(int32_t));
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, sizeof(int32_t), st);
+        if (e == cudaSuccess) e = launch_wait_selftest(d, 1024u, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&flags, d, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (st) cudaStreamDestroy(st);
+        if (d) cudaFree(d);
+        cuda_check(e, "bounded-wait self-test");
+        *timed_out = (flags & ERR_STAGE_TIMEOUT) ? 1 : 0;
+        *kernel_returned = (flags >> 30) & 1;
     });
 }
 

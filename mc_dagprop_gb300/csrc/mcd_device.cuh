@@ -357,9 +357,10 @@ __device__ __forceinline__ void stage_issue(const KArgs &a, int stage, char *buf
 }
 
 // Bounded wait for a stage buffer; false (and the error flag latched) if the copy
-// did not land within the limit.
-__device__ __forceinline__ bool stage_wait(uint64_t *bar, uint32_t parity, int32_t *err) {
-    for (uint32_t it = 0; it < (1u << 24); ++it)
+// did not land within `limit` polls.
+__device__ __forceinline__ bool stage_wait(uint64_t *bar, uint32_t parity, int32_t *err,
+                                           uint32_t limit = 1u << 24) {
+    for (uint32_t it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     atomicOr(err, ERR_STAGE_TIMEOUT);
     return false;

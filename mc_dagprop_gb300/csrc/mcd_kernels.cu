@@ -10,6 +10,7 @@
 #include <mutex>
 #include <utility>
 
+#include "mcd_device.cuh"
 #include "mcd_internal.hpp"
 
 namespace mcd {
@@ -106,6 +107,21 @@ __global__ void __launch_bounds__(256) k_batch_finish(const FArgs *__restrict__ 
     }
 }
 
+// Self-test of the bounded stage wait: an mbarrier whose phase expects 16 bytes
+// that no copy delivers, waited on by every thread with a short poll limit.  The
+// wait must give up, latch ERR_STAGE_TIMEOUT and let the kernel return.
+__global__ void k_wait_selftest(int32_t *err, uint32_t limit) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_expect_tx(&bar, 16);  // the arrival; the 16 bytes never come
+    __syncthreads();
+    if (!stage_wait(&bar, 0u, err, limit) && threadIdx.x == 0) atomicOr(err, 1 << 30);  // "returned"
+}
+
 // Every event's earliest in ticks of 2^-q seconds (KArgs::te) for one run.
 __global__ void k_event_ticks(const double *__restrict__ earliest, int32_t E, int32_t q, long long *__restrict__ te) {
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x)
@@ -197,6 +213,11 @@ cudaError_t launch_batch_finish(const FArgs *fs, int32_t n_dags, int32_t max_eve
     if (n_dags <= 0 || max_events <= 0) return cudaSuccess;
     const unsigned gy = (unsigned)(n_dags < 65535 ? n_dags : 65535);  // grid y limit; the kernel strides
     k_batch_finish<<<dim3((unsigned)((max_events + 7) / 8), gy), 256, 0, st>>>(fs, n_dags);  // a warp per event
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wait_selftest(int32_t *err, uint32_t limit, cudaStream_t st) {
+    k_wait_selftest<<<1, 64, 0, st>>>(err, limit);
     return cudaGetLastError();
 }
 

@@ -169,7 +169,7 @@ def run_reference_arm(args):
     rank, world, _ = _dist_env()
     if rank != 0:
         return 0
-    flat, gen = build_dag()
+    flat, gen = build_dag(n_layers=args.layers)
     per_step_seconds = float(os.environ.get("MCD_REF_STEP_SECONDS", "5"))
     for _ in range(args.warmup):
         cpu_baseline(flat, gen, seconds=min(1.0, per_step_seconds))

@@ -182,3 +182,9 @@ def test_compiler_layout_decisions():
     big = flat_from_lists([0.0] * (n + 1), {(i, n): (i, 1.0, 1) for i in range(n)}, [(n, [(i, i) for i in range(n)])], 1e6)
     rc, info, msg = describe(big, [("constant", 1, 1.0)])
     assert rc == MCD_OK and info.n_levels == 2
+    # distribution tables beyond 16 KB stay in global memory (the kTablesGlobal kernels)
+    vals = np.arange(1000, dtype=np.float64)
+    rc, info, msg = describe(W.config0()[0], [("empirical_absolute", 1, vals, np.ones(1000)), ("constant", 2, 0.5)])
+    assert rc == MCD_OK and info.tables_in_smem == 0
+    rc, info, msg = describe(W.config0()[0], [("empirical_absolute", 1, vals[:100], np.ones(100)), ("constant", 2, 0.5)])
+    assert rc == MCD_OK and info.tables_in_smem == 1

@@ -29,6 +29,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -615,8 +616,10 @@ def main():
     if lib.mcd_dag_check(h) != 0:
         raise RuntimeError(lib.mcd_last_error().decode())
 
-    clocks = Clocks(os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv")
-                    if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else f"/tmp/mcd_clocks_{rank}.csv")
+    # the raw nvidia-smi samples go to $MCD_CLOCKS_DIR (kept with a run's other
+    # outputs) or a temporary file; their summary is part of the JSON line
+    clocks_dir = os.environ.get("MCD_CLOCKS_DIR") or tempfile.gettempdir()
+    clocks = Clocks(os.path.join(clocks_dir, f"mcd_clocks_rank{rank}.csv"))
     if rank == 0:
         clocks.start()
         time.sleep(0.4)

@@ -216,8 +216,8 @@ void request_args(Request *r) {
 }
 
 // A compile thread's pinned staging buffer: records are gathered there and
-// uploaded in one DMA copy (a copy from pageable memory is staged by the driver
-// on the calling thread and serialises with other threads' CUDA calls).
+// uploaded in one DMA copy (a copy from pageable memory is staged by the CUDA
+// driver on the calling thread and serialises with other threads' CUDA calls).
 struct Staging {
     char *p = nullptr;
     size_t bytes = 0;

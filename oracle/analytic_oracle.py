@@ -1,6 +1,6 @@
 """CPU restatement of the reference's analytic PMF propagator (test infrastructure).
 
-This module is the checker for the GPU analytic engine
+This module is the oracle for the GPU analytic engine
 (``mc_dagprop_gb300.analytic``): only tests, the golden-fixture script and
 ``bench.py``'s CPU baseline use it.  It restates, step for step, the algorithm of
 

@@ -1,7 +1,7 @@
 /*
  * mcd_oracle.c -- CPU restatement of the reference Monte Carlo path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the timed CPU
+ * TEST INFRASTRUCTURE ONLY: the oracle for the CUDA path and the timed CPU
  * baseline.  Never linked into the product library.  Every function cites the
  * reference file:line it follows (paths inside the reference project).
  *

@@ -1,7 +1,7 @@
 /*
  * mcd_oracle.h -- CPU restatement of the reference Monte Carlo path.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker that the CUDA path is compared
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle the CUDA path is compared
  * against, and the timed CPU baseline.  The product library never links it.
  *
  * It restates, in plain C, what the reference computes in

@@ -1,7 +1,8 @@
 """ctypes wrapper around the C oracle (``mcd_oracle.c``).
 
 TEST INFRASTRUCTURE ONLY: tests, ``__graft_entry__.smoke()`` and the CPU-baseline
-leg of ``bench.py`` use it as the checker.  The product path never imports it.
+leg of ``bench.py`` use it as the oracle results are compared with.  The product
+path never imports it.
 
 The oracle restates the reference's ``Simulator`` (src/mc_dagprop/monte_carlo/
 _core.cpp:161-362) and its libstdc++ distribution arithmetic in C; it is pinned

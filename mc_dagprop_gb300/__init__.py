@@ -1,9 +1,10 @@
 """GB300-native Monte Carlo DAG propagation, a drop-in for ``mc_dagprop``'s
-Monte Carlo path (``MonteCarloPropagator.run`` / ``run_many``).
+Monte Carlo path (``MonteCarloPropagator.run`` / ``run_many``), with its analytic
+PMF propagator (``create_analytic_propagator``) on the GPU as well.
 
 The compiled extension (``_core`` over ``_lib/libmcdagprop_gb300.so``) is
-required; there is no CPU fallback.  Build it with ``python -c "import
-__graft_entry__ as g; g.build()"`` or ``python mc_dagprop_gb300/_build.py``.
+required; there is no CPU fallback.  Build it with
+``python mc_dagprop_gb300/_build.py``.
 """
 from __future__ import annotations
 

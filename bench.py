@@ -104,19 +104,50 @@ class Clocks:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def build_dag(n_layers=2000, width=100):
-    from mc_dagprop_gb300 import workloads as W
+def _workloads():
+    """The synthetic-workload generator, loaded from its file alone: importing it
+    through the package would run the package's __init__ and map the CUDA engine,
+    which the reference arm must not load (the module needs only numpy)."""
+    name = "_mcd_bench_workloads"
+    if name not in sys.modules:
+        import importlib.util
 
-    return W.config1(seed=1, n_layers=n_layers, width=width)
+        spec = importlib.util.spec_from_file_location(name, os.path.join(ROOT, "mc_dagprop_gb300", "workloads.py"))
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules[name]
+
+
+def build_dag(n_layers=2000, width=100):
+    return _workloads().config1(seed=1, n_layers=n_layers, width=width)
+
+
+def _levels(flat):
+    """Number of levels (longest path from a source, plus one) of a layered
+    workload DAG, whose precedence targets come in topological order."""
+    lvl = np.zeros(len(flat["earliest"]), np.int64)
+    off, src = flat["pred_offsets"], flat["pred_src"]
+    for k, t in enumerate(flat["target"]):
+        if off[k + 1] > off[k]:
+            lvl[t] = lvl[src[off[k]:off[k + 1]]].max() + 1
+    return int(lvl.max()) + 1 if len(lvl) else 0
+
+
+def _dag_config(flat, samples_per_step):
+    """The `config` object both arms print for the single-large-DAG workload (the
+    workload's definition; what each arm actually ran is stated beside it)."""
+    return {"workload": WORKLOAD, "events": len(flat["earliest"]), "links": int(flat["act_idx"].max()) + 1,
+            "preds": int(len(flat["pred_src"])), "levels": _levels(flat), "samples_per_step": samples_per_step,
+            "outputs": "realized (E,S) f64 + durations (L,S) f64 + cause_event (E,S) i32"}
 
 
 def make_propagator(flat, gen):
     import mc_dagprop_gb300 as m
-    from mc_dagprop_gb300 import workloads as W
 
     return m.MonteCarloPropagator.from_arrays(
         flat["earliest"], flat["act_idx"], flat["act_duration"], flat["act_type"], flat["target"],
-        flat["pred_offsets"], flat["pred_src"], flat["pred_act"], flat["max_delay"], W.to_generator(m, gen))
+        flat["pred_offsets"], flat["pred_src"], flat["pred_act"], flat["max_delay"], _workloads().to_generator(m, gen))
 
 
 def _capi():
@@ -186,9 +217,9 @@ def run_reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "events": len(flat["earliest"]), "links": int(flat["act_idx"].max()) + 1,
-                   "implementation": "C restatement of the reference's run_many (oracle/mcd_oracle.c), "
-                                     "one simulator per host thread"},
+        "config": _dag_config(flat, args.samples),
+        "implementation": "C restatement of the reference's run_many (oracle/mcd_oracle.c), one simulator per "
+                          "host thread; each step a bounded sample of the workload (see cpu_baseline.sample)",
         "cpu_baseline": cb,
         "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
@@ -706,17 +737,19 @@ def main():
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "events": E, "links": L, "preds": info["n_preds"],
-                       "levels": info["n_levels"], "samples_per_step": S, "samples_total": S * args.steps * world,
-                       "outputs": "realized (E,S) f64 + durations (L,S) f64 + cause_event (E,S) i32, sample-minor",
-                       "l2": f"outputs {out_bytes / 1e9:.1f} GB per step >> 129 MB L2, no flush needed; "
-                             f"compiled DAG ({info['device_bytes'] / 1e6:.1f} MB) stays L2-resident by design",
-                       "window_slots": info["window_slots"], "window_in_smem": info["window_in_smem"],
-                       "warps_per_cta": info["n_warps"], "parallelism": f"replicas x{world}, disjoint seeds"},
+            "config": _dag_config(flat, S),
+            "gpu": {"samples_total": S * args.steps * world,
+                    "output_layout": "sample-minor rows (E,S), (L,S), (E,S) in HBM",
+                    "l2": f"outputs {out_bytes / 1e9:.1f} GB per step >> 129 MB L2, no flush needed; "
+                          f"compiled DAG ({info['device_bytes'] / 1e6:.1f} MB) stays L2-resident by design",
+                    "compiled_levels": info["n_levels"], "window_slots": info["window_slots"],
+                    "window_in_smem": info["window_in_smem"], "warps_per_cta": info["n_warps"],
+                    "parallelism": f"replicas x{world}, disjoint seeds"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": alg_bytes,
-                         "kernel": "k_propagate<false,true> (fused Philox sampler + FP64 propagation)",
+                         "kernel": "k_propagate<GIVEN=0, WIN_SMEM=1, STATS=0, POSITIVE=1, TS=smem> (fused Philox sampler + FP64 "
+                                   "propagation)",
                          "kernel_ms": float(np.mean(kernel_ms))},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": ck,
         }))

@@ -216,8 +216,9 @@ int mcd_stats_device(mcd_dag *dag, const int64_t *seeds, int64_t seed0, int64_t 
  * events whose propagation window fits in shared memory (larger ones fail with
  * MCD_ERR_INVALID).  Inputs, outputs and the compiled DAG are the caller's, as in
  * mcd_stats_device (device pointers; asynchronous on `stream`, NULL = the
- * handle's stream).  The first call on a device looks the array's device address
- * up; make that first call before any stream capture.  All calls share the one
+ * handle's stream).  The first call on a device (and in each CUDA context of it:
+ * after a cudaDeviceReset, or with another context made current) looks the
+ * array's device address up; make that first call before any stream capture.  All calls share the one
  * array, and each call clears it first: calls that overlap on the GPU (other
  * streams, other threads, other handles) race and corrupt each other's results. */
 #define MCD_NOALLOC_MAX_EVENTS 32000

@@ -830,21 +830,24 @@ int mcd_stats_host(mcd_dag *g, const int64_t *seeds, int64_t seed0, int64_t n, c
         cuda_check(cudaSetDevice(g->device), "cudaSetDevice");
         cudaStream_t st = g->stream[0];
         const size_t E = (size_t)g->h.E;
-        // device copies of the seeds and the outputs live after the accumulators
-        const size_t acc_bytes = align_up(E * 8, 256), hist_bytes = align_up(E * kHistStride * 4, 256);
+        // device copies of the seeds and the outputs live after every region
+        // stats_device carves (accumulators, histograms, earliest ticks, and the
+        // chunk scratch when the window is off chip), so none of them aliases
+        const size_t acc_bytes = align_up(E * 8, 256), hist_bytes = align_up(E * kHistStride * 4, 256),
+                     te_bytes = align_up(E * 8, 256);
         const size_t seeds_bytes = seeds ? align_up((size_t)n * 8, 256) : 0;
         const size_t out_bytes = align_up(E * 8, 256);
         const size_t hist_out = out->hist ? hist_bytes : 0;
-        // reserve: [outputs (5 x E doubles) | hist copy | seeds], then the accumulators
+        // reserve: [accumulators | hist | ticks | scratch] ... [outputs (5 x E doubles) | hist copy | seeds]
         const size_t head = 5 * out_bytes + hist_out + seeds_bytes;
+        size_t scratch_bytes = 0;
         if (!g->h.win_smem) {
             const int64_t C = std::max<int64_t>(32, std::min<int64_t>(n, (int64_t)((512ull << 20) / std::max<size_t>(E * 8, 1)) / 32 * 32));
-            ensure_ws(g, head + acc_bytes + hist_bytes + align_up(E * (size_t)C * 8, 256));
-        } else {
-            ensure_ws(g, head + acc_bytes + hist_bytes);
+            scratch_bytes = align_up(E * (size_t)C * 8, 256);
         }
-        // stats_device carves its accumulators from the start of the workspace,
-        // so the staging area goes at the end
+        ensure_ws(g, acc_bytes + hist_bytes + te_bytes + scratch_bytes + head);
+        // stats_device carves its regions from the start of the workspace, so the
+        // staging area goes at the end
         char *tail = g->ws + g->ws_bytes - head;
         double *o[5];
         for (int k = 0; k < 5; ++k) o[k] = reinterpret_cast<double *>(tail + k * out_bytes);

@@ -187,24 +187,56 @@ cudaError_t launch_propagate(const KArgs &a, bool given, bool win_smem, bool sta
 constexpr size_t kNoAllocScratchBytes = 34ull << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of g_noalloc_scratch on the current device, looked up once per
-// device (cudaGetSymbolAddress, with that device current) and cached.
+// Unique id of the calling thread's current CUDA context (the driver's
+// cuCtxGetCurrent and cuCtxGetId, found through the runtime so the library needs
+// no link to the driver library; ids are never reused within a process), or 0
+// when no context is current yet.
+static unsigned long long current_context_id() {
+    using CtxGetCurrent = int (*)(void **);
+    using CtxGetId = int (*)(void *, unsigned long long *);
+    static const std::pair<CtxGetCurrent, CtxGetId> fns = [] {
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult qa{}, qb{};
+        const bool ok = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) ==
+                            cudaSuccess &&
+                        qa == cudaDriverEntryPointSuccess &&
+                        cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) ==
+                            cudaSuccess &&
+                        qb == cudaDriverEntryPointSuccess;
+        return ok ? std::make_pair(reinterpret_cast<CtxGetCurrent>(a), reinterpret_cast<CtxGetId>(b))
+                  : std::make_pair((CtxGetCurrent) nullptr, (CtxGetId) nullptr);
+    }();
+    void *ctx = nullptr;
+    unsigned long long id = 0;
+    if (!fns.first || fns.first(&ctx) != 0 || !ctx || fns.second(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// Device address of g_noalloc_scratch in the current device's context, looked up
+// (cudaGetSymbolAddress, with that device current) once per device and context and
+// cached under both: a device reset or another context made current on the same
+// device loads the module anew, at another address, so a cache keyed by the device
+// alone would hand out a stale pointer.  Without a context id (an older driver),
+// every call looks the address up again.
 cudaError_t noalloc_scratch(void **ptr, size_t *bytes) {
-    constexpr int kMaxDevices = 64;
-    static void *cached[kMaxDevices] = {};
+    static std::map<std::pair<int, unsigned long long>, void *> cached;
     static std::mutex mu;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(mu);
-    if (!cached[dev]) {
+    unsigned long long ctx = current_context_id();
+    auto it = ctx ? cached.find({dev, ctx}) : cached.end();
+    if (it == cached.end()) {
         void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // makes the device's primary context current if none was
         if (e != cudaSuccess) return e;
-        cached[dev] = p;
+        ctx = current_context_id();
+        if (ctx) cached[{dev, ctx}] = p;
+        *ptr = p;
+    } else {
+        *ptr = it->second;
     }
-    *ptr = cached[dev];
     *bytes = kNoAllocScratchBytes;
     return cudaSuccess;
 }

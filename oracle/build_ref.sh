@@ -1,6 +1,8 @@
 #!/usr/bin/env bash
 # Compiles the reference's Monte Carlo extension from its own sources, where they
-# lie under /root/reference (read-only), into oracle/_ref/.  Nothing of the
+# lie ($MCD_REFERENCE_ROOT, by default the read-only checkout of this machine),
+# into oracle/_ref/, and records that place in oracle/_ref/REFERENCE_ROOT for
+# oracle/ref_loader.py.  Nothing of the
 # reference is copied: only the compiled module is written, and oracle/ref_loader.py
 # loads it next to the reference's own pure-Python `mc_dagprop.types` module.
 #
@@ -30,4 +32,5 @@ PY
 SUFFIX="$(python3 -c 'import sysconfig; print(sysconfig.get_config_var("EXT_SUFFIX"))')"
 g++ -O3 -std=c++20 -flto -shared -fPIC -I"$PYINC" -I"$PB11" -I"$REF/src/mc_dagprop/monte_carlo" \
     "$SRC" -o "$OUT/_core$SUFFIX"
+printf "%s\n" "$REF" > "$OUT/REFERENCE_ROOT"
 echo "built $OUT/_core$SUFFIX"

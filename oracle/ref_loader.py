@@ -19,7 +19,22 @@ import sys
 import types
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("MCD_REFERENCE_ROOT", "/root/reference")
+
+
+def _ref_root() -> str:
+    """Where the reference's sources are: $MCD_REFERENCE_ROOT, else the place
+    oracle/build_ref.sh compiled them from (recorded next to the module)."""
+    env = os.environ.get("MCD_REFERENCE_ROOT")
+    if env:
+        return env
+    rec = os.path.join(HERE, "_ref", "REFERENCE_ROOT")
+    if os.path.isfile(rec):
+        with open(rec) as f:
+            return f.read().strip()
+    return ""
+
+
+REF_ROOT = _ref_root()
 
 
 def ref_so_path() -> str | None:
@@ -32,32 +47,60 @@ def available() -> bool:
         os.path.join(REF_ROOT, "src", "mc_dagprop", "types.py"))
 
 
+_LOADED: dict = {}
+
+
+class _ReferenceNamespace:
+    """Installs the reference's package names (`mc_dagprop`, `mc_dagprop.types`,
+    ...) in sys.modules while its modules initialise, then puts back whatever held
+    those names before -- e.g. this repository's own `mc_dagprop` drop-in package
+    -- so both can live in one process.  The reference's modules keep the objects
+    they imported while loading."""
+
+    def __enter__(self):
+        self.saved = {k: v for k, v in sys.modules.items() if k == "mc_dagprop" or k.startswith("mc_dagprop.")}
+        for k in self.saved:
+            del sys.modules[k]
+        for k, v in _LOADED.items():
+            sys.modules[k] = v
+        if "mc_dagprop" not in sys.modules:
+            pkg = types.ModuleType("mc_dagprop")
+            pkg.__path__ = []  # namespace-like: submodules registered by hand
+            sys.modules["mc_dagprop"] = pkg
+        return sys.modules["mc_dagprop"]
+
+    def __exit__(self, *exc):
+        for k in [k for k in sys.modules if k == "mc_dagprop" or k.startswith("mc_dagprop.")]:
+            if exc[0] is None:
+                _LOADED[k] = sys.modules[k]
+            del sys.modules[k]
+        sys.modules.update(self.saved)
+        return False
+
+
 def load():
     """Return the reference's ``_core`` module (MonteCarloPropagator, DagContext, ...)."""
     name = "mc_dagprop.monte_carlo._core"
-    if name in sys.modules:
-        return sys.modules[name]
+    if name in _LOADED:
+        return _LOADED[name]
     so = ref_so_path()
     if so is None:
         raise ImportError("oracle/_ref is not built (run oracle/build_ref.sh)")
     pkg_dir = os.path.join(REF_ROOT, "src", "mc_dagprop")
-    if "mc_dagprop" not in sys.modules:
-        pkg = types.ModuleType("mc_dagprop")
-        pkg.__path__ = []  # namespace-like: submodules registered by hand below
-        sys.modules["mc_dagprop"] = pkg
-    spec = importlib.util.spec_from_file_location("mc_dagprop.types", os.path.join(pkg_dir, "types.py"))
-    tmod = importlib.util.module_from_spec(spec)
-    sys.modules["mc_dagprop.types"] = tmod
-    spec.loader.exec_module(tmod)
-    mc = types.ModuleType("mc_dagprop.monte_carlo")
-    mc.__path__ = []
-    sys.modules["mc_dagprop.monte_carlo"] = mc
-    loader = importlib.machinery.ExtensionFileLoader(name, so)
-    spec = importlib.util.spec_from_file_location(name, so, loader=loader)
-    core = importlib.util.module_from_spec(spec)
-    sys.modules[name] = core
-    loader.exec_module(core)
-    mc._core = core
+    with _ReferenceNamespace():
+        spec = importlib.util.spec_from_file_location("mc_dagprop.types", os.path.join(pkg_dir, "types.py"))
+        tmod = importlib.util.module_from_spec(spec)
+        sys.modules["mc_dagprop.types"] = tmod
+        spec.loader.exec_module(tmod)
+        mc = types.ModuleType("mc_dagprop.monte_carlo")
+        mc.__path__ = []
+        sys.modules["mc_dagprop.monte_carlo"] = mc
+        loader = importlib.machinery.ExtensionFileLoader(name, so)
+        spec = importlib.util.spec_from_file_location(name, so, loader=loader)
+        core = importlib.util.module_from_spec(spec)
+        sys.modules[name] = core
+        loader.exec_module(core)
+        mc._core = core
     return core
 
 
@@ -66,18 +109,18 @@ def load_analytic():
     (loaded from its sources; it imports ``Event`` from the package root, which is
     the compiled module's class)."""
     name = "mc_dagprop.analytic"
-    if name in sys.modules:
-        return sys.modules[name]
+    if name in _LOADED:
+        return _LOADED[name]
     core = load()
-    root = sys.modules["mc_dagprop"]
-    for attr in ("Event", "EventTimestamp", "Activity", "DagContext", "GenericDelayGenerator", "SimResult"):
-        if hasattr(core, attr):
-            setattr(root, attr, getattr(core, attr))
-    pkg_dir = os.path.join(REF_ROOT, "src", "mc_dagprop", "analytic")
-    spec = importlib.util.spec_from_file_location(name, os.path.join(pkg_dir, "__init__.py"),
-                                                  submodule_search_locations=[pkg_dir])
-    mod = importlib.util.module_from_spec(spec)
-    sys.modules[name] = mod
-    spec.loader.exec_module(mod)
-    root.analytic = mod
+    with _ReferenceNamespace() as root:
+        for attr in ("Event", "EventTimestamp", "Activity", "DagContext", "GenericDelayGenerator", "SimResult"):
+            if hasattr(core, attr):
+                setattr(root, attr, getattr(core, attr))
+        pkg_dir = os.path.join(REF_ROOT, "src", "mc_dagprop", "analytic")
+        spec = importlib.util.spec_from_file_location(name, os.path.join(pkg_dir, "__init__.py"),
+                                                      submodule_search_locations=[pkg_dir])
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+        root.analytic = mod
     return mod

@@ -9,8 +9,12 @@ synthetic DAGs and stores inputs and outputs as compressed ``.npz`` files:
   gamma_state_ref.npz  the same DAG under a gamma-only generator, seeds 5,5,6 run in
                       sequence on one propagator (the reference's gamma draws carry
                       a cached normal across runs)
+  config0_hashes_ref.npz  the 1,000-event DAG over all 10,000 seeds 0..9999: digests
+                      (tests/mcd_testlib.py block_digests) of the reference's realized, durations
+                      and cause_event rows, per block of 100 seeds -- the full run
+                      pinned in a few KB
 
-Usage:  python tests/golden/make_golden.py     (needs the reference sources)
+Usage:  python tests/golden/make_golden.py [name ...]   (needs the reference sources)
 """
 from __future__ import annotations
 
@@ -26,8 +30,11 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 sys.path.insert(0, ROOT)
 
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
 import ref_loader  # noqa: E402
 from mc_dagprop_gb300 import workloads as W  # noqa: E402
+from mcd_testlib import block_digests  # noqa: E402
 
 
 def encode_gen(gen):
@@ -58,13 +65,33 @@ def dump(name, flat, gen, seeds):
     print("wrote", name)
 
 
-def main():
+def dump_hashes(name, flat, gen, seeds):
+    ref = ref_loader.load()
+    sim = ref.MonteCarloPropagator(W.to_context(ref, flat), W.to_generator(ref, gen))
+    res = sim.run_many([int(s) for s in seeds])
+    np.savez_compressed(
+        os.path.join(HERE, name),
+        seeds=np.asarray(seeds, np.int64), block=np.int64(100),
+        realized=block_digests(np.array([r.realized for r in res])),
+        durations=block_digests(np.array([r.durations for r in res])),
+        cause=block_digests(np.array([r.cause_event for r in res])),
+    )
+    print("wrote", name)
+
+
+def main(names):
     flat0, gen0 = W.config0()
-    dump("config0_ref.npz", flat0, gen0, np.arange(16))
     flat5, gen5 = W.config1(seed=11, n_layers=30, width=40)
-    dump("five_types_ref.npz", flat5, gen5, np.arange(8))
-    dump("gamma_state_ref.npz", flat5, [("gamma", t, 2.0, 0.05, math.inf) for t in range(1, 6)], [5, 5, 6])
+    jobs = {
+        "config0_ref.npz": lambda n: dump(n, flat0, gen0, np.arange(16)),
+        "five_types_ref.npz": lambda n: dump(n, flat5, gen5, np.arange(8)),
+        "gamma_state_ref.npz": lambda n: dump(
+            n, flat5, [("gamma", t, 2.0, 0.05, math.inf) for t in range(1, 6)], [5, 5, 6]),
+        "config0_hashes_ref.npz": lambda n: dump_hashes(n, flat0, gen0, np.arange(10_000)),
+    }
+    for n in names or jobs:
+        jobs[n](n)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

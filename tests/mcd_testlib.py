@@ -165,6 +165,20 @@ def load_golden(name: str):
     return flat, gen, z
 
 
+def block_digests(rows: np.ndarray, block: int = 100) -> np.ndarray:
+    """8-byte BLAKE2b digest of the raw bytes of each block of `block` consecutive
+    rows (sample-major: one row per seed), as uint64 -- how the golden fixture
+    config0_hashes_ref.npz pins the reference's full 10,000-seed run."""
+    import hashlib
+
+    rows = np.ascontiguousarray(rows)
+    out = np.empty((len(rows) + block - 1) // block, np.uint64)
+    for i in range(len(out)):
+        h = hashlib.blake2b(rows[i * block:(i + 1) * block].tobytes(), digest_size=8)
+        out[i] = np.frombuffer(h.digest(), np.uint64)[0]
+    return out
+
+
 def flat_from_lists(earliest, links, precedence, max_delay):
     """Flat DAG from python lists: links = {(src,dst): (idx, duration, type)}."""
     act_src = np.array([k[0] for k in links], np.int32)

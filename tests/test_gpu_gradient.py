@@ -1,9 +1,11 @@
 """Adjoint gradient of J = mean_s sum_e (realized - earliest).
 
-1. Against a CPU gradient built from the same samples' cause_event, realized and
-   durations (the GPU's own run_many outputs): earliest-time derivatives are
-   integer path counts / n, so they must match exactly; base-duration
-   derivatives carry d(duration)/d(base) in float, so within 1e-5 relative.
+1. Against a CPU gradient built from the oracle's cause_event and realized times
+   (the reference's propagation loop, _core.cpp:331-350, restated in C) for the
+   same samples' durations (the GPU sampler's, which the adjoint differentiates):
+   earliest-time derivatives are integer path counts / n, so they must match
+   exactly; base-duration derivatives carry d(duration)/d(base) in float, so
+   within 1e-5 relative.
 2. Against central finite differences with common random numbers (the same
    seeds), step 1e-3 s, on random coordinates: within 1e-3 absolute + 1e-3 relative.
 3. Through the torch.autograd.Function wrapper.
@@ -14,6 +16,7 @@ import numpy as np
 import pytest
 
 import mc_dagprop_gb300 as m
+import oracle
 from mc_dagprop_gb300 import batching
 from mc_dagprop_gb300 import workloads as W
 
@@ -76,7 +79,8 @@ def test_gradient_matches_cpu_chain(cuda, max_delay):
     prop = batching.compile_dag(flat, gen)
     n, seed0 = 3000, 12345
     g = prop.gradient(n, seed0)
-    real, dur, cause = prop.run_many_arrays(np.arange(seed0, seed0 + n, dtype=np.int64))
+    _, dur, _ = prop.run_many_arrays(np.arange(seed0, seed0 + n, dtype=np.int64))
+    real, cause = oracle.OracleSim(flat, gen).propagate_given(dur)  # the reference's chains
     obj, ge, gl = cpu_gradient(flat, gen, real, dur, cause)
     assert abs(g["objective"] - obj) <= 1e-9 * max(1.0, abs(obj))
     np.testing.assert_array_equal(g["grad_earliest"], ge)

@@ -9,6 +9,7 @@
 from __future__ import annotations
 
 import math
+import os
 import platform
 
 import numpy as np
@@ -43,6 +44,21 @@ def test_oracle_matches_golden(name):
         assert np.array_equal(c2, z["cause"])
     else:  # another libm may round log differently in the last place
         np.testing.assert_allclose(d2, z["durations"], rtol=1e-12)
+
+
+@pytest.mark.skipif(not EXACT_HOST, reason="the fixture's durations come from the x86-64 libm")
+def test_oracle_matches_reference_all_10000_seeds_config0():
+    """The full 10,000-seed run of the 1,000-event configuration (seeds 0..9999),
+    pinned by digests of the reference's own rows (config0_hashes_ref.npz)."""
+    from mc_dagprop_gb300 import workloads as W
+    from mcd_testlib import block_digests
+
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "config0_hashes_ref.npz"))
+    flat, gen = W.config0()
+    real, dur, cause = oracle.OracleSim(flat, gen).run_many(z["seeds"], threads=os.cpu_count() or 1)
+    for name, rows in (("durations", dur), ("realized", real), ("cause", cause)):
+        bad = np.flatnonzero(block_digests(rows, int(z["block"])) != z[name])
+        assert len(bad) == 0, f"{name}: blocks {bad[:5].tolist()} differ from the reference"
 
 
 def test_gamma_state_carries_across_runs():

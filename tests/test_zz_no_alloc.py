@@ -6,10 +6,13 @@ device), or an allocation would synchronise the device in the middle of their
 latency-critical loop.  For them the library keeps the statistics accumulators
 in one fixed 34 MiB device array (DAGs up to MCD_NOALLOC_MAX_EVENTS events).
 
-This test calls the entry point through the C ABI, twice in a row on the same
-handle (the array keeps the previous call's contents, so the second call checks
-that each call starts from zero), and compares every output with the allocating
-entry point mcd_stats_device on the same seeds: the statistics are
+This test calls the entry point through the C ABI on a freshly created handle,
+before anything else ran on that handle, twice in a row (the array keeps the
+previous call's contents, so the second call checks that each call starts from
+zero), and checks that the device's free memory is the same before and after
+those calls (so nothing was allocated behind the caller's back).  It then
+compares every output with the allocating entry point mcd_stats_device, run on a
+second handle of the same DAG with the same seeds: the statistics are
 deterministic (exact integer accumulation), so the tolerance is zero.  It lives in
 its own file, collected last, and works alone or after the other tests.
 """
@@ -42,29 +45,49 @@ def _outputs(torch, E, dev):
     return t, s
 
 
+def _bind(L):
+    L.mcd_stats_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.POINTER(Stats), C.c_void_p]
+    L.mcd_stats_device_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.POINTER(Stats),
+                                           C.c_void_p]
+
+
 def test_noalloc_stats_match_allocating_entry_point(cuda):
     import torch
 
     L = lib()
-    L.mcd_stats_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.POINTER(Stats), C.c_void_p]
-    L.mcd_stats_device_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.POINTER(Stats),
-                                           C.c_void_p]
+    _bind(L)
+    # Load the kernels this path launches (and look the fixed array up) on a small
+    # DAG of the same delay kinds first: a module loaded lazily on its first launch
+    # takes device memory, which is not an allocation of the entry point.
+    wflat, wgen = W.config1(seed=16, n_layers=4, width=8)
+    warm = propagator_from_flat(m, wflat, wgen)
+    wout, wout_s = _outputs(torch, warm.node_count(), cuda)
+    assert L.mcd_stats_device_noalloc(C.c_void_p(warm._handle()), None, 0, 64, C.byref(wout_s), None) == MCD_OK, \
+        last_error()
+    assert L.mcd_dag_check(C.c_void_p(warm._handle())) == MCD_OK, last_error()
+
     flat, gen = W.config1(seed=17, n_layers=60, width=80)
-    prop = propagator_from_flat(m, flat, gen)
+    prop = propagator_from_flat(m, flat, gen)  # a fresh handle: no workspace yet
     h = C.c_void_p(prop._handle())
     E = prop.node_count()
     seeds = torch.arange(3000, dtype=torch.int64, device=cuda) * 7 + 11
+    outs = [_outputs(torch, E, cuda) for _ in range(2)]
     torch.cuda.synchronize()
-
-    ref, ref_s = _outputs(torch, E, cuda)
-    assert L.mcd_stats_device(h, seeds.data_ptr(), 0, 3000, C.byref(ref_s), None) == MCD_OK, last_error()
-    assert L.mcd_dag_check(h) == MCD_OK, last_error()
-
-    for call in range(2):  # twice in a row: the fixed array must be cleared by each call
-        out, out_s = _outputs(torch, E, cuda)
+    free_before = torch.cuda.mem_get_info(cuda)[0]
+    for out, out_s in outs:  # twice in a row: the fixed array must be cleared by each call
         rc = L.mcd_stats_device_noalloc(h, seeds.data_ptr(), 0, 3000, C.byref(out_s), None)
         assert rc == MCD_OK, last_error()
         assert L.mcd_dag_check(h) == MCD_OK, last_error()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(cuda)[0] == free_before, "device memory was allocated"
+
+    # the allocating entry point on a second handle of the same DAG
+    prop2 = propagator_from_flat(m, flat, gen)
+    h2 = C.c_void_p(prop2._handle())
+    ref, ref_s = _outputs(torch, E, cuda)
+    assert L.mcd_stats_device(h2, seeds.data_ptr(), 0, 3000, C.byref(ref_s), None) == MCD_OK, last_error()
+    assert L.mcd_dag_check(h2) == MCD_OK, last_error()
+    for call, (out, _) in enumerate(outs):
         for k in ("mean", "p50", "p90", "p99", "pot", "hist"):
             a, b = out[k].cpu().numpy(), ref[k].cpu().numpy()
             assert np.array_equal(a, b), (call, k)
@@ -73,8 +96,7 @@ def test_noalloc_stats_match_allocating_entry_point(cuda):
 
 def test_noalloc_rejects_too_many_events(cuda):
     L = lib()
-    L.mcd_stats_device_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.POINTER(Stats),
-                                           C.c_void_p]
+    _bind(L)
     flat, gen = W.config1(seed=18, n_layers=400, width=100)  # 40,000 events
     prop = propagator_from_flat(m, flat, gen)
     s = Stats()

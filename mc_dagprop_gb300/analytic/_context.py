@@ -1,12 +1,20 @@
-"""Analytic context types and validation (the reference's ``analytic/_context.py``).
+"""Analytic context types (the reference's ``analytic/_context.py``) and their
+structural validation.
 
-Same classes, fields and checks (``validate_context``, _context.py:93-158), with
-the reference's error messages."""
+The dataclasses and enums are the reference's public types, with the same names,
+fields and values.  ``validate_context`` reports the reference's errors
+(_context.py:93-158) -- the same messages, and when a context has several
+problems, the one the reference reports first -- but is organised as one ordered
+stream of problems (``_problems``): vectorised checks over the events' bounds,
+one check per activity and per precedence entry, and a cycle test that peels the
+DAG level by level (every event whose predecessors are all peeled is peeled in
+the same step; an event that never is lies on a cycle).
+"""
 from __future__ import annotations
 
-from collections import deque
 from dataclasses import dataclass
 from enum import IntEnum, unique
+from typing import Iterator
 
 import numpy as np
 
@@ -68,51 +76,94 @@ class AnalyticContext:
     max_delay: Second | None = None
 
 
-def validate_context(context: AnalyticContext) -> None:
-    """Structural checks: bounds, activity indices and PMFs, step, cycles."""
+def _event_problem(events) -> str | None:
+    """The first event whose bounds are out of order or whose actual time lies
+    outside them (NaN times fail the second test, as in a chained comparison)."""
+    if not events:
+        return None
+    t = np.array([(e.timestamp.earliest, e.timestamp.latest, e.timestamp.actual) for e in events], dtype=float)
+    early, late, act = t[:, 0], t[:, 1], t[:, 2]
+    inverted = early > late
+    outside = ~((early <= act) & (act <= late))
+    bad = np.flatnonzero(inverted | outside)
+    if not len(bad):
+        return None
+    i = int(bad[0])
+    return f"event {i} has earliest > latest" if inverted[i] else f"event {i} actual time outside bounds"
+
+
+def _activity_problem(key, edge: AnalyticActivity, n_events: int, step) -> str | None:
+    """Checks of one activity: its endpoints, then its PMF (which raises its own
+    errors), its step, its grid, its mass."""
+    src, dst = key
+    if not (0 <= src < n_events and 0 <= dst < n_events):
+        return f"activity {(src, dst)} references invalid node"
+    pmf = edge.pmf
+    pmf.validate()
+    if not np.isclose(pmf.step, step):
+        return f"edge {(src, dst)} step {pmf.step} does not match context step size {step}"
+    pmf.validate_alignment(step)
+    if not np.isclose(pmf.total_mass, 1.0):
+        return f"activity {(src, dst)} PMF does not sum to 1, got {pmf.total_mass}"
+    return None
+
+
+def _has_cycle(n_events: int, src: np.ndarray, dst: np.ndarray) -> bool:
+    """Level peeling: repeatedly remove every event with no unremoved predecessor;
+    the graph is acyclic exactly when every event is removed."""
+    waiting = np.bincount(dst, minlength=n_events) if len(dst) else np.zeros(n_events, np.int64)
+    order = np.argsort(src, kind="stable")
+    out_dst = dst[order]
+    out_start = np.searchsorted(src[order], np.arange(n_events + 1))
+    level = np.flatnonzero(waiting == 0)
+    removed = 0
+    while len(level):
+        removed += len(level)
+        reach = np.concatenate([out_dst[out_start[v]:out_start[v + 1]] for v in level]) if len(dst) else []
+        if not len(reach):
+            break
+        np.subtract.at(waiting, reach, 1)
+        level = np.unique(reach[waiting[reach] == 0])
+    return removed != n_events
+
+
+def _problems(context: AnalyticContext) -> Iterator[str]:
     n_events = len(context.events)
     if context.step <= 0.0:
-        raise ValueError("step_size must be positive")
+        yield "step_size must be positive"
     if context.max_delay is not None and context.max_delay < 0.0:
-        raise ValueError("max_delay must be non-negative when provided")
-    for i, ev in enumerate(context.events):
-        ts = ev.timestamp
-        if ts.earliest > ts.latest:
-            raise ValueError(f"event {i} has earliest > latest")
-        if not (ts.earliest <= ts.actual <= ts.latest):
-            raise ValueError(f"event {i} actual time outside bounds")
-    for (src, dst), (_, edge) in context.activities.items():
-        if not (0 <= src < n_events and 0 <= dst < n_events):
-            raise ValueError(f"activity {(src, dst)} references invalid node")
-        edge.pmf.validate()
-        if not np.isclose(edge.pmf.step, context.step):
-            raise ValueError(f"edge {(src, dst)} step {edge.pmf.step} does not match context step size {context.step}")
-        edge.pmf.validate_alignment(context.step)
-        if not np.isclose(edge.pmf.total_mass, 1.0):
-            raise ValueError(f"activity {(src, dst)} PMF does not sum to 1, got {edge.pmf.total_mass}")
-    adjacency: list[list[int]] = [[] for _ in range(n_events)]
-    indegree = [0] * n_events
+        yield "max_delay must be non-negative when provided"
+    msg = _event_problem(context.events)
+    if msg:
+        yield msg
+    for key, (_, edge) in context.activities.items():
+        msg = _activity_problem(key, edge, n_events, context.step)
+        if msg:
+            yield msg
+    src, dst = [], []
     for target, preds in context.precedence_list:
         if not (0 <= target < n_events):
-            raise ValueError(f"target index {target} out of range")
-        for src, link in preds:
-            if not (0 <= src < n_events):
-                raise ValueError(f"predecessor index {src} out of range")
-            edge = context.activities.get((src, target))
-            if edge is None:
-                raise ValueError(f"missing activity for {(src, target)}")
-            if edge[0] != link:
-                raise ValueError(f"edge index {link} for {(src, target)} does not match context mapping {edge[0]}")
-            adjacency[src].append(target)
-            indegree[target] += 1
-    q = deque(i for i, d in enumerate(indegree) if d == 0)
-    seen = 0
-    while q:
-        node = q.popleft()
-        seen += 1
-        for dst in adjacency[node]:
-            indegree[dst] -= 1
-            if indegree[dst] == 0:
-                q.append(dst)
-    if seen != n_events:
-        raise ValueError("precedence list contains a cycle")
+            yield f"target index {target} out of range"
+            continue
+        for s, link in preds:
+            if not (0 <= s < n_events):
+                yield f"predecessor index {s} out of range"
+                continue
+            mapped = context.activities.get((s, target))
+            if mapped is None:
+                yield f"missing activity for {(s, target)}"
+                continue
+            if mapped[0] != link:
+                yield f"edge index {link} for {(s, target)} does not match context mapping {mapped[0]}"
+            src.append(s)
+            dst.append(target)
+    if _has_cycle(n_events, np.asarray(src, np.int64), np.asarray(dst, np.int64)):
+        yield "precedence list contains a cycle"
+
+
+def validate_context(context: AnalyticContext) -> None:
+    """Raise ``ValueError`` with the first structural problem of ``context``:
+    step and delay cap, event bounds, activities and their PMFs, the precedence
+    list's indices and activity mapping, cycles."""
+    for msg in _problems(context):
+        raise ValueError(msg)

@@ -1,9 +1,21 @@
-"""Discrete PMFs on an integer step grid (the reference's ``analytic/_pmf.py``).
+"""Discrete PMFs on an equidistant integer grid (the reference's public
+``DiscretePMF``, ``analytic/_pmf.py``).
 
-``DiscretePMF`` carries the data the GPU engine propagates; its ``convolve`` and
-``maximum`` are host utilities for single pairs (the propagation itself runs on
-the GPU, ``AnalyticPropagator.run``).  Validation rules and error messages follow
-the reference (_pmf.py:26-67) so callers see the same exceptions.
+``DiscretePMF`` carries what the GPU engine propagates.  Its construction checks
+and their messages are the reference's (_pmf.py:26-67), because callers match on
+them.  ``convolve`` and ``maximum`` are host utilities for one pair of PMFs (the
+propagation itself runs on the GPU, ``AnalyticPropagator.run``); both work on the
+operands' common integer grid in extended precision, as the GPU fold does:
+
+* the sum of two variables is the discrete convolution of their masses, which
+  starts at the sum of their first values;
+* the maximum of two independent variables has the CDF ``F_a * F_b``, so its
+  masses are the increments of that product on the grid spanning both operands.
+
+A result then carries the mass its operands imply -- exactly 1 when both are
+normalised (rounding drift is scaled away), else the product of their masses
+-- and is rescaled only when its sum strays from that by more than 1e-12
+relative (1e-15 absolute), the reference's tolerance.
 """
 from __future__ import annotations
 
@@ -13,9 +25,11 @@ import numpy as np
 
 from ..types import ProbabilityMass, Second
 
+_RTOL, _ATOL = 1e-12, 1e-15
 
-def _close(a: float, b: float) -> bool:
-    return bool(np.isclose(a, b, rtol=1e-12, atol=1e-15))
+
+def _near(x: float, y: float) -> bool:
+    return bool(np.isclose(x, y, rtol=_RTOL, atol=_ATOL))
 
 
 @dataclass(frozen=True, slots=True)
@@ -38,31 +52,36 @@ class DiscretePMF:
                                 f"(type: {type(self.step)})")
 
     def validate(self) -> None:
-        if len(self.values) == 0:
+        """Non-empty, equal lengths, sorted values, total mass at most 1."""
+        v, p = self.values, self.probabilities
+        if len(v) == 0:
             raise ValueError("PMF values cannot be empty")
-        if len(self.values) != len(self.probabilities):
+        if len(v) != len(p):
             raise ValueError("values and probs must have same length")
-        if len(self.values) > 1 and not np.all(self.values[1:] >= self.values[:-1]):
+        if len(v) > 1 and not (np.diff(v) >= 0).all():  # NaN fails too
             raise ValueError("values must be sorted in non-decreasing order")
-        s = self.probabilities.sum()
-        if not (1.0 >= s or np.isclose(s, 1.0)):
+        total = p.sum()
+        if not total <= 1.0 and not np.isclose(total, 1.0):  # NaN fails too
             raise ValueError("Probabilities must sum to <= 1.0")
 
     def validate_alignment(self, step: Second) -> None:
+        """Values spaced by ``step`` and on its grid."""
         if not np.isclose(self.step, step):
             raise ValueError(f"PMF step {self.step} does not match expected {step}")
         if step <= 0.0:
             raise ValueError("step must be positive")
-        if len(self.values) == 0:
+        v = self.values
+        if len(v) == 0:
             raise ValueError("PMF values cannot be empty")
-        if len(self.values) > 1 and not np.allclose(np.diff(self.values), step):
+        if len(v) > 1 and not np.allclose(np.diff(v), step):
             raise ValueError("PMF grid spacing does not match step")
-        if self.values.size > 0 and not np.isclose(self.values[0] % step, 0.0):
+        if not np.isclose(v[0] % step, 0.0):
             raise ValueError("PMF values are not aligned to step grid")
 
     @staticmethod
     def delta(v: Second, step: Second) -> "DiscretePMF":
-        return DiscretePMF(np.array([v], dtype=float), np.array([1.0]), step=step)
+        """Unit mass at ``v``."""
+        return DiscretePMF(np.array([v], dtype=float), np.ones(1), step=step)
 
     @property
     def total_mass(self) -> ProbabilityMass:
@@ -71,39 +90,34 @@ class DiscretePMF:
     def shift(self, delta: Second) -> "DiscretePMF":
         return DiscretePMF(self.values + delta, self.probabilities.copy(), step=self.step)
 
-    # host utilities: the same operations the GPU engine applies per event
-    def _with_mass(self, values: np.ndarray, probs: np.ndarray, m1: float, m2: float) -> "DiscretePMF":
-        expected = 1.0 if _close(m1, 1.0) and _close(m2, 1.0) else m1 * m2
+    # ------------------------------------------------------------ host utilities
+    def _implied_mass(self, other: "DiscretePMF") -> float:
+        ma, mb = float(self.total_mass), float(other.total_mass)
+        return 1.0 if _near(ma, 1.0) and _near(mb, 1.0) else ma * mb
+
+    def _result(self, first: float, probs: np.ndarray, mass: float) -> "DiscretePMF":
+        probs = np.asarray(probs, dtype=float)
         total = probs.sum()
-        if total > 0 and not _close(total, expected):
-            probs = probs * (expected / total)
-        return DiscretePMF(values, probs, step=self.step)
+        if total > 0 and not _near(total, mass):
+            probs = probs * (mass / total)
+        return DiscretePMF(first + self.step * np.arange(len(probs)), probs, step=self.step)
 
     def convolve(self, other: "DiscretePMF") -> "DiscretePMF":
-        """PMF of X + Y (extended-precision accumulation, then mass correction)."""
-        if len(self.values) == 1:
-            vals, probs = other.values + self.values[0], other.probabilities * self.probabilities[0]
-        elif len(other.values) == 1:
-            vals, probs = self.values + other.values[0], self.probabilities * other.probabilities[0]
-        else:
-            probs = np.convolve(self.probabilities.astype(np.longdouble),
-                                other.probabilities.astype(np.longdouble)).astype(float)
-            vals = self.values[0] + other.values[0] + self.step * np.arange(len(probs))
-        return self._with_mass(vals, probs, float(self.total_mass), float(other.total_mass))
+        """PMF of X + Y for independent X ~ self, Y ~ other."""
+        q = np.longdouble
+        probs = np.convolve(self.probabilities.astype(q), other.probabilities.astype(q))
+        return self._result(self.values[0] + other.values[0], probs, self._implied_mass(other))
 
     def maximum(self, other: "DiscretePMF") -> "DiscretePMF":
-        """PMF of max(X, Y) from cumulative sums on the common grid."""
-        lo = np.minimum(self.values[0], other.values[0])
-        hi = np.maximum(self.values[-1], other.values[-1])
-        grid = np.arange(lo, hi + self.step, self.step)
-        a = np.zeros(len(grid), dtype=np.longdouble)
-        b = np.zeros(len(grid), dtype=np.longdouble)
-        oa = int(round((self.values[0] - lo) / self.step))
-        ob = int(round((other.values[0] - lo) / self.step))
-        a[oa:oa + len(self.probabilities)] = self.probabilities
-        b[ob:ob + len(other.probabilities)] = other.probabilities
-        ca = np.cumsum(a, dtype=np.longdouble)
-        cb = np.cumsum(b, dtype=np.longdouble)
-        ca_before = np.concatenate((np.zeros(1, dtype=np.longdouble), ca[:-1]))
-        probs = (a * cb + b * ca_before).astype(float)
-        return self._with_mass(grid, probs, float(self.total_mass), float(other.total_mass))
+        """PMF of max(X, Y) for independent X ~ self, Y ~ other."""
+        lo = min(self.values[0], other.values[0])
+        hi = max(self.values[-1], other.values[-1])
+        n = len(np.arange(lo, hi + self.step, self.step))
+        cdf = np.ones(n, dtype=np.longdouble)
+        for pmf in (self, other):
+            k = int(round((pmf.values[0] - lo) / self.step))  # the operand's first grid point
+            col = np.zeros(n, dtype=np.longdouble)
+            col[k:k + len(pmf.probabilities)] = pmf.probabilities
+            cdf *= np.cumsum(col)
+        probs = np.diff(cdf, prepend=np.longdouble(0.0))  # a monotone product: no negative increments
+        return self._result(lo, probs, self._implied_mass(other))

@@ -231,119 +231,132 @@ class _Stats(C.Structure):
                 ("p_on_time", C.c_void_p), ("hist", C.c_void_p)]
 
 
-def run_batched(args):
-    """Batching workload: 512 DAGs (events log-uniform 100-50,000, layer width
+def batched_measure(n_dags=512, steps=3, warmup=1, fast_gen=True):
+    """Batching workload: `n_dags` DAGs (events log-uniform 100-50,000, layer width
     20-200, two delay kinds), each with its own sample count (log-uniform
     1,000-100,000) and seed range; per-event mean and p50/p90/p99 from 256-bin
     histograms.  The batched form (persistent launches per width class, CUDA
     graphs, warps per CTA from the autotuner) against the plain form (one
     mcd_stats_device call per DAG, each DAG compiled with its own automatic
-    warps, the same statistics) on the same GPU."""
+    warps, the same statistics) on the same GPU; for the whole set and for the
+    DAGs whose sample count is below one tile per SM (4,864), which one plain
+    launch cannot spread over the GPU.  Returns a dict."""
     import torch
 
     from mc_dagprop_gb300 import batching
-    from mc_dagprop_gb300 import workloads as W
 
+    W = _workloads()
     t0 = time.perf_counter()
-    dags = W.config2(n_dags=args.dags)
+    dags = W.config2(n_dags=n_dags, fast=fast_gen)
     gen_s = time.perf_counter() - t0
     items = [(d[0], d[1], int(d[2]), int(d[3])) for d in dags]
-    units = sum(int(f["act_idx"].max() + 1) * n for f, _, n, _ in items)
-    t0 = time.perf_counter()
-    runner = batching.BatchRunner(items, use_cache=False)
-    setup_s = time.perf_counter() - t0
-    plain_props = [batching.compile_dag(f, g) for f, g, _, _ in items]
+    links = [int(f["act_idx"].max() + 1) for f, _, _, _ in items]
     lib = _capi()
     lib.mcd_stats_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.POINTER(_Stats), C.c_void_p]
     dev = torch.device("cuda", 0)
-    outs = []
-    for p in plain_props:
-        t = torch.empty((5, p.node_count()), dtype=torch.float64, device=dev)
-        outs.append((t, _Stats(*(t[k].data_ptr() for k in range(5)), None)))
     stream = torch.cuda.Stream(device=dev)
 
-    def plain_run():
-        for i, (p, (t, st)) in enumerate(zip(plain_props, outs)):
-            if lib.mcd_stats_device(C.c_void_p(p._handle()), None, items[i][3], items[i][2], C.byref(st),
-                                    C.c_void_p(stream.cuda_stream)) != 0:
-                raise RuntimeError(lib.mcd_last_error().decode())
+    def measure(idx):
+        sub = [items[i] for i in idx]
+        units = sum(links[i] * items[i][2] for i in idx)
+        t0 = time.perf_counter()
+        runner = batching.BatchRunner(sub, use_cache=False)
+        setup_s = time.perf_counter() - t0
+        props = [batching.compile_dag(f, g) for f, g, _, _ in sub]
+        outs = []
+        for p in props:
+            t = torch.empty((5, p.node_count()), dtype=torch.float64, device=dev)
+            outs.append((t, _Stats(*(t[k].data_ptr() for k in range(5)), None)))
 
-    plain_run()  # workspaces allocated here
-    torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record(stream)
-    for _ in range(args.steps):
-        plain_run()
-    b.record(stream)
-    torch.cuda.synchronize()
-    plain_ms = a.elapsed_time(b) / args.steps
-    for _ in range(max(1, args.warmup)):
-        runner.run()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()  # several streams: host clock around synchronised runs
-    for _ in range(args.steps):
-        runner.run()
-    batch_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-    mism = 0
-    for i in range(0, len(items), max(1, len(items) // 32)):
-        got = runner.stats(i)
-        ref = outs[i][0].cpu().numpy()
-        mism += int(not np.array_equal(got["mean"], ref[0]) or not np.array_equal(got["p99"], ref[3]))
+        def plain_run():
+            for i, (p, (t, st)) in enumerate(zip(props, outs)):
+                if lib.mcd_stats_device(C.c_void_p(p._handle()), None, sub[i][3], sub[i][2], C.byref(st),
+                                        C.c_void_p(stream.cuda_stream)) != 0:
+                    raise RuntimeError(lib.mcd_last_error().decode())
+
+        for _ in range(max(1, warmup)):
+            plain_run()  # workspaces allocated here
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            plain_run()
+        b.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = a.elapsed_time(b) / steps
+        for _ in range(max(1, warmup)):
+            runner.run()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()  # several streams: host clock around synchronised runs
+        for _ in range(steps):
+            runner.run()
+        batch_ms = (time.perf_counter() - t0) * 1e3 / steps
+        mism = checked = 0
+        for i in range(0, len(sub), max(1, len(sub) // 32)):
+            got = runner.stats(i)
+            ref = outs[i][0].cpu().numpy()
+            checked += 1
+            mism += int(not np.array_equal(got["mean"], ref[0]) or not np.array_equal(got["p99"], ref[3]))
+        return {"value": units / (batch_ms * 1e-3), "unit": METRIC, "ms_per_step": batch_ms, "steps": steps,
+                "dags": len(sub), "events_total": int(sum(len(f["earliest"]) for f, _, _, _ in sub)),
+                "sample_edges_per_step": units,
+                "classes (warps, ctas_per_sm, dags, items)": runner.classes,
+                "plain": {"value": units / (plain_ms * 1e-3), "ms_per_step": plain_ms,
+                          "path": "one mcd_stats_device call per DAG on one stream, automatic warps per DAG"},
+                "batched_over_plain": plain_ms / batch_ms, "checked_dags": checked, "check_mismatches": mism,
+                "host_seconds_classify_autotune_compile": setup_s}
+
+    out = measure(list(range(len(items))))
+    sub_wave = [i for i, it in enumerate(items) if it[2] < 152 * 32]
+    out["sub_wave"] = measure(sub_wave) if sub_wave else None
+    out["host_seconds_generate"] = gen_s
+    return out
+
+
+def run_batched(args):
+    r = batched_measure(args.dags, args.steps, args.warmup)
     print(json.dumps({
-        "metric": "sample-edges/s (batched statistics)", "value": units / (batch_ms * 1e-3), "unit": METRIC,
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": batch_ms, "higher_is_better": True,
+        "metric": "sample-edges/s (batched statistics)", "value": r.pop("value"), "unit": METRIC, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r.pop("ms_per_step"), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "512 DAGs, events log-uniform 100-50,000 (width 20-200), samples log-uniform "
-                               "1,000-100,000, own seed ranges; per-event mean, p50/p90/p99 (256-bin histograms)",
-                   "dags": len(items), "events_total": int(sum(len(f["earliest"]) for f, _, _, _ in items)),
-                   "sample_edges_per_step": units,
-                   "classes (warps, ctas_per_sm, dags, items)": runner.classes},
-        "plain": {"value": units / (plain_ms * 1e-3), "ms_per_step": plain_ms,
-                  "path": "one mcd_stats_device call per DAG on one stream, automatic warps per DAG"},
-        "batched_over_plain": plain_ms / batch_ms, "check_mismatches": mism,
-        "host_seconds": {"generate": gen_s, "classify_autotune_compile": setup_s},
+                               "1,000-100,000, own seed ranges; per-event mean, p50/p90/p99 (256-bin histograms)"},
+        **r,
     }))
     return 0
 
 
-def run_serving(args):
-    """Serving workload: Poisson arrivals at `--rate` requests/s for `--duration` s.
-    Each request is a DAG from the config-0 generator with events log-uniform in
-    200-20,000, samples log-uniform in 4,096-65,536, the five delay kinds and its
-    own seeds, asking for per-event mean and p50/p90/p99.  DAGs come from a pool
-    of `--pool` generated ones (generation is not part of serving); every request
-    still travels the whole path -- submit, host compile, admission against the
-    64 GB budget, batched launch, statistics back.  Reported: completed
-    sample-edges/s and p50/p99 latency, against the plain per-request path (create
-    the propagator, mcd_stats_host, one request after another) on a sample of the
-    same requests."""
+def make_requests(n, seed):
+    """`n` fresh serving requests (a new DAG each, see workloads.fresh_request),
+    with their generators built for the server: (flat, generator, samples, seed0,
+    links)."""
+    import mc_dagprop_gb300 as m
+
+    W = _workloads()
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        f, g, ns, s0 = W.fresh_request(rng)
+        out.append((f, W.to_generator(m, g), ns, s0, int(f["act_idx"].max()) + 1, g))
+    return out
+
+
+def serve(server, requests, rate, seed=7):
+    """Submits `requests` with Poisson arrivals at `rate` per second and collects
+    them; returns completed sample-edges/s over the span from the first arrival
+    to the last completion, latency percentiles and counts."""
     import threading
 
-    import mc_dagprop_gb300 as m
-    from mc_dagprop_gb300 import batching
-    from mc_dagprop_gb300 import workloads as W
-
-    pool = W.config4_requests(n_requests=args.pool)
-    gens = [W.to_generator(m, g) for _, g, _, _ in pool]
-    links = [int(f["act_idx"].max()) + 1 for f, _, _, _ in pool]
-    rng = np.random.default_rng(7)
-    n_req = int(args.rate * args.duration)
-    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n_req))
-    which = rng.integers(0, len(pool), n_req)
-    server = m.Server(memory_budget=64 << 30, n_streams=args.streams, n_warps=0, compile_threads=args.compile_threads)
-    # warm the server (kernels loaded, pool grown) with a few requests
-    for i in range(4):
-        f, _, n, s0 = pool[i]
-        t = server.submit(f["earliest"], f["act_idx"], f["act_duration"], f["act_type"], f["target"],
-                          f["pred_offsets"], f["pred_src"], f["pred_act"], f["max_delay"], gens[i], 10**12 + i, 256)
-        server.wait(t, timeout_ms=60_000)
-    tickets = [None] * n_req
-    lat = np.zeros(n_req)
-    done_at = np.zeros(n_req)
+    n = len(requests)
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+    tickets = [None] * n
+    lat = np.zeros(n)
+    done_at = np.zeros(n)
     errors = []
 
     def collector():
-        for i in range(n_req):
+        for i in range(n):
             while tickets[i] is None:
                 time.sleep(0.0002)
             try:
@@ -358,48 +371,99 @@ def run_serving(args):
     th = threading.Thread(target=collector)
     th.start()
     t0 = time.perf_counter()
-    for i in range(n_req):
+    late = 0.0
+    for i, (f, g, ns, s0, _, _) in enumerate(requests):
         now = time.perf_counter() - t0
         if arrivals[i] > now:
             time.sleep(arrivals[i] - now)
-        f, _, n, _ = pool[which[i]]
+        else:
+            late = max(late, now - arrivals[i])
         tickets[i] = server.submit(f["earliest"], f["act_idx"], f["act_duration"], f["act_type"], f["target"],
-                                   f["pred_offsets"], f["pred_src"], f["pred_act"], f["max_delay"], gens[which[i]],
-                                   1000 * i, n)
+                                   f["pred_offsets"], f["pred_src"], f["pred_act"], f["max_delay"], g, s0, ns)
     submit_s = time.perf_counter() - t0
     th.join()
     wall = max(done_at.max() - t0, 1e-9)
-    units = sum(links[which[i]] * pool[which[i]][2] for i in range(n_req))
-    counters = server.counters()
+    units = sum(r[2] * r[4] for r in requests)
+    return {"rate_per_s": rate, "requests": n, "offered_seconds": float(arrivals[-1]),
+            "offered_sample_edges_per_s": units / float(arrivals[-1]), "value": units / wall,
+            "completed_seconds": wall, "submit_seconds": submit_s, "max_submit_lag_s": late,
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                           "max": float(lat.max())},
+            "errors": len(errors)}
+
+
+def plain_serving(requests, compile_threads):
+    """The plain per-request GPU path with the server's host-compile parallelism:
+    `compile_threads` threads compile the requests in order (from_arrays, the GIL
+    released), and each compiled request runs its statistics alone
+    (run_stats: one mcd_stats_host call) one after another."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import mc_dagprop_gb300 as m
+
+    def compile_one(r):
+        f, g = r[0], r[1]
+        return m.MonteCarloPropagator.from_arrays(f["earliest"], f["act_idx"], f["act_duration"], f["act_type"],
+                                                  f["target"], f["pred_offsets"], f["pred_src"], f["pred_act"],
+                                                  f["max_delay"], g)
+
+    t0 = time.perf_counter()
+    units = 0
+    with ThreadPoolExecutor(max_workers=compile_threads) as ex:
+        for r, prop in zip(requests, ex.map(compile_one, requests)):
+            prop.run_stats(n=r[2], seed0=r[3])
+            units += r[2] * r[4]
+    return {"value": units / (time.perf_counter() - t0), "requests": len(requests),
+            "path": f"per request: from_arrays (compile + upload; {compile_threads} compile threads ahead) then "
+                    "run_stats (mcd_stats_host), one request on the GPU at a time"}
+
+
+def serving_measure(rate=400.0, duration=10.0, overload_rate=2000.0, overload_duration=2.0, streams=4,
+                    compile_threads=8, plain_requests=300, seed=4):
+    """Serving workload: fresh DAG per request (events log-uniform 200-20,000,
+    samples log-uniform 4,096-65,536, five delay kinds, own seeds), per-event
+    mean and p50/p90/p99, 64 GB device budget.  One run at `rate` (below the
+    device's capacity, so latency is service latency), one at `overload_rate`
+    (the configuration's rate, above capacity: completed throughput is the
+    device's, latency there is queueing), and the plain per-request path on the
+    first `plain_requests` requests with the same compile parallelism."""
+    import mc_dagprop_gb300 as m
+
+    t0 = time.perf_counter()
+    reqs = make_requests(int(rate * duration), seed)
+    over = make_requests(int(overload_rate * overload_duration), seed + 1) if overload_rate else []
+    gen_s = time.perf_counter() - t0
+    server = m.Server(memory_budget=64 << 30, n_streams=streams, n_warps=0, compile_threads=compile_threads)
+    serve(server, make_requests(8, seed + 2), 1000.0)  # warm: kernels loaded, pool grown
+    out = {"sustained": serve(server, reqs, rate)}
+    if over:
+        out["overload"] = serve(server, over, overload_rate, seed=8)
+    c = server.counters()
     del server
-    # plain per-request path on a sample of the same requests, one after another
-    k = min(args.plain_requests, n_req)
-    t1 = time.perf_counter()
-    plain_units = 0
-    for i in range(k):
-        f, g, n, _ = pool[which[i]]
-        prop = batching.compile_dag(f, g)
-        prop.run_stats(n=n, seed0=1000 * i)
-        plain_units += links[which[i]] * n
-    plain_s = time.perf_counter() - t1
+    out["plain"] = plain_serving(reqs[:plain_requests], compile_threads)
+    out["served_over_plain"] = out["sustained"]["value"] / out["plain"]["value"]
+    if over:
+        out["overload_served_over_plain"] = out["overload"]["value"] / out["plain"]["value"]
+    out["server"] = {"streams": streams, "compile_threads": compile_threads, "memory_budget_gb": 64,
+                     "batches": int(c["batches"]), "completed": int(c["completed"]),
+                     "seconds": {k: round(float(c[k]), 3) for k in ("compile_seconds", "upload_seconds",
+                                                                     "launch_seconds")}}
+    out["host_seconds_generate"] = gen_s
+    return out
+
+
+def run_serving(args):
+    r = serving_measure(args.rate, args.duration, args.overload_rate, args.overload_duration, args.streams,
+                        args.compile_threads, args.plain_requests)
+    s = r["sustained"]
     print(json.dumps({
-        "metric": "sample-edges/s (served statistics)", "value": units / wall, "unit": METRIC, "n_gpus": 1,
-        "steps": 1, "warmup": 4, "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "Poisson arrivals; requests: events log-uniform 200-20,000, samples log-uniform "
-                               "4,096-65,536, five delay kinds, own seeds; per-event mean, p50/p90/p99",
-                   "rate_per_s": args.rate, "duration_s": args.duration, "requests": n_req, "dag_pool": len(pool),
-                   "offered_sample_edges_per_s": units / args.duration, "streams": args.streams,
-                   "compile_threads": args.compile_threads, "memory_budget_gb": 64},
-        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                       "max": float(lat.max())},
-        "completed": int(counters["completed"]), "batches": int(counters["batches"]), "errors": len(errors),
-        "server_seconds": {k: round(float(counters[k]), 3) for k in ("compile_seconds", "upload_seconds",
-                                                                      "launch_seconds")},
-        "submit_seconds": submit_s,
-        "plain": {"value": plain_units / plain_s, "requests": k,
-                  "path": "per request: create propagator (host compile + upload) + mcd_stats_host, sequential"},
-        "served_over_plain": (units / wall) / (plain_units / plain_s),
+        "metric": "sample-edges/s (served statistics)", "value": s["value"], "unit": METRIC, "n_gpus": 1,
+        "steps": 1, "warmup": 1, "ms_per_step": s["completed_seconds"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "Poisson arrivals; every request a fresh DAG: events log-uniform 200-20,000, "
+                               "samples log-uniform 4,096-65,536, five delay kinds, own seeds; per-event mean, "
+                               "p50/p90/p99; 64 GB device budget"},
+        **r,
     }))
     return 0
 
@@ -580,12 +644,15 @@ def main():
     ap.add_argument("--layers", type=int, default=2000)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--workload", default="single", choices=["single", "batched", "gradient", "serving", "analytic"])
-    ap.add_argument("--rate", type=float, default=2000.0)
-    ap.add_argument("--duration", type=float, default=5.0)
-    ap.add_argument("--pool", type=int, default=128)
+    ap.add_argument("--rate", type=float, default=400.0)
+    ap.add_argument("--duration", type=float, default=10.0)
+    ap.add_argument("--overload-rate", type=float, default=2000.0)
+    ap.add_argument("--overload-duration", type=float, default=2.0)
     ap.add_argument("--streams", type=int, default=4)
     ap.add_argument("--compile-threads", type=int, default=8)
-    ap.add_argument("--plain-requests", type=int, default=200)
+    ap.add_argument("--plain-requests", type=int, default=300)
+    ap.add_argument("--no-extra", action="store_true",
+                    help="leave the batched and serving legs out of the default line")
     ap.add_argument("--grad-samples", type=int, default=65536)
     ap.add_argument("--fd-coords", type=int, default=200)
     ap.add_argument("--dags", type=int, default=512)
@@ -728,9 +795,65 @@ def main():
         for p in bufs:
             lib.mcd_host_free(p)
 
+    # e2e through the Python drop-in (run_many_arrays: new numpy arrays per call,
+    # as a reference user receives its results).  The arrays come from the
+    # module's recycled page-locked pool: the first call pins the memory, later
+    # calls of a loop reuse it.
+    e2e_dropin = None
+    if rank == 0:
+        n3 = min(args.e2e_samples, 2432)
+        seeds3 = np.arange(2 * 10**9, 2 * 10**9 + n3, dtype=np.int64)
+        t0 = time.perf_counter()
+        r3 = prop.run_many_arrays(seeds3)
+        first_ms = (time.perf_counter() - t0) * 1e3
+        del r3
+        reps = 3
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            r3 = prop.run_many_arrays(seeds3)
+            del r3
+        dt = (time.perf_counter() - t0) / reps
+        e2e_dropin = {"value": n3 * L / dt, "unit": METRIC, "h2d_bytes_per_step": n3 * 8,
+                      "d2h_bytes_per_step": n3 * (8 * E + 8 * L + 4 * E), "samples_per_step": n3,
+                      "ms_per_step": dt * 1e3, "first_call_ms": first_ms,
+                      "path": "MonteCarloPropagator.run_many_arrays: new numpy arrays per call (the module's "
+                              "recycled page-locked pool), sample-major (the reference's SimResult rows)"}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(flat, gen, seconds=float(os.environ.get("MCD_CPU_SECONDS", "10")), single_core_seconds=4.0)
+
+    # the batched and served forms, compact, on the same GPU after the plain one
+    extra = {}
+    if rank == 0 and world == 1 and not args.no_extra:
+        del real, durs, cause
+        torch.cuda.empty_cache()
+        b = batched_measure(args.dags, steps=3, warmup=1)
+        extra["batched"] = {
+            "metric": "sample-edges/s (batched statistics: 512 DAGs, events 100-50,000, samples 1,000-100,000)",
+            "value": b["value"], "plain_value": b["plain"]["value"], "batched_over_plain": b["batched_over_plain"],
+            "ms_per_step": b["ms_per_step"], "plain_ms_per_step": b["plain"]["ms_per_step"], "dags": b["dags"],
+            "sample_edges_per_step": b["sample_edges_per_step"], "checked_dags": b["checked_dags"],
+            "check_mismatches": b["check_mismatches"],
+            "sub_wave": None if b["sub_wave"] is None else {
+                "what": "the DAGs with fewer than 4,864 samples (one tile per SM)", "dags": b["sub_wave"]["dags"],
+                "value": b["sub_wave"]["value"], "plain_value": b["sub_wave"]["plain"]["value"],
+                "batched_over_plain": b["sub_wave"]["batched_over_plain"],
+                "check_mismatches": b["sub_wave"]["check_mismatches"]}}
+        sv = serving_measure(args.rate, args.duration, args.overload_rate, args.overload_duration, args.streams,
+                             args.compile_threads, args.plain_requests)
+        su, ov = sv["sustained"], sv.get("overload")
+        extra["serving"] = {
+            "metric": "sample-edges/s (served statistics; every request a fresh DAG, events 200-20,000, "
+                      "samples 4,096-65,536)",
+            "value": su["value"], "rate_per_s": su["rate_per_s"], "requests": su["requests"],
+            "offered_sample_edges_per_s": su["offered_sample_edges_per_s"],
+            "latency_ms": su["latency_ms"], "errors": su["errors"],
+            "plain_value": sv["plain"]["value"], "served_over_plain": sv["served_over_plain"],
+            "overload": None if ov is None else {
+                "rate_per_s": ov["rate_per_s"], "requests": ov["requests"], "value": ov["value"],
+                "latency_ms": ov["latency_ms"], "errors": ov["errors"],
+                "served_over_plain": sv["overload_served_over_plain"]}}
 
     if rank == 0:
         print(json.dumps({
@@ -751,7 +874,8 @@ def main():
                          "kernel": "k_propagate<GIVEN=0, WIN_SMEM=1, STATS=0, POSITIVE=1, TS=smem> (fused Philox sampler + FP64 "
                                    "propagation)",
                          "kernel_ms": float(np.mean(kernel_ms))},
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": ck,
+            "cpu_baseline": cpu, "e2e": e2e, "e2e_dropin": e2e_dropin, "gpu_launches": args.steps, "clocks": ck,
+            **extra,
         }))
     if dist:
         dist.destroy_process_group()

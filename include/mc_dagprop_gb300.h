@@ -16,7 +16,7 @@
  *   mcd_run_device            the same, device buffers, sample-minor layout
  *   mcd_propagate_*           the propagation loop alone       _core.cpp:331-350
  *   mcd_batch_*               many DAGs in one persistent launch (no reference counterpart)
- *   mcd_gradient_host         pathwise gradient of expected tardiness (no reference counterpart)
+ *   mcd_gradient_host/_plan   pathwise gradient of expected tardiness (no reference counterpart)
  *   mcd_server_*              continuous-batching request server (no reference counterpart)
  *   mcd_stats_*               per-event statistics (no reference counterpart; the
  *                             reference's users stack run_many results in numpy,
@@ -259,10 +259,20 @@ int mcd_batch_occupancy(int32_t n_warps, int64_t smem_bytes, int32_t *blocks_per
  * and dJ/d base duration [activity_count] (per link index; Activity.minimal_duration
  * of the activity with that idx), any may be NULL.  The derivative follows each
  * sample's winning predecessor chain (the cause_event tie rule): slope 1 along
- * unclamped chains, d(duration)/d(base) at the winning link.  Needs finite times,
- * a window that fits in shared memory and at most 16,383 predecessors per event. */
+ * unclamped chains, d(duration)/d(base) at the winning link.  Needs finite times
+ * and at most 16,383 predecessors per event.  Samples run in chunks; when the
+ * winners of every event of a chunk (6 bytes per event and sample) do not fit the
+ * memory budget (half the free device memory, at most 16 GiB), the levels are
+ * split into blocks whose forward pass is recomputed from checkpoints of the
+ * propagation window, block by block, last block first.  Every plan gives the
+ * same bits. */
 int mcd_gradient_host(mcd_dag *dag, int64_t seed0, int64_t n, double *objective, double *grad_earliest,
                       double *grad_base);
+/* The plan the handle's last mcd_gradient_host call used: samples per chunk,
+ * level blocks (1: every winner kept, no recomputation) and device bytes of its
+ * per-chunk buffers; any may be NULL. */
+int mcd_gradient_plan(const mcd_dag *dag, int64_t *samples_per_chunk, int64_t *level_blocks,
+                      int64_t *buffer_bytes);
 
 /* ---- Serving: continuous batching of statistics requests (no reference counterpart) ----
  * submit() copies a request (a DAG, its generator, seeds seed0 .. seed0+n-1) and
@@ -289,6 +299,10 @@ typedef struct mcd_server_info {
     double compile_seconds;   /* host compile time summed over requests */
     double upload_seconds;    /* allocation + upload time summed over requests */
     double launch_seconds;    /* scheduler time spent forming and launching batches */
+    int64_t resident_hits;    /* requests whose DAG was already resident (no compile, no record upload) */
+    int64_t resident_dags;    /* compiled DAGs resident now */
+    int64_t resident_bytes;   /* their device bytes (part of bytes_in_use) */
+    int64_t evicted;          /* resident DAGs evicted to make room */
 } mcd_server_info;
 int mcd_server_create(const mcd_server_options *opt, mcd_server **out);
 void mcd_server_destroy(mcd_server *server);

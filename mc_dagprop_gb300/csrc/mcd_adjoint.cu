@@ -20,9 +20,16 @@
 namespace mcd {
 
 // One CTA per tile of 32 samples; warps take each stage's events one at a time
-// from the stage's counter, stages from last to first.  Shared memory: [counts: window_slots x 32 uint32][stage
-// buffer 0][stage buffer 1][tables][2 mbarriers] -- the forward layout, whose
-// window rows are twice the size the counts need.
+// from the stage's counter, stages from a.stage_end - 1 down to a.stage_begin
+// (the whole DAG, or one level block of a recomputation).  Counts of events still
+// to be visited: with the window on chip, the forward window's slots in shared
+// memory -- [counts: window_slots x 32 uint32][stage buffer 0][stage buffer
+// 1][tables][2 mbarriers], the forward layout, whose window rows are twice the
+// size the counts need -- started from and left in a.cnt_ckpt between blocks
+// (kAdjCntLoad / kAdjCntSave); otherwise one uint32 per event and sample in
+// a.cnt_rows (global, by caller index).  Records: row (compiled index -
+// a.code_base) of a.adj_code / a.adj_dfac.
+template <bool WIN_SMEM>
 __global__ void __launch_bounds__(768) k_adjoint(const KArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     uint32_t *cnt = reinterpret_cast<uint32_t *>(smem);
@@ -31,7 +38,11 @@ __global__ void __launch_bounds__(768) k_adjoint(const KArgs a) {
     const int lane = threadIdx.x & 31;
     const int64_t s = (int64_t)blockIdx.x * kTile + lane;
     const bool active = s < a.n;
-    for (int i = threadIdx.x; i < a.window_slots * kTile; i += blockDim.x) cnt[i] = 0u;
+    const int cnt_n = a.window_slots * kTile;
+    if (WIN_SMEM) {
+        const uint32_t *in = (a.adj_flags & kAdjCntLoad) ? a.cnt_ckpt + (int64_t)blockIdx.x * cnt_n : nullptr;
+        for (int i = threadIdx.x; i < cnt_n; i += blockDim.x) cnt[i] = in ? in[i] : 0u;
+    }
     int *stage_ctr = reinterpret_cast<int *>(bars + 2);
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], 1);
@@ -41,13 +52,13 @@ __global__ void __launch_bounds__(768) k_adjoint(const KArgs a) {
         stage_ctr[1] = 0;
     }
     __syncthreads();
-    const int NS = a.n_stages;
+    const int NS = a.stage_end - a.stage_begin;
     if (threadIdx.x == 0) {
-        if (NS > 0) stage_issue(a, NS - 1, stage_buf0, &bars[0]);
-        if (NS > 1) stage_issue(a, NS - 2, stage_buf0 + a.stage_bytes, &bars[1]);
+        if (NS > 0) stage_issue(a, a.stage_end - 1, stage_buf0, &bars[0]);
+        if (NS > 1) stage_issue(a, a.stage_end - 2, stage_buf0 + a.stage_bytes, &bars[1]);
     }
-    for (int j = 0; j < NS; ++j) {  // j-th stage from the end
-        const int l = NS - 1 - j;
+    for (int j = 0; j < NS; ++j) {  // j-th stage from the end of the range
+        const int l = a.stage_end - 1 - j;
         const int b = j & 1;
         const char *buf = stage_buf0 + b * a.stage_bytes;
         const bool ok = stage_wait(&bars[b], (uint32_t)((j >> 1) & 1), a.err);
@@ -72,16 +83,20 @@ __global__ void __launch_bounds__(768) k_adjoint(const KArgs a) {
             const int i = i_next;
             if (lane == 0) i_next = take_next(ctr);
             const EvRec ev = load_ev(sev + i);
-            const int64_t o = (int64_t)row_off(ev.user, (uint32_t)a.ld) + s;
+            const int64_t o = (int64_t)row_off(meta.x + i - a.code_base, (uint32_t)a.ld) + s;
             const uint32_t code = active ? (uint32_t)a.adj_code[o] : kAdjNone;
             const float dfac = active ? a.adj_dfac[o] : 0.0f;
             const uint32_t k = code & kAdjNone;
             const bool clamped = (code & kAdjClamped) != 0u;
             const bool delayed = (code & kAdjDelayed) != 0u;
             uint32_t c = delayed ? 1u : 0u;
-            if (ev.slot >= 0) {  // read and clear: the slot's next tenant starts from zero
-                c += cnt[ev.slot * kTile + lane];
-                cnt[ev.slot * kTile + lane] = 0u;
+            if (WIN_SMEM) {
+                if (ev.slot >= 0) {  // read and clear: the slot's next tenant starts from zero
+                    c += cnt[ev.slot * kTile + lane];
+                    cnt[ev.slot * kTile + lane] = 0u;
+                }
+            } else if (active) {
+                c += a.cnt_rows[(int64_t)row_off(ev.user, (uint32_t)a.ld) + s];
             }
             if (!active) c = 0u;
             // this lane's share of d J / d earliest, >= -1: summed over the warp as ge + 1
@@ -93,7 +108,11 @@ __global__ void __launch_bounds__(768) k_adjoint(const KArgs a) {
             const unsigned wmask = __ballot_sync(0xFFFFFFFFu, wins);
             if (wins) {
                 const PredRec pr = load_pred(spred + (ev.pred_begin - meta.z + (int)k));
-                if (pr.src_slot >= 0) atomicAdd(&cnt[pr.src_slot * kTile + lane], c);
+                if (WIN_SMEM) {
+                    if (pr.src_slot >= 0) atomicAdd(&cnt[pr.src_slot * kTile + lane], c);
+                } else {
+                    atomicAdd(&a.cnt_rows[(int64_t)row_off(pr.src_user, (uint32_t)a.ld) + s], c);
+                }
                 // lanes whose winner is the same predecessor add their link terms in one atomic
                 const long long gl = (pr.link >= 0 && dfac != 0.0f)
                                          ? __float2ll_rn((float)c * dfac * (float)(1 << kAdjDfacShift))
@@ -109,13 +128,23 @@ __global__ void __launch_bounds__(768) k_adjoint(const KArgs a) {
         __syncthreads();
         if (threadIdx.x == 0 && j + 2 < NS) stage_issue(a, l - 2, stage_buf0 + b * a.stage_bytes, &bars[b]);
     }
+    if (WIN_SMEM && (a.adj_flags & kAdjCntSave)) {  // counts of earlier events, for the next block down
+        uint32_t *out = a.cnt_ckpt + (int64_t)blockIdx.x * cnt_n;
+        for (int i = threadIdx.x; i < cnt_n; i += blockDim.x) out[i] = cnt[i];
+    }
 }
 
-template <bool POSITIVE, int TS>
+// Forward half: the propagation kernel in its adjoint form.  With the window
+// off chip, predecessors come from (and realized times go to) the global rows
+// a.scratch[E][ld], which hold every event's time: a level block's recomputation
+// needs no other checkpoint.
+template <bool WIN_SMEM, bool POSITIVE, int TS>
 __global__ void __launch_bounds__(768) k_adjoint_forward(const KArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
-    propagate_tile<false, true, false, POSITIVE, true, TS>(a, (int64_t)blockIdx.x, nullptr, a.ld, false, smem,
-                                                           reinterpret_cast<uint64_t *>(smem + a.smem_bar_off), false);
+    propagate_tile<false, WIN_SMEM, false, POSITIVE, true, TS>(a, (int64_t)blockIdx.x, WIN_SMEM ? nullptr : a.scratch,
+                                                               a.ld, false, smem,
+                                                               reinterpret_cast<uint64_t *>(smem + a.smem_bar_off),
+                                                               false);
 }
 
 // grad_earliest[e] = grad_e[e] / n, grad_base[l] = grad_l[l] 2^-20 / n, and the
@@ -141,21 +170,34 @@ __global__ void k_adjoint_finish(const long long *grad_e, const long long *grad_
     }
 }
 
-cudaError_t launch_adjoint(const KArgs &a, cudaStream_t st) {
+template <bool WIN_SMEM>
+static void (*forward_kernel(const KArgs &a))(const KArgs) {
+    if (a.tables_in_smem)
+        return a.positive ? k_adjoint_forward<WIN_SMEM, true, kTablesSmem> : k_adjoint_forward<WIN_SMEM, false, kTablesSmem>;
+    return a.positive ? k_adjoint_forward<WIN_SMEM, true, kTablesGlobal> : k_adjoint_forward<WIN_SMEM, false, kTablesGlobal>;
+}
+
+// The forward half over stages [a.stage_begin, a.stage_end).
+cudaError_t launch_adjoint_forward(const KArgs &a, cudaStream_t st) {
     if (a.n <= 0) return cudaSuccess;
     const dim3 grid((unsigned)((a.n + kTile - 1) / kTile)), block((unsigned)(a.n_warps * 32));
     const size_t smem = (size_t)a.smem_total;
-    void (*fwd)(const KArgs);
-    if (a.tables_in_smem) fwd = a.positive ? k_adjoint_forward<true, kTablesSmem> : k_adjoint_forward<false, kTablesSmem>;
-    else fwd = a.positive ? k_adjoint_forward<true, kTablesGlobal> : k_adjoint_forward<false, kTablesGlobal>;
+    void (*fwd)(const KArgs) = a.win_smem ? forward_kernel<true>(a) : forward_kernel<false>(a);
     cudaError_t e = raise_smem_limit((const void *)fwd, smem);
     if (e != cudaSuccess) return e;
     fwd<<<grid, block, smem, st>>>(a);
-    e = cudaGetLastError();
+    return cudaGetLastError();
+}
+
+// The backward half over stages [a.stage_begin, a.stage_end), last stage first.
+cudaError_t launch_adjoint_backward(const KArgs &a, cudaStream_t st) {
+    if (a.n <= 0) return cudaSuccess;
+    const dim3 grid((unsigned)((a.n + kTile - 1) / kTile)), block((unsigned)(a.n_warps * 32));
+    const size_t smem = (size_t)a.smem_total;
+    void (*bwd)(const KArgs) = a.win_smem ? k_adjoint<true> : k_adjoint<false>;
+    cudaError_t e = raise_smem_limit((const void *)bwd, smem);
     if (e != cudaSuccess) return e;
-    e = raise_smem_limit((const void *)k_adjoint, smem);
-    if (e != cudaSuccess) return e;
-    k_adjoint<<<grid, block, smem, st>>>(a);
+    bwd<<<grid, block, smem, st>>>(a);
     return cudaGetLastError();
 }
 

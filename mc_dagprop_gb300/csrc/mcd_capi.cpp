@@ -241,6 +241,10 @@ void carve(mcd_dag *g, int64_t C, int sets, bool staged, ChunkBufs cb[2]) {
 // decides, so two different inputs never share an image.  The cache holds weak
 // references: an image lives as long as a handle uses it.
 
+}  // namespace
+
+namespace mcd {
+
 void put_bytes(std::vector<unsigned char> &k, const void *p, size_t n) {
     if (!n) return;
     const size_t o = k.size();
@@ -327,6 +331,10 @@ uint64_t hash_bytes(const std::vector<unsigned char> &k) {
     h = (h ^ tail) * 0xC4CEB9FE1A85EC53ull;
     return h ^ (h >> 29);
 }
+
+}  // namespace mcd
+
+namespace {
 
 std::mutex g_cache_mu;
 std::unordered_multimap<uint64_t, std::weak_ptr<const DagImage>> g_cache;

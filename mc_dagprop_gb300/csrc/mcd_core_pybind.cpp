@@ -16,8 +16,12 @@
 #include <pybind11/pybind11.h>
 #include <pybind11/stl.h>
 
+#include <unistd.h>
+
 #include <cstdint>
+#include <cstdlib>
 #include <limits>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -124,18 +128,108 @@ struct Generator {
     }
 };
 
+// ---- Host memory for results: page-locked blocks, recycled.
+// The device writes results into page-locked host memory at the link's full
+// rate, but pinning memory is slow (about as slow as the copy it speeds up), so
+// blocks are kept when their arrays die and handed to the next call that fits.
+// The pool holds at most a quarter of the machine's memory
+// ($MCD_PINNED_POOL_MB overrides; 0 turns it off); past that, results go to
+// ordinary (pageable) memory, copied through the device.  The pool lives until
+// the process exits.
+class PinnedPool {
+   public:
+    static PinnedPool &get() {
+        static PinnedPool *p = new PinnedPool();  // never destroyed: outlives the CUDA context's teardown
+        return *p;
+    }
+    // A block of at least `bytes`, or null (pool full or disabled).
+    void *acquire(size_t bytes) {
+        if (bytes == 0) return nullptr;
+        std::lock_guard<std::mutex> lk(mu_);
+        auto it = free_.lower_bound(bytes);
+        if (it != free_.end() && it->first <= bytes + bytes / 4) {  // a free block that fits without much waste
+            void *p = it->second;
+            free_.erase(it);
+            return p;
+        }
+        while (held_ + bytes > cap_ && !free_.empty()) {  // make room: return the largest free blocks
+            auto big = std::prev(free_.end());
+            mcd_host_free(big->second);
+            held_ -= big->first;
+            size_.erase(big->second);
+            free_.erase(big);
+        }
+        if (held_ + bytes > cap_) return nullptr;
+        void *p = nullptr;
+        if (mcd_host_alloc(bytes, &p) != MCD_OK || !p) return nullptr;
+        held_ += bytes;
+        size_[p] = bytes;
+        return p;
+    }
+    void release(void *p) {
+        if (!p) return;
+        std::lock_guard<std::mutex> lk(mu_);
+        auto it = size_.find(p);
+        if (it != size_.end()) free_.emplace(it->second, p);
+    }
+
+   private:
+    PinnedPool() {
+        const long pages = sysconf(_SC_PHYS_PAGES), page = sysconf(_SC_PAGE_SIZE);
+        cap_ = pages > 0 && page > 0 ? (size_t)pages * (size_t)page / 4 : 0;
+        if (const char *e = std::getenv("MCD_PINNED_POOL_MB")) cap_ = (size_t)std::max(0ll, std::atoll(e)) << 20;
+    }
+    std::mutex mu_;
+    std::multimap<size_t, void *> free_;
+    std::unordered_map<void *, size_t> size_;
+    size_t held_ = 0, cap_ = 0;
+};
+
+// One result buffer: a pooled page-locked block, else pageable memory.
+struct HostBuf {
+    void *p = nullptr;
+    bool pinned = false;
+    HostBuf() = default;
+    explicit HostBuf(size_t bytes) {
+        p = PinnedPool::get().acquire(bytes);
+        pinned = p != nullptr;
+        if (!p && bytes) {
+            p = std::malloc(bytes);
+            if (!p) throw std::bad_alloc();
+        }
+    }
+    HostBuf(const HostBuf &) = delete;
+    HostBuf &operator=(const HostBuf &) = delete;
+    ~HostBuf() {
+        if (pinned) PinnedPool::get().release(p);
+        else std::free(p);
+    }
+};
+
+// A numpy array of `shape` over a new HostBuf, which returns to the pool when
+// the array dies.
+template <typename T>
+py::array_t<T> host_array(std::vector<py::ssize_t> shape) {
+    size_t n = 1;
+    for (py::ssize_t d : shape) n *= (size_t)d;
+    auto *buf = new HostBuf(n * sizeof(T));
+    py::capsule owner(buf, [](void *b) { delete static_cast<HostBuf *>(b); });
+    return py::array_t<T>(shape, static_cast<T *>(buf->p), owner);
+}
+
 // ---- SimResult: one sample of a result block, exposed as zero-copy numpy views.
 struct SimBlock {
     int64_t E = 0, L = 0;
-    std::vector<double> realized, durations;
-    std::vector<int32_t> cause;
+    std::unique_ptr<HostBuf> realized, durations, cause;
 };
 struct SimResult {
     std::shared_ptr<SimBlock> blk;
     int64_t i = 0;
-    double *realized() const { return blk->realized.data() + i * blk->E; }
-    double *durations() const { return blk->durations.data() + i * blk->L; }
-    int32_t *cause() const { return blk->cause.data() + i * blk->E; }
+    double *realized() const { return static_cast<double *>(blk->realized->p) + i * blk->E; }
+    double *durations() const {
+        return blk->durations ? static_cast<double *>(blk->durations->p) + i * blk->L : nullptr;
+    }
+    int32_t *cause() const { return static_cast<int32_t *>(blk->cause->p) + i * blk->E; }
 };
 
 // ---- MonteCarloPropagator
@@ -206,14 +300,15 @@ class Propagator {
         const int64_t n = (int64_t)seeds.size();
         blk->E = E_;
         blk->L = L_;
-        blk->realized.resize((size_t)(n * E_));
-        if (want_dur) blk->durations.resize((size_t)(n * L_));
-        blk->cause.resize((size_t)(n * E_));
+        blk->realized.reset(new HostBuf((size_t)(n * E_) * sizeof(double)));
+        if (want_dur) blk->durations.reset(new HostBuf((size_t)(n * L_) * sizeof(double)));
+        blk->cause.reset(new HostBuf((size_t)(n * E_) * sizeof(int32_t)));
         int rc;
         {
             py::gil_scoped_release release;
-            rc = mcd_run_many_host(dag_.get(), seeds.data(), n, blk->realized.data(),
-                                   want_dur ? blk->durations.data() : nullptr, blk->cause.data());
+            rc = mcd_run_many_host(dag_.get(), seeds.data(), n, static_cast<double *>(blk->realized->p),
+                                   want_dur ? static_cast<double *>(blk->durations->p) : nullptr,
+                                   static_cast<int32_t *>(blk->cause->p));
         }
         raise_status(rc);
         return blk;
@@ -234,12 +329,12 @@ class Propagator {
     py::tuple run_many_arrays(py::array_t<int64_t, py::array::c_style | py::array::forcecast> seeds,
                               bool durations) {
         const int64_t n = (int64_t)seeds.size();
-        py::array_t<double> real({n, E_});
-        py::array_t<int32_t> cause({n, E_});
+        py::array_t<double> real = host_array<double>({n, E_});
+        py::array_t<int32_t> cause = host_array<int32_t>({n, E_});
         py::object dur = py::none();
         double *dp = nullptr;
         if (durations) {
-            py::array_t<double> d({n, L_});
+            py::array_t<double> d = host_array<double>({n, L_});
             dp = d.mutable_data();
             dur = d;
         }
@@ -258,8 +353,8 @@ class Propagator {
         if (durations.ndim() != 2 || durations.shape(1) != L_)
             throw py::value_error("durations must have shape (n_samples, activity_count())");
         const int64_t n = durations.shape(0);
-        py::array_t<double> real({n, E_});
-        py::array_t<int32_t> cause({n, E_});
+        py::array_t<double> real = host_array<double>({n, E_});
+        py::array_t<int32_t> cause = host_array<int32_t>({n, E_});
         const double *dp = durations.data();
         double *rp = real.mutable_data();
         int32_t *cp = cause.mutable_data();
@@ -319,10 +414,15 @@ class Propagator {
             rc = mcd_gradient_host(dag_.get(), seed0, n, &obj, gp, bp);
         }
         raise_status(rc);
+        int64_t plan[3] = {0, 0, 0};
+        raise_status(mcd_gradient_plan(dag_.get(), &plan[0], &plan[1], &plan[2]));
         py::dict d;
         d["objective"] = obj;
         d["grad_earliest"] = ge;
         d["grad_base"] = gb;
+        d["samples_per_chunk"] = plan[0];
+        d["level_blocks"] = plan[1];
+        d["buffer_bytes"] = plan[2];
         return d;
     }
     py::tuple link_streams() const {
@@ -517,6 +617,10 @@ class Server {
         d["compile_seconds"] = i.compile_seconds;
         d["upload_seconds"] = i.upload_seconds;
         d["launch_seconds"] = i.launch_seconds;
+        d["resident_hits"] = i.resident_hits;
+        d["resident_dags"] = i.resident_dags;
+        d["resident_bytes"] = i.resident_bytes;
+        d["evicted"] = i.evicted;
         return d;
     }
 
@@ -712,7 +816,9 @@ PYBIND11_MODULE(_core, m) {
              "dict of mean, p50, p90, p99, p_on_time (and the raw histogram when hist=True)")
         .def("gradient", &Propagator::gradient, py::arg("n"), py::arg("seed0") = 0,
              "Pathwise gradient of J = mean_s sum_e (realized - earliest) over seeds seed0..seed0+n-1: "
-             "dict of objective, grad_earliest (per event), grad_base (per link index)")
+             "dict of objective, grad_earliest (per event), grad_base (per link index), and the plan used "
+             "(samples_per_chunk, level_blocks: 1 = every winner kept, more = level blocks recomputed from "
+             "checkpoints; buffer_bytes)")
         .def("info", &Propagator::info, "Compiled-DAG facts")
         .def("link_streams", &Propagator::link_streams,
              "(block, word) per link: the Philox block of its draws and its first word (-1: whole block)")

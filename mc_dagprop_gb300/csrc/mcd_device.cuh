@@ -225,7 +225,7 @@ __device__ __forceinline__ double draw_empirical(const DistParam &p, const Alias
 template <bool STAGED, bool TSMEM>
 __device__ __forceinline__ double sampled_duration(const KArgs &a, int32_t kd, double v, int32_t dvo, uint32_t block,
                                                    uint32_t link, uint64_t seed, U4 &grp, const unsigned char *smem,
-                                                   int stage, float &dfac) {
+                                                   int buf, float &dfac) {
     const DistParam *dists = TSMEM ? reinterpret_cast<const DistParam *>(smem + a.smem_tables_off) : a.dist;
     const DistParam &p = dists[kd >> 8];
     int32_t *err = a.err;
@@ -240,7 +240,7 @@ __device__ __forceinline__ double sampled_duration(const KArgs &a, int32_t kd, d
     if (kind == K_EXP) return draw_exponential(p, v, r, dfac);
     const double *vt = nullptr;
     if (dvo >= 0)
-        vt = STAGED ? reinterpret_cast<const double *>(smem + a.smem_stage_off + (stage & 1) * a.stage_bytes + dvo)
+        vt = STAGED ? reinterpret_cast<const double *>(smem + a.smem_stage_off + buf * a.stage_bytes + dvo)
                     : a.vals + (dvo ^ kVtGlobal);
     return draw_empirical(p, alias, picks, vt, v, kind == K_EMP_REL, r, grp.y, (kd & KD_TWO_WORD) != 0, dfac);
 }
@@ -251,7 +251,7 @@ __device__ __forceinline__ double sampled_duration(const KArgs &a, int32_t kd, d
 // grp: the words of the block the event's previous exponential or empirical
 // reference drew, redrawn here unless KD_REUSE says they are this link's block.
 // link: the link's index (the key of its own redraw blocks); dvo: the record's
-// dvo (PredRec); stage: the stage whose staging buffer holds the link's
+// dvo (PredRec); buf: the staging buffer (0 or 1) that holds the link's
 // duration table (STAGED; otherwise the table is in KArgs::vals).  Every table
 // address is derived here from the kernel arguments, so that the propagation
 // loop keeps no table pointers live.
@@ -262,14 +262,14 @@ enum : int { kTablesGlobal = 0, kTablesSmem = 1, kTablesEither = 2 };
 template <bool STAGED, int TS>
 __device__ __forceinline__ double link_duration(const KArgs &a, int32_t kd, double v, int32_t dvo, uint32_t block,
                                                 uint32_t link, uint64_t seed, U4 &grp, const unsigned char *smem,
-                                                int stage, float &dfac) {
+                                                int buf, float &dfac) {
     if ((kd & KD_KIND_MASK) == K_FIXED) {
         dfac = __int_as_float(dvo);
         return v;
     }
     if (TS == kTablesSmem || (TS == kTablesEither && a.tables_in_smem))
-        return sampled_duration<STAGED, true>(a, kd, v, dvo, block, link, seed, grp, smem, stage, dfac);
-    return sampled_duration<STAGED, false>(a, kd, v, dvo, block, link, seed, grp, smem, stage, dfac);
+        return sampled_duration<STAGED, true>(a, kd, v, dvo, block, link, seed, grp, smem, buf, dfac);
+    return sampled_duration<STAGED, false>(a, kd, v, dvo, block, link, seed, grp, smem, buf, dfac);
 }
 
 // ---------------------------------------------------------------- records
@@ -473,10 +473,11 @@ __device__ __forceinline__ int take_next(uint32_t ctr) {
 // compiler orders them costliest first).  STAGED: sev/spred point into the
 // staging buffer in shared memory; otherwise into global memory.  pred0: the
 // stage's first predecessor record (the records' pred_begin/pred_end are
-// global indices).
+// global indices); ev0: its first event's compiled index; buf: the staging
+// buffer (0 or 1) that holds the stage.
 template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ, bool STAGED, int TS>
-__device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec *sev, const PredRec *spred, int pred0,
-                                             int n_ev, uint32_t ctr, const TileCtx &t, unsigned char *smem,
+__device__ __forceinline__ void stage_events(const KArgs &a, int buf, const EvRec *sev, const PredRec *spred, int pred0,
+                                             int ev0, int n_ev, uint32_t ctr, const TileCtx &t, unsigned char *smem,
                                              U4 &grp) {
     double *win = reinterpret_cast<double *>(smem);
     const int lane = t.lane;
@@ -491,7 +492,8 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec 
         const EvRec ev = load_ev(sev + i);
         // the event's earliest in ticks, needed after its predecessors (the load's
         // latency hides behind them)
-        const long long te = (STATS || ADJ) && a.stats_fixed ? __ldg(a.te + ev.user) : 0ll;
+        const long long te =
+            (STATS || (ADJ && (a.adj_flags & kAdjObjective))) && a.stats_fixed ? __ldg(a.te + ev.user) : 0ll;
         // POSITIVE: keys are the bits themselves (init_key == init_bits, ub_key == ub_bits),
         // so one 64-bit value carries both
         long long lk = POSITIVE ? ev.init_bits : ev.init_key, lbits = ev.init_bits;
@@ -508,7 +510,7 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec 
                 dur = (t.active && pr.link >= 0) ? __ldg(at_row(t.dincol, pr.link, t.ld_in8)) : 0.0;
             } else {
                 dur = link_duration<STAGED, TS>(a, pr.kd, pr.v, pr.dvo, (uint32_t)pr.block, (uint32_t)pr.link, t.seed,
-                                            grp, smem, l, dfac);
+                                            grp, smem, buf, dfac);
                 if (!STATS && !ADJ && (pr.kd & KD_WRITE) && t.dcol) *at_row(t.dcol, pr.link, t.ld8) = dur;
             }
             // with the window on chip every source has a slot (the compiler checks it)
@@ -540,9 +542,9 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec 
         if (STATS) accumulate_stats<POSITIVE>(a, ev, lbits, te, t.active, t.active_mask);
         if (ADJ) {
             const bool delayed = lk > (POSITIVE ? ev.init_bits : ev.init_key);  // realized > earliest
-            accumulate_sum<POSITIVE>(a, ev, lbits, te, t.active);
-            if (t.active) {
-                const int64_t o = (int64_t)row_off(ev.user, (uint32_t)a.ld) + t.s;
+            if (a.adj_flags & kAdjObjective) accumulate_sum<POSITIVE>(a, ev, lbits, te, t.active);
+            if (t.active && a.adj_code) {  // rows by compiled index, from the block's first event
+                const int64_t o = (int64_t)row_off(ev0 + i - a.code_base, (uint32_t)a.ld) + t.s;
                 a.adj_code[o] = (uint16_t)(win_code | (delayed ? kAdjDelayed : 0u));
                 a.adj_dfac[o] = win_dfac;
             }
@@ -574,7 +576,12 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int l, const EvRec 
 // and initialised again between tiles).
 // ADJ: the forward half of the adjoint: per event and sample, the winning
 // predecessor's position, clamp and delay flags and d(duration)/d(base) go to
-// a.adj_code / a.adj_dfac, and (realized - earliest) to the objective sum.
+// a.adj_code / a.adj_dfac (when not null), and (realized - earliest) to the
+// objective sum (kAdjObjective).  It runs stages [a.stage_begin, a.stage_end)
+// only: with the window on chip it starts from the window a.win_in holds for
+// this tile (when not null), and saves the window into a.win_ckpt as each of the
+// a.blk_start stages begins -- the checkpoints a level-block recomputation
+// starts from.
 template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ = false, int TS = kTablesEither>
 __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, double *rows, int64_t rows_ld,
                                                bool rows_tile_local, unsigned char *smem, uint64_t *bars,
@@ -605,6 +612,16 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
         for (int i = threadIdx.x; i < n8; i += blockDim.x)
             reinterpret_cast<uint2 *>(s_dist)[i] = reinterpret_cast<const uint2 *>(a.dist)[i];
     }
+    // stages run: all, or (adjoint) one block of them
+    const int s_begin = ADJ ? a.stage_begin : 0;
+    const int s_end = ADJ ? a.stage_end : a.n_stages;
+    const int win_n = a.window_slots * kTile;  // doubles of one tile's window
+    if (ADJ && WIN_SMEM && a.win_in) {  // a block recomputed from its checkpoint
+        const double *src = a.win_in + (int64_t)tile * win_n;
+        double *win = reinterpret_cast<double *>(smem);
+        for (int i = threadIdx.x; i < win_n; i += blockDim.x) win[i] = src[i];
+    }
+    int next_blk = 0;  // the next checkpoint to save (ADJ with a.win_ckpt)
     int *stage_ctr = reinterpret_cast<int *>(bars + 2);
     U4 grp{};  // the words of the Philox block the current event last drew (see KD_REUSE)
     if (threadIdx.x == 0) {
@@ -625,45 +642,54 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
     __syncthreads();
     char *stage_buf0 = reinterpret_cast<char *>(smem + a.smem_stage_off);
     if (threadIdx.x == 0) {
-        if (a.n_stages > 0) stage_issue(a, 0, stage_buf0, &bars[0]);
-        if (a.n_stages > 1) stage_issue(a, 1, stage_buf0 + a.stage_bytes, &bars[1]);
+        if (s_begin < s_end) stage_issue(a, s_begin, stage_buf0, &bars[0]);
+        if (s_begin + 1 < s_end) stage_issue(a, s_begin + 1, stage_buf0 + a.stage_bytes, &bars[1]);
     }
 
     // a stage's metadata is loaded one stage ahead: its latency then hides behind
     // the previous stage's events instead of stalling every warp at the stage start
     const int4 *smeta = reinterpret_cast<const int4 *>(a.stage_meta);
     int4 meta_next = make_int4(0, 0, 0, 0), mv_next = make_int4(0, 0, 0, 0);
-    if (a.n_stages > 0) {
-        meta_next = __ldg(smeta);
-        mv_next = __ldg(smeta + 1);
+    if (s_begin < s_end) {
+        meta_next = __ldg(smeta + 2 * s_begin);
+        mv_next = __ldg(smeta + 2 * s_begin + 1);
     }
-    for (int l = 0; l < a.n_stages; ++l) {
+    for (int l = s_begin; l < s_end; ++l) {
         const int4 meta = meta_next, mv = mv_next;
-        if (l + 1 < a.n_stages) {
+        if (l + 1 < s_end) {
             meta_next = __ldg(smeta + 2 * (l + 1));
             mv_next = __ldg(smeta + 2 * (l + 1) + 1);
         }
-        const int b = l & 1;
-        const bool ok = stage_wait(&bars[b], (uint32_t)((l >> 1) & 1), a.err);
+        const int j = l - s_begin;  // stages run so far: buffer, barrier phase and counter
+        const int b = j & 1;
+        const bool ok = stage_wait(&bars[b], (uint32_t)((j >> 1) & 1), a.err);
         if (__syncthreads_or(!ok)) {  // a copy that never landed: drain, then leave together
-            if (threadIdx.x == 0 && l + 1 < a.n_stages)
-                stage_wait(&bars[b ^ 1], (uint32_t)(((l + 1) >> 1) & 1), a.err);
+            if (threadIdx.x == 0 && l + 1 < s_end)
+                stage_wait(&bars[b ^ 1], (uint32_t)(((j + 1) >> 1) & 1), a.err);
             __syncthreads();
             return false;
         }
-        if (threadIdx.x == 0) stage_ctr[(l + 1) & 1] = 0;  // last used by stage l - 1, before the barrier
-        const uint32_t ctr = smem_u32(&stage_ctr[l & 1]);
+        if (ADJ && WIN_SMEM && a.win_ckpt && next_blk < a.n_blk && l == __ldg(a.blk_start + next_blk)) {
+            // the window as this block starts (every earlier stage's stores are behind the barrier)
+            double *dst = a.win_ckpt + ((int64_t)next_blk * gridDim.x + tile) * win_n;
+            const double *win = reinterpret_cast<const double *>(smem);
+            for (int i = threadIdx.x; i < win_n; i += blockDim.x) dst[i] = win[i];
+            ++next_blk;
+            __syncthreads();  // before this stage's events overwrite slots
+        }
+        if (threadIdx.x == 0) stage_ctr[(j + 1) & 1] = 0;  // last used by stage l - 1, before the barrier
+        const uint32_t ctr = smem_u32(&stage_ctr[j & 1]);
         if (meta.y >= 0) {  // records in the staging buffer (shared memory)
             const unsigned char *buf = smem + a.smem_stage_off + b * a.stage_bytes;
             stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, true, TS>(
-                a, l, reinterpret_cast<const EvRec *>(buf), reinterpret_cast<const PredRec *>(buf + mv.z), meta.z,
-                meta.y, ctr, t, smem, grp);
+                a, b, reinterpret_cast<const EvRec *>(buf), reinterpret_cast<const PredRec *>(buf + mv.z), meta.z,
+                meta.x, meta.y, ctr, t, smem, grp);
         } else {  // a stage whose records exceed the buffer is read from global memory
-            stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, false, TS>(a, l, a.ev + meta.x, a.pred + meta.z, meta.z,
-                                                                       -meta.y, ctr, t, smem, grp);
+            stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, false, TS>(a, b, a.ev + meta.x, a.pred + meta.z,
+                                                                       meta.z, meta.x, -meta.y, ctr, t, smem, grp);
         }
         __syncthreads();
-        if (threadIdx.x == 0 && l + 2 < a.n_stages)
+        if (threadIdx.x == 0 && l + 2 < s_end)
             stage_issue(a, l + 2, stage_buf0 + b * a.stage_bytes, &bars[b]);
     }
     // Aux pass: duration rows of links no precedence entry references.

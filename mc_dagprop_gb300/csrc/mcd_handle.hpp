@@ -59,6 +59,7 @@ struct mcd_dag {
     int32_t *d_err = nullptr;  // latched kernel errors of this handle's launches
     char *ws = nullptr;        // workspace
     size_t ws_bytes = 0;
+    int64_t last_adj_plan[3] = {0, 0, 0};  // the last gradient's samples per chunk, level blocks, buffer bytes
     explicit mcd_dag(std::shared_ptr<const mcd::DagImage> image)
         : img(std::move(image)), h(img->h), device(img->device), dbytes(img->dbytes), d_ev(img->d_ev),
           d_pred(img->d_pred), d_aux(img->d_aux), d_dist(img->d_dist), d_vals(img->d_vals), d_wk(img->d_wk),

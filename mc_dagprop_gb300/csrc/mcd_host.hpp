@@ -103,6 +103,14 @@ std::vector<unsigned char> tables_block(const HostDag &h);
 
 // n_warps: warps per CTA the kernels will run with (0: chosen from the DAG's width).
 void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &out, int32_t n_warps);
+
+// The content key of a compiled DAG: everything compile_dag reads, serialized
+// (the arrays, the generator, warps per CTA, device, the compiler's environment
+// overrides); false where the arrays are too malformed to read safely.  Caches
+// of compiled DAGs pick a bucket by hash_bytes and decide by full comparison.
+bool image_key(const mcd_dag_desc &d, const mcd_generator &gen, int32_t n_warps, int device,
+               std::vector<unsigned char> &k);
+uint64_t hash_bytes(const std::vector<unsigned char> &k);
 int64_t order_key_host(int64_t bits);
 
 }  // namespace mcd

@@ -193,11 +193,27 @@ struct KArgs {
     const long long *te;          // [E] ticks_of(earliest, tick_q), caller order (fixed ticks only)
     uint32_t *hist;               // [E][kHistStride]
     // adjoint
-    uint16_t *adj_code;           // [E][ld] winner position and flags (forward), read backward
-    float *adj_dfac;              // [E][ld] d(duration)/d(base) of the winning link
+    uint16_t *adj_code;           // [events of the block][ld] winner position and flags (forward), read
+                                  // backward; row = compiled event index - code_base; null: not recorded
+    float *adj_dfac;              // [events of the block][ld] d(duration)/d(base) of the winning link
     long long *grad_e;            // [E] sum over samples of the earliest-time derivative (counts)
     long long *grad_l;            // [L] sum over samples of cnt * dfac * 2^20 per link
+    // adjoint by level blocks: the kernels run stages [stage_begin, stage_end)
+    int32_t stage_begin, stage_end;
+    int32_t code_base;            // compiled index of the event whose records are row 0 of adj_code
+    int32_t adj_flags;            // kAdjObjective | kAdjCntLoad | kAdjCntSave
+    const int32_t *blk_start;     // [n_blk] first stage of each block after the first (checkpoint pass)
+    int32_t n_blk;
+    double *win_ckpt;             // [n_blk][tiles][window_slots * 32]: the window as block k + 1 starts
+    const double *win_in;         // [tiles][window_slots * 32]: the window to start from, or null
+    uint32_t *cnt_ckpt;           // [tiles][window_slots * 32]: backward counts carried between blocks
+    uint32_t *cnt_rows;           // [E][ld] backward counts by caller index (window not on chip)
 };
+
+// KArgs::adj_flags
+constexpr int32_t kAdjObjective = 1;  // forward: add (realized - earliest) to the objective sum
+constexpr int32_t kAdjCntLoad = 2;    // backward: start from the counts in cnt_ckpt (else zero)
+constexpr int32_t kAdjCntSave = 4;    // backward: leave the counts in cnt_ckpt for the next block
 
 // Arguments of the persistent batch kernel.
 struct BatchArgs {

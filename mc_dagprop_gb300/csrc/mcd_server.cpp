@@ -4,9 +4,16 @@
 // statistics.  submit() copies the inputs and returns a ticket at once.
 //   - A pool of host threads compiles the DAGs (mcd_compile.cpp) with warps per
 //     CTA from each DAG's width (rounded to 2, 4, 8 or 16), waits until the
-//     request's device block fits the memory budget, takes the block from the
-//     stream-ordered allocator and uploads the compiled records on its own
-//     stream: uploads run in parallel, off the scheduler.
+//     request's device blocks fit the memory budget, takes them from the
+//     stream-ordered allocator and uploads on its own stream: uploads run in
+//     parallel, off the scheduler.
+//   - Compiled DAGs stay resident on the device after their requests finish,
+//     keyed by their content (the DAG's arrays, the generator, warps per CTA):
+//     a request for a DAG already resident skips the compile and the upload of
+//     its records and only gets accumulators of its own.  Resident DAGs no
+//     request uses are evicted, least recently used first, when the budget
+//     needs room.  (Draws need no per-request generator state on the device:
+//     Philox is keyed by the sample's seed, the link and the attempt.)
 //   - Requests are batched by class: equal warps per CTA, equal CTAs per SM for
 //     their shared-memory layout (so no request lowers another's occupancy) and
 //     the same kernel variant (positive times or not, tables in shared memory or
@@ -51,14 +58,13 @@ namespace {
 
 enum State : int { Q_COMPILE = 0, Q_READY = 1, Q_RUNNING = 2, Q_DONE = 3, Q_FAILED = 4 };
 
-// Offsets of one request's device block: compiled records, then the
-// accumulators (zeroed at upload), then the statistics.
-struct Layout {
-    size_t ev, pred, aux, tables, vals, wk, meta, earliest, ub, te, err, acc, hist, out, total;
+// Offsets inside a resident DAG's device block: its compiled records.
+struct ImgLayout {
+    size_t ev, pred, aux, tables, vals, wk, meta, earliest, ub, total;
 };
 
-Layout layout_of(const HostDag &h) {
-    Layout L{};
+ImgLayout img_layout_of(const HostDag &h) {
+    ImgLayout L{};
     size_t o = 0;
     auto take = [&](size_t bytes) {
         const size_t at = o;
@@ -74,14 +80,49 @@ Layout layout_of(const HostDag &h) {
     L.meta = take(h.stage_meta.size() * 4);
     L.earliest = take((size_t)h.E * 8);
     L.ub = take((size_t)h.E * 8);
-    L.te = take((size_t)h.E * 8);
-    L.err = take(4);
-    L.acc = take((size_t)h.E * 8);
-    L.hist = take((size_t)h.E * kHistStride * 4);
-    L.out = take((size_t)h.E * 5 * 8);
     L.total = o;
     return L;
 }
+
+// Offsets inside a request's own device block: the earliest times in the
+// request's ticks, then the error flag and the accumulators (zeroed at upload),
+// then the statistics.
+struct RqLayout {
+    size_t te, err, acc, hist, out, total;
+};
+
+RqLayout rq_layout_of(int32_t E) {
+    RqLayout L{};
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o += align_up(std::max<size_t>(bytes, 1), 256);
+        return at;
+    };
+    L.te = take((size_t)E * 8);
+    L.err = take(4);
+    L.acc = take((size_t)E * 8);
+    L.hist = take((size_t)E * kHistStride * 4);
+    L.out = take((size_t)E * 5 * 8);
+    L.total = o;
+    return L;
+}
+
+// A compiled DAG on the device, shared by the requests for it.
+struct Resident {
+    std::vector<unsigned char> key;  // empty: not shared (malformed arrays)
+    uint64_t hash = 0;
+    HostDag h;                       // after the upload: the scalars and the earliest times
+    ImgLayout lay{};
+    char *dimg = nullptr;
+    size_t bytes = 0;
+    int32_t per_sm = 1;              // batch class: (h.n_warps, per_sm)
+    double tile_cost = 0;            // work per 32-sample tile, for longest-first ordering
+    int refs = 0;                    // requests holding it (compiling, waiting, uploaded or running)
+    bool ready = false, failed = false;
+    std::string error;
+    uint64_t last_use = 0;
+};
 
 struct Request {
     int64_t ticket = 0;
@@ -92,12 +133,11 @@ struct Request {
     double max_delay = 0.0;
     mcd_generator gen;
     int64_t seed0 = 0, n = 0;
-    // compiled (records dropped after upload)
-    HostDag h;
-    Layout lay{};
-    size_t bytes = 0;       // device block
-    int32_t per_sm = 1;     // batch class: (h.n_warps, per_sm)
-    double tile_cost = 0;   // work per 32-sample tile, for longest-first ordering
+    // the compiled DAG (shared) and this request's own device block
+    std::shared_ptr<Resident> res;
+    RqLayout lay{};
+    size_t bytes = 0;       // own device block
+    int32_t E = 0;
     std::string error;
     // device (uploaded until the batch completes)
     char *dblock = nullptr;
@@ -144,6 +184,11 @@ struct mcd_server {
     int64_t bytes_in_use = 0;
     int64_t completed = 0, launched_batches = 0, running = 0, pending = 0;
     double compile_s = 0.0, upload_s = 0.0, launch_s = 0.0;
+    // resident compiled DAGs by content hash; their bytes count in bytes_in_use
+    std::unordered_multimap<uint64_t, std::shared_ptr<Resident>> residents;
+    std::condition_variable cv_resident;
+    uint64_t use_clock = 0;
+    int64_t resident_hits = 0, resident_bytes = 0, evicted = 0;
     char *zeros = nullptr;  // pinned zero bytes: accumulators are cleared by the copy engines
     std::string fatal;      // a CUDA failure of the scheduler: every later call reports it
 };
@@ -158,19 +203,21 @@ double seconds_since(Clock::time_point t0) { return std::chrono::duration<double
 
 // Kernel and finish arguments of an uploaded request.
 void request_args(Request *r) {
-    const HostDag &h = r->h;
-    const Layout &L = r->lay;
+    const HostDag &h = r->res->h;
+    const ImgLayout &I = r->res->lay;
+    const RqLayout &L = r->lay;
+    const char *g = r->res->dimg;
     char *b = r->dblock;
     const StatsParams sp = stats_params(h, r->n);
     KArgs &a = r->ka;
     a = KArgs{};
-    a.ev = reinterpret_cast<const EvRec *>(b + L.ev);
-    a.pred = reinterpret_cast<const PredRec *>(b + L.pred);
-    a.aux = reinterpret_cast<const LinkRec *>(b + L.aux);
-    a.dist = reinterpret_cast<const DistParam *>(b + L.tables);
-    a.vals = reinterpret_cast<const double *>(b + L.vals);
-    a.wk_off = reinterpret_cast<const int32_t *>(b + L.wk);
-    a.stage_meta = reinterpret_cast<const int32_t *>(b + L.meta);
+    a.ev = reinterpret_cast<const EvRec *>(g + I.ev);
+    a.pred = reinterpret_cast<const PredRec *>(g + I.pred);
+    a.aux = reinterpret_cast<const LinkRec *>(g + I.aux);
+    a.dist = reinterpret_cast<const DistParam *>(g + I.tables);
+    a.vals = reinterpret_cast<const double *>(g + I.vals);
+    a.wk_off = reinterpret_cast<const int32_t *>(g + I.wk);
+    a.stage_meta = reinterpret_cast<const int32_t *>(g + I.meta);
     a.n_stages = h.n_stages;
     a.n_warps = h.n_warps;
     a.n_aux = (int32_t)h.aux.size();
@@ -200,8 +247,8 @@ void request_args(Request *r) {
     f = FArgs{};
     f.acc = a.acc;
     f.hist = a.hist;
-    f.earliest = reinterpret_cast<const double *>(b + L.earliest);
-    f.ub = reinterpret_cast<const double *>(b + L.ub);
+    f.earliest = reinterpret_cast<const double *>(g + I.earliest);
+    f.ub = reinterpret_cast<const double *>(g + I.ub);
     f.E = h.E;
     f.stats_fixed = sp.fixed;
     f.tick_q = sp.q;
@@ -228,21 +275,24 @@ struct Staging {
     }
 };
 
-// Uploads the compiled records into the request's block and zeroes its
-// accumulators; returns when the copies have landed.  Only copies: a kernel
-// (such as a memset) would queue behind the persistent batch launches that
-// hold every SM, while the copy engines are free.
-void upload_request(const mcd_server *S, Request *r, cudaStream_t st, Staging &stage) {
-    const HostDag &h = r->h;
-    const Layout &L = r->lay;
-    if (L.err > stage.bytes) {
-        const size_t bytes = std::max(L.err, stage.bytes * 2);
-        if (stage.p) stage.retired.push_back(stage.p);
-        stage.p = nullptr;
-        stage.bytes = 0;
-        cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&stage.p), bytes, cudaHostAllocDefault), "staging");
-        stage.bytes = bytes;
-    }
+// Grows a compile thread's pinned staging buffer to at least `bytes`.
+void stage_reserve(Staging &stage, size_t bytes) {
+    if (bytes <= stage.bytes) return;
+    const size_t want = std::max(bytes, stage.bytes * 2);
+    if (stage.p) stage.retired.push_back(stage.p);
+    stage.p = nullptr;
+    stage.bytes = 0;
+    cuda_check(cudaHostAlloc(reinterpret_cast<void **>(&stage.p), want, cudaHostAllocDefault), "staging");
+    stage.bytes = want;
+}
+
+// Uploads a compiled DAG's records into its resident block; returns when the
+// copy has landed.  Only copies: a kernel would queue behind the persistent
+// batch launches that hold every SM, while the copy engines are free.
+void upload_image(Resident *res, cudaStream_t st, Staging &stage) {
+    const HostDag &h = res->h;
+    const ImgLayout &L = res->lay;
+    stage_reserve(stage, L.total);
     auto put = [&](size_t off, const void *src, size_t bytes) {
         if (bytes) std::memcpy(stage.p + off, src, bytes);
     };
@@ -258,22 +308,68 @@ void upload_request(const mcd_server *S, Request *r, cudaStream_t st, Staging &s
     put(L.meta, h.stage_meta.data(), h.stage_meta.size() * 4);
     put(L.earliest, h.earliest.data(), (size_t)h.E * 8);
     put(L.ub, h.ub.data(), (size_t)h.E * 8);
-    {  // earliest in ticks of the request's statistics
-        const StatsParams sp = stats_params(h, r->n);
-        auto *te = reinterpret_cast<long long *>(stage.p + L.te);
-        for (int32_t e = 0; e < h.E; ++e) {
-            long long b;
-            std::memcpy(&b, &h.earliest[(size_t)e], 8);
-            te[e] = sp.fixed ? ticks_of(b, sp.q) : 0ll;
-        }
+    cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&res->dimg), res->bytes, st), "resident allocation");
+    cuda_check(cudaMemcpyAsync(res->dimg, stage.p, L.total, cudaMemcpyHostToDevice, st), "resident upload");
+    cuda_check(cudaStreamSynchronize(st), "resident upload sync");  // the staging buffer is reused next
+}
+
+// Uploads a request's own block: the earliest times in the request's ticks,
+// then zeros over the error flag and the accumulators.
+void upload_request(const mcd_server *S, Request *r, cudaStream_t st, Staging &stage) {
+    const HostDag &h = r->res->h;
+    const RqLayout &L = r->lay;
+    stage_reserve(stage, L.err);
+    const StatsParams sp = stats_params(h, r->n);
+    auto *te = reinterpret_cast<long long *>(stage.p + L.te);
+    for (int32_t e = 0; e < h.E; ++e) {
+        long long b;
+        std::memcpy(&b, &h.earliest[(size_t)e], 8);
+        te[e] = sp.fixed ? ticks_of(b, sp.q) : 0ll;
     }
     cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&r->dblock), r->bytes, st), "request allocation");
     char *b = r->dblock;
-    cuda_check(cudaMemcpyAsync(b, stage.p, L.err, cudaMemcpyHostToDevice, st), "request upload");  // records
+    cuda_check(cudaMemcpyAsync(b, stage.p, L.err, cudaMemcpyHostToDevice, st), "request upload");
     for (size_t off = L.err; off < L.out; off += kZeroBytes)  // flags + accumulators
         cuda_check(cudaMemcpyAsync(b + off, S->zeros, std::min(kZeroBytes, L.out - off), cudaMemcpyHostToDevice, st),
                    "request reset");
     cuda_check(cudaStreamSynchronize(st), "request upload sync");  // the staging buffer is reused next
+}
+
+// Waits (caller holds the lock) until `bytes` more fit the budget, evicting
+// resident DAGs no request holds, least recently used first.  False when the
+// server stops.
+bool admit(mcd_server *S, std::unique_lock<std::mutex> &lk, size_t bytes, cudaStream_t st) {
+    for (;;) {
+        if (S->stop) return false;
+        if (S->bytes_in_use + (int64_t)bytes <= S->opt.memory_budget) {
+            S->bytes_in_use += (int64_t)bytes;
+            return true;
+        }
+        auto lru = S->residents.end();
+        for (auto it = S->residents.begin(); it != S->residents.end(); ++it)
+            if (it->second->ready && it->second->refs == 0 &&
+                (lru == S->residents.end() || it->second->last_use < lru->second->last_use))
+                lru = it;
+        if (lru == S->residents.end()) {  // nothing to evict: wait for running requests to finish
+            S->cv_budget.wait(lk);
+            continue;
+        }
+        std::shared_ptr<Resident> victim = lru->second;
+        S->residents.erase(lru);
+        cudaFreeAsync(victim->dimg, st);  // no batch uses it (refs == 0)
+        victim->dimg = nullptr;
+        S->bytes_in_use -= (int64_t)victim->bytes;
+        S->resident_bytes -= (int64_t)victim->bytes;
+        S->evicted += 1;
+    }
+}
+
+// Drops a request's hold on its resident DAG (caller holds the lock).
+void release_resident(mcd_server *S, Request *r) {
+    if (!r->res) return;
+    r->res->refs -= 1;
+    r->res->last_use = ++S->use_clock;
+    S->cv_budget.notify_all();
 }
 
 template <typename T>
@@ -315,7 +411,105 @@ void compile_loop(mcd_server *S) {
             d.pred_src = r->pred_src.data();
             d.pred_act = r->pred_act.data();
             d.max_delay = r->max_delay;
-            compile_dag(d, r->gen, r->h, S->opt.n_warps > 0 ? S->opt.n_warps : kBatchClassWarps);
+            const int32_t warps = S->opt.n_warps > 0 ? S->opt.n_warps : kBatchClassWarps;
+            // the resident DAG of this content, or a new one this thread compiles
+            std::vector<unsigned char> key;
+            const bool keyed = image_key(d, r->gen, warps, S->device, key);
+            const uint64_t hash = keyed ? hash_bytes(key) : 0;
+            bool mine = false;
+            {
+                std::unique_lock<std::mutex> lk(S->mu);
+                if (keyed) {
+                    auto range = S->residents.equal_range(hash);
+                    for (auto it = range.first; it != range.second; ++it)
+                        if (!it->second->failed && it->second->key == key) {
+                            r->res = it->second;
+                            break;
+                        }
+                }
+                if (r->res) {
+                    r->res->refs += 1;
+                    S->resident_hits += 1;
+                } else {
+                    r->res = std::make_shared<Resident>();
+                    r->res->hash = hash;
+                    r->res->refs = 1;
+                    if (keyed) {
+                        r->res->key = std::move(key);
+                        S->residents.emplace(hash, r->res);
+                    }
+                    mine = true;
+                }
+            }
+            Resident *res = r->res.get();
+            if (mine) {
+                try {
+                    compile_dag(d, r->gen, res->h, warps);
+                    if (!res->h.win_smem)  // the served kernel keeps every window on chip
+                        throw McdError(MCD_ERR_INVALID, "request DAG's window does not fit in shared memory");
+                    res->lay = img_layout_of(res->h);
+                    res->bytes = res->lay.total;
+                    if ((int64_t)(res->bytes + rq_layout_of(res->h.E).total) > S->opt.memory_budget)
+                        throw McdError(MCD_ERR_INVALID, "request needs more device memory than the server's budget");
+                    int per_sm = 0;
+                    cuda_check(batch_blocks_per_sm(true, res->h.positive, res->h.tables_in_smem, res->h.n_warps,
+                                                   (size_t)res->h.smem_total, &per_sm),
+                               "occupancy query");
+                    res->per_sm = std::max(1, per_sm);
+                    res->tile_cost = (double)res->h.pred.size() + 2.0 * res->h.E;
+                    const double t_compile = seconds_since(t0);
+                    {
+                        std::unique_lock<std::mutex> lk(S->mu);
+                        S->compile_s += t_compile;
+                        if (!admit(S, lk, res->bytes, st)) throw McdError(MCD_ERR_RUNTIME, "server stopped");
+                        S->resident_bytes += (int64_t)res->bytes;
+                    }
+                    const Clock::time_point t1 = Clock::now();
+                    upload_image(res, st, stage);
+                    HostDag &h = res->h;  // the scalars and the earliest times stay
+                    drop(h.ev);
+                    drop(h.pred);
+                    drop(h.aux);
+                    drop(h.dist);
+                    drop(h.alias);
+                    drop(h.picks);
+                    drop(h.vals);
+                    drop(h.wk_off);
+                    drop(h.stage_meta);
+                    drop(h.link_kd);
+                    drop(h.link_v);
+                    drop(h.link_dv);
+                    drop(h.link_block);
+                    drop(h.link_word);
+                    drop(h.ub);
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    S->upload_s += seconds_since(t1);
+                    res->ready = true;
+                    S->cv_resident.notify_all();
+                } catch (const std::exception &e) {
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    res->failed = true;
+                    res->error = e.what();
+                    for (auto it = S->residents.begin(); it != S->residents.end(); ++it)
+                        if (it->second.get() == res) {
+                            if (res->dimg) {
+                                cudaFreeAsync(res->dimg, st);
+                                res->dimg = nullptr;
+                                S->bytes_in_use -= (int64_t)res->bytes;
+                                S->resident_bytes -= (int64_t)res->bytes;
+                            }
+                            S->residents.erase(it);
+                            break;
+                        }
+                    S->cv_resident.notify_all();
+                    throw;
+                }
+            } else {  // another request's thread compiles or compiled it
+                std::unique_lock<std::mutex> lk(S->mu);
+                S->cv_resident.wait(lk, [&] { return S->stop || res->ready || res->failed; });
+                if (res->failed) throw McdError(MCD_ERR_INVALID, res->error);
+                if (!res->ready) throw McdError(MCD_ERR_RUNTIME, "server stopped");
+            }
             drop(r->earliest);
             drop(r->act_duration);
             drop(r->act_idx);
@@ -324,47 +518,18 @@ void compile_loop(mcd_server *S) {
             drop(r->pred_src);
             drop(r->pred_act);
             drop(r->pred_offsets);
-            if (!r->h.win_smem)  // the served kernel keeps every window on chip
-                throw McdError(MCD_ERR_INVALID, "request DAG's window does not fit in shared memory");
-            r->lay = layout_of(r->h);
+            // this request's own block
+            r->E = res->h.E;
+            r->lay = rq_layout_of(r->E);
             r->bytes = r->lay.total;
-            if ((int64_t)r->bytes > S->opt.memory_budget)
-                throw McdError(MCD_ERR_INVALID, "request needs more device memory than the server's budget");
-            int per_sm = 0;
-            cuda_check(batch_blocks_per_sm(true, r->h.positive, r->h.tables_in_smem, r->h.n_warps,
-                                           (size_t)r->h.smem_total, &per_sm),
-                       "occupancy query");
-            r->per_sm = std::max(1, per_sm);
-            r->tile_cost = (double)r->h.pred.size() + 2.0 * r->h.E;
-            const double t_compile = seconds_since(t0);
             {  // admission: wait until the block fits the budget
                 std::unique_lock<std::mutex> lk(S->mu);
-                S->compile_s += t_compile;
-                S->cv_budget.wait(lk, [&] {
-                    return S->stop || S->bytes_in_use + (int64_t)r->bytes <= S->opt.memory_budget;
-                });
-                if (S->stop) break;
-                S->bytes_in_use += (int64_t)r->bytes;
+                if (!admit(S, lk, r->bytes, st)) break;
                 holds_budget = true;
             }
             const Clock::time_point t1 = Clock::now();
             upload_request(S, r, st, stage);
             request_args(r);
-            HostDag &h = r->h;  // only the scalars stay
-            drop(h.ev);
-            drop(h.pred);
-            drop(h.aux);
-            drop(h.dist);
-            drop(h.alias);
-            drop(h.picks);
-            drop(h.vals);
-            drop(h.wk_off);
-            drop(h.stage_meta);
-            drop(h.link_kd);
-            drop(h.link_v);
-            drop(h.link_dv);
-            drop(h.earliest);
-            drop(h.ub);
             std::lock_guard<std::mutex> lk(S->mu);
             S->upload_s += seconds_since(t1);
             r->state = Q_READY;
@@ -380,6 +545,7 @@ void compile_loop(mcd_server *S) {
                 S->bytes_in_use -= (int64_t)r->bytes;
                 S->cv_budget.notify_all();
             }
+            release_resident(S, r);
             r->error = e.what();
             r->state = Q_FAILED;
             r->t_done = Clock::now();
@@ -401,13 +567,13 @@ void launch_batch(mcd_server *S, Slot &slot, std::vector<Request *> &batch) {
     std::vector<int32_t> order(nb);
     for (size_t i = 0; i < nb; ++i) order[i] = (int32_t)i;
     std::stable_sort(order.begin(), order.end(),
-                     [&](int32_t x, int32_t y) { return batch[x]->tile_cost > batch[y]->tile_cost; });
+                     [&](int32_t x, int32_t y) { return batch[x]->res->tile_cost > batch[y]->res->tile_cost; });
     size_t smem = 0, out_elems = 0, n_items = 0;
     int32_t max_E = 0;
     for (Request *r : batch) {
-        smem = std::max(smem, (size_t)r->h.smem_total);
-        max_E = std::max(max_E, r->h.E);
-        out_elems += (size_t)r->h.E * 5;
+        smem = std::max(smem, (size_t)r->res->h.smem_total);
+        max_E = std::max(max_E, r->E);
+        out_elems += (size_t)r->E * 5;
         n_items += (size_t)((r->n + kTile - 1) / kTile);
     }
     const size_t s_ka = align_up(nb * sizeof(KArgs), 256), s_fa = align_up(nb * sizeof(FArgs), 256),
@@ -461,15 +627,16 @@ void launch_batch(mcd_server *S, Slot &slot, std::vector<Request *> &batch) {
     ba.scratch = nullptr;  // requests keep their window in shared memory (checked at compile)
     ba.scratch_stride = 0;
     ba.smem_bytes = (int32_t)smem;
-    const int32_t nw = batch[0]->h.n_warps;
-    const int grid = batch[0]->per_sm * S->sms;  // the class's CTAs per SM, on every SM
-    cuda_check(launch_batch_stats(ba, true, batch[0]->h.positive, batch[0]->h.tables_in_smem, nw, smem, grid, st),
+    const HostDag &h0 = batch[0]->res->h;
+    const int32_t nw = h0.n_warps;
+    const int grid = batch[0]->res->per_sm * S->sms;  // the class's CTAs per SM, on every SM
+    cuda_check(launch_batch_stats(ba, true, h0.positive, h0.tables_in_smem, nw, smem, grid, st),
                "batch launch");
     cuda_check(launch_batch_finish(reinterpret_cast<const FArgs *>(slot.meta_dev + s_ka), (int32_t)nb, max_E, st),
                "batch finish");
     size_t pos = 0;
     for (Request *r : batch) {
-        const size_t e5 = (size_t)r->h.E * 5;
+        const size_t e5 = (size_t)r->E * 5;
         cuda_check(cudaMemcpyAsync(slot.pinned + pos, r->dblock + r->lay.out, e5 * 8, cudaMemcpyDeviceToHost, st),
                    "results download");
         cuda_check(cudaFreeAsync(r->dblock, st), "request free");
@@ -486,7 +653,7 @@ void complete_slot(mcd_server *S, Slot &slot) {
     size_t pos = 0;
     std::vector<Request *> done = slot.batch;
     for (Request *r : done) {
-        const size_t e5 = (size_t)r->h.E * 5;
+        const size_t e5 = (size_t)r->E * 5;
         r->out.assign(slot.pinned + pos, slot.pinned + pos + e5);
         pos += e5;
     }
@@ -498,6 +665,7 @@ void complete_slot(mcd_server *S, Slot &slot) {
         S->bytes_in_use -= (int64_t)r->bytes;
         S->completed += 1;
         S->running -= 1;
+        release_resident(S, r);
     }
     slot.batch.clear();
     slot.busy = false;
@@ -511,12 +679,13 @@ std::vector<Request *> take_class(mcd_server *S) {
     std::vector<Request *> batch;
     if (S->ready.empty()) return batch;
     const Request *first = S->ready.front();
-    const int32_t nw = first->h.n_warps, per_sm = first->per_sm;
-    const bool positive = first->h.positive, tsmem = first->h.tables_in_smem;
+    const HostDag &h0 = first->res->h;
+    const int32_t nw = h0.n_warps, per_sm = first->res->per_sm;
+    const bool positive = h0.positive, tsmem = h0.tables_in_smem;
     std::deque<Request *> rest;
     for (Request *r : S->ready) {
-        if (r->h.n_warps == nw && r->per_sm == per_sm && r->h.positive == positive &&
-            r->h.tables_in_smem == tsmem &&
+        const HostDag &h = r->res->h;
+        if (h.n_warps == nw && r->res->per_sm == per_sm && h.positive == positive && h.tables_in_smem == tsmem &&
             (S->opt.max_batch <= 0 || (int32_t)batch.size() < S->opt.max_batch))
             batch.push_back(r);
         else
@@ -568,6 +737,7 @@ void schedule_loop(mcd_server *S) {
             S->cv_done.notify_all();
             S->cv_budget.notify_all();
             S->cv_compile.notify_all();
+            S->cv_resident.notify_all();
             return;
         }
     }
@@ -614,6 +784,7 @@ void mcd_server_destroy(mcd_server *S) {
     S->cv_compile.notify_all();
     S->cv_sched.notify_all();
     S->cv_budget.notify_all();
+    S->cv_resident.notify_all();
     if (S->scheduler.joinable()) S->scheduler.join();
     for (std::thread &t : S->compilers)
         if (t.joinable()) t.join();
@@ -629,6 +800,8 @@ void mcd_server_destroy(mcd_server *S) {
     }
     for (auto &kv : S->all)  // uploaded requests that never ran
         if (kv.second->dblock && kv.second->state != Q_RUNNING) cudaFree(kv.second->dblock);
+    for (auto &kv : S->residents)
+        if (kv.second->dimg) cudaFree(kv.second->dimg);
     if (S->zeros) cudaFreeHost(S->zeros);
     delete S;
 }
@@ -692,7 +865,7 @@ int mcd_server_wait(mcd_server *S, int64_t ticket, double wait_ms, const mcd_sta
             return;
         }
         *done = 1;
-        const size_t E = (size_t)r->h.E;
+        const size_t E = (size_t)r->E;
         double *dst[5] = {host ? host->mean : nullptr, host ? host->p50 : nullptr, host ? host->p90 : nullptr,
                           host ? host->p99 : nullptr, host ? host->p_on_time : nullptr};
         for (int k = 0; k < 5; ++k)
@@ -715,6 +888,10 @@ int mcd_server_counters(mcd_server *S, mcd_server_info *info) {
         info->compile_seconds = S->compile_s;
         info->upload_seconds = S->upload_s;
         info->launch_seconds = S->launch_s;
+        info->resident_hits = S->resident_hits;
+        info->resident_dags = (int64_t)S->residents.size();
+        info->resident_bytes = S->resident_bytes;
+        info->evicted = S->evicted;
     });
 }
 

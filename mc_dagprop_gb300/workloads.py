@@ -91,6 +91,71 @@ def layered_dag(seed: int, n_layers: int, width: int, back: int, types, max_dela
     }
 
 
+def layered_dag_fast(rng: np.random.Generator, n_layers: int, width: int, back: int, types, max_delay: float,
+                     max_preds: int = 4) -> dict:
+    """The distribution of ``layered_dag`` (same layers, earliest times, predecessor
+    counts and pools, durations and types), drawn with whole-array operations
+    so that a serving benchmark can build a fresh DAG for every request (about a
+    millisecond for 4,000 events).  Each event's predecessors are a uniform random subset
+    of its pool (Floyd's sampling without replacement, one column per pick)
+    in uniformly random order.  It is another random stream than
+    ``layered_dag``'s: equal in law, not in values."""
+    E = n_layers * width
+    layer = np.repeat(np.arange(n_layers), width)
+    earliest = 60.0 * layer + rng.uniform(0.0, 30.0, E)
+    tl = layer[width:]                                   # layers of the targets (events past layer 0)
+    lo = np.maximum(0, tl - back) * width                # first event of each target's pool
+    pool = tl * width - lo
+    cnt = np.minimum(rng.integers(1, max_preds + 1, len(tl)), pool)
+    k = max_preds
+    pick = np.full((len(tl), k), -1, np.int64)
+    for m in range(k):  # Floyd: for j = pool-cnt .. pool-1, take t in [0, j], or j when t is taken
+        live = m < cnt
+        j = pool - cnt + m
+        t = np.floor(rng.random(len(tl)) * (j + 1)).astype(np.int64)
+        taken = (pick[:, :m] == t[:, None]).any(axis=1)
+        pick[:, m] = np.where(live, np.where(taken, j, t), -1)
+    keys = np.where(pick >= 0, rng.random(pick.shape), 2.0)  # random order, unused slots last
+    pick = np.take_along_axis(pick, np.argsort(keys, axis=1), axis=1)
+    keep = pick >= 0
+    pred_src = (lo[:, None] + pick)[keep].astype(np.int32)
+    P = len(pred_src)
+    target = np.arange(width, E, dtype=np.int32)
+    pred_offsets = np.zeros(len(target) + 1, np.int64)
+    pred_offsets[1:] = np.cumsum(cnt)
+    types = np.asarray(types, np.int32)
+    return {
+        "earliest": earliest,
+        "act_idx": np.arange(P, dtype=np.int32),
+        "act_duration": rng.uniform(30.0, 300.0, P),
+        "act_type": types[rng.integers(0, len(types), P)],
+        "act_src": pred_src.copy(),
+        "act_dst": np.repeat(target, cnt).astype(np.int32),
+        "target": target,
+        "pred_offsets": pred_offsets,
+        "pred_src": pred_src,
+        "pred_act": np.arange(P, dtype=np.int32),
+        "max_delay": float(max_delay),
+    }
+
+
+def fresh_request(rng: np.random.Generator, ev_lo: int = 200, ev_hi: int = 20_000, s_lo: int = 4_096,
+                  s_hi: int = 65_536) -> tuple:
+    """One serving request of the serving configuration: a fresh DAG from the
+    layered generator with events log-uniform in [ev_lo, ev_hi] (layer width
+    log-uniform in 20-200, predecessors from the previous 3 layers), the five
+    delay kinds (their empirical weights drawn anew), max_delay 1,800 s, a
+    sample count log-uniform in [s_lo, s_hi] and a random seed base.
+    Returns (flat, gen, n_samples, seed0)."""
+    ev = int(round(math.exp(rng.uniform(math.log(ev_lo), math.log(ev_hi)))))
+    width = int(round(math.exp(rng.uniform(math.log(20), math.log(200)))))
+    width = max(1, min(width, ev // 2))
+    n_layers = max(2, int(round(ev / width)))
+    flat = layered_dag_fast(rng, n_layers, width, 3, [1, 2, 3, 4, 5], 1800.0)
+    ns = int(round(math.exp(rng.uniform(math.log(s_lo), math.log(s_hi)))))
+    return flat, gen_five_types(rng), ns, int(rng.integers(0, 2**40))
+
+
 def config0(seed: int = 0):
     """1,000 events in 50 layers of 20, predecessors from the previous 1-3 layers,
     types {1: constant 1.5, 2: exponential mean 0.1 d}, max_delay 1800 s;
@@ -112,9 +177,10 @@ def config3(seed: int = 3):
 
 
 def mixed_dags(seed: int, n_dags: int, ev_lo: int, ev_hi: int, s_lo: int, s_hi: int,
-               five_types: bool):
+               five_types: bool, fast: bool = False):
     """A stream of DAGs with log-uniform event counts (layer width log-uniform in
-    20-200) and log-uniform sample counts; each DAG gets its own seed range."""
+    20-200) and log-uniform sample counts; each DAG gets its own seed range.
+    fast: draw each DAG with ``layered_dag_fast`` (the same law, another stream)."""
     rng = np.random.default_rng(seed)
     out = []
     seed_base = 0
@@ -124,20 +190,23 @@ def mixed_dags(seed: int, n_dags: int, ev_lo: int, ev_hi: int, s_lo: int, s_hi: 
         width = max(1, min(width, ev // 2))
         n_layers = max(2, int(round(ev / width)))
         ns = int(round(math.exp(rng.uniform(math.log(s_lo), math.log(s_hi)))))
+        types = [1, 2, 3, 4, 5] if five_types else [1, 2]
+        if fast:
+            flat = layered_dag_fast(np.random.default_rng(seed * 100003 + i), n_layers, width, 3, types, 1800.0)
+        else:
+            flat = layered_dag(seed * 100003 + i, n_layers, width, 3, types, 1800.0)
         if five_types:
-            flat = layered_dag(seed * 100003 + i, n_layers, width, 3, [1, 2, 3, 4, 5], 1800.0)
             gen = gen_five_types(np.random.default_rng(seed * 7919 + i))
         else:
-            flat = layered_dag(seed * 100003 + i, n_layers, width, 3, [1, 2], 1800.0)
             gen = list(GEN_TWO_TYPES)
         out.append((flat, gen, ns, seed_base))
         seed_base += ns
     return out
 
 
-def config2(seed: int = 2, n_dags: int = 512):
+def config2(seed: int = 2, n_dags: int = 512, fast: bool = False):
     """512 DAGs, events log-uniform 100-50,000, samples log-uniform 1,000-100,000."""
-    return mixed_dags(seed, n_dags, 100, 50_000, 1_000, 100_000, five_types=False)
+    return mixed_dags(seed, n_dags, 100, 50_000, 1_000, 100_000, five_types=False, fast=fast)
 
 
 def config4_requests(seed: int = 4, n_requests: int = 120_000):

@@ -221,3 +221,132 @@ def six_event_flat():
              (3, 4): (4, 10.0, 3)}
     prec = [(1, [(0, 0)]), (2, [(1, 1)]), (3, [(1, 2)]), (4, [(2, 3), (3, 4)])]
     return flat_from_lists(earliest, links, prec, 1e6)
+
+
+def event_levels(flat: dict) -> np.ndarray:
+    """Level of every event (longest path from a source) of a DAG whose
+    precedence targets come in topological order (the layered generators')."""
+    lvl = np.zeros(len(flat["earliest"]), np.int64)
+    off, src = flat["pred_offsets"], flat["pred_src"]
+    for k, t in enumerate(flat["target"]):
+        if off[k + 1] > off[k]:
+            lvl[t] = lvl[src[off[k]:off[k + 1]]].max() + 1
+    return lvl
+
+
+def _link_tables(flat: dict, gen: list, L: int):
+    """Per link: base duration, how its d(duration)/d(base) is formed (1: the
+    sampled factor duration / base -- exponential, gamma, relative tables; 2:
+    1 + factor -- constants; 0: 1 -- absolute tables and unmapped types), and the
+    constant factor."""
+    base = np.zeros(L)
+    code = np.zeros(L, np.int8)
+    factor = np.zeros(L)
+    types = {g[1]: g for g in gen}
+    for i, d, t in zip(flat["act_idx"], flat["act_duration"], flat["act_type"]):
+        base[i] = d
+        spec = types.get(int(t), ("none",))
+        if spec[0] in ("exponential", "gamma", "empirical_relative"):
+            code[i] = 1
+        elif spec[0] == "constant":
+            code[i] = 2
+            factor[i] = spec[2]
+    return base, code, factor
+
+
+def chain_gradient(flat: dict, gen: list, real: np.ndarray, dur: np.ndarray, cause: np.ndarray):
+    """CPU pathwise gradient of J = mean_s sum_e (realized - earliest) from the
+    samples' realized times, durations and cause_event (the winning predecessor of
+    the reference's propagation loop, _core.cpp:331-350): a sample's derivative
+    flows back along its winning chain with slope 1 while the winner is not
+    clamped at earliest + max_delay.  Levels are walked from the last to the
+    first, all events of a level at once.  Assumes distinct predecessors per event
+    (the layered generators').  Returns (objective, grad_earliest, grad_base)."""
+    S, E = real.shape
+    L = dur.shape[1]
+    earliest = np.asarray(flat["earliest"], np.float64)
+    ub = earliest + flat["max_delay"]
+    off = np.asarray(flat["pred_offsets"])
+    tgt = np.asarray(flat["target"])
+    ev_of = np.repeat(tgt, np.diff(off))  # the event each precedence entry belongs to
+    src = np.asarray(flat["pred_src"], np.int64)
+    link = np.asarray(flat["pred_act"], np.int64)
+    lvl = event_levels(flat)
+    delayed = real > earliest[None, :]
+    cnt = np.zeros((E, S), np.int64)  # event-major for np.add.at over rows
+    ge = np.zeros(E, np.int64)
+    gl = np.zeros(L)
+    entry_lvl = lvl[ev_of]
+    base, code, factor = _link_tables(flat, gen, L)
+    for lv in range(int(lvl.max()), -1, -1):
+        evs = np.flatnonzero(lvl == lv)
+        c = cnt[evs] + delayed[:, evs].T  # (events of the level, S)
+        ent = np.flatnonzero(entry_lvl == lv)
+        e_ent = ev_of[ent]
+        pos = np.searchsorted(evs, e_ent)  # row of each entry's event in c
+        win = cause[:, e_ent].T == src[ent][:, None]  # (entries, S)
+        valid = link[ent] < L
+        dsum = np.where(valid[:, None], dur[:, np.minimum(link[ent], L - 1)].T, 0.0)
+        clamped = win & (real[:, src[ent]].T + dsum > ub[e_ent][:, None])
+        flow = win & ~clamped
+        won = np.zeros((len(evs), S), bool)
+        np.logical_or.at(won, pos, flow)
+        ge[evs] = np.where(won, 0, c).sum(axis=1) - delayed[:, evs].sum(axis=0)
+        contrib = np.where(flow, c[pos], 0)
+        np.add.at(cnt, src[ent], contrib)
+        ok = valid & flow.any(axis=1)
+        if ok.any():  # d(duration)/d(base) as the GPU records it, in float32
+            lk = link[ent][ok]
+            sampled = (dur[:, lk] / base[lk]).astype(np.float32).astype(np.float64).T
+            fixed = np.where(code[lk] == 2, np.float32(1.0) + factor[lk].astype(np.float32), np.float32(1.0))
+            dfac = np.where((code[lk] == 1)[:, None], sampled, fixed.astype(np.float64)[:, None])
+            np.add.at(gl, lk, (contrib[ok] * dfac).sum(axis=1))
+    obj = (real - earliest[None, :]).sum(axis=1).mean()
+    return obj, ge / S, gl / S
+
+
+def chain_gradient_loop(flat, gen, real, dur, cause):
+    """chain_gradient written event by event (the definition, for small DAGs)."""
+    S, E = real.shape
+    earliest = flat["earliest"]
+    ub = earliest + flat["max_delay"]
+    L = dur.shape[1]
+    base = np.zeros(L)
+    kind = np.zeros(L, dtype=object)
+    types = {g[1]: g for g in gen}
+    for i, d, t in zip(flat["act_idx"], flat["act_duration"], flat["act_type"]):
+        base[i] = d
+        kind[i] = types.get(int(t), ("none",))
+    preds = {}
+    off = flat["pred_offsets"]
+    for k, t in enumerate(flat["target"]):
+        preds[int(t)] = list(zip(flat["pred_src"][off[k]:off[k + 1]], flat["pred_act"][off[k]:off[k + 1]]))
+    cnt = np.zeros((S, E), np.int64)
+    ge = np.zeros(E, np.int64)
+    gl = np.zeros(L)
+    delayed = real > earliest[None, :]
+    for e in range(E - 1, -1, -1):  # layered DAGs: index order is topological
+        c = cnt[:, e] + delayed[:, e]
+        ce = cause[:, e]
+        pl = preds.get(e, [])
+        clamped = np.zeros(S, bool)
+        for src, l in pl:
+            sel = ce == src
+            clamped[sel] = real[sel, src] + dur[sel, l] > ub[e]
+        ge[e] = np.sum(np.where((ce < 0) | clamped, c, 0)) - delayed[:, e].sum()
+        flow = (ce >= 0) & ~clamped
+        for src, l in pl:
+            sel = flow & (ce == src)
+            if not sel.any():
+                continue
+            np.add.at(cnt[:, src], np.nonzero(sel)[0], c[sel])
+            spec = kind[l]
+            if spec[0] in ("exponential", "gamma", "empirical_relative"):
+                dfac = (dur[sel, l] / base[l]).astype(np.float32)
+            elif spec[0] == "constant":
+                dfac = np.float32(1.0 + spec[2])
+            else:
+                dfac = np.float32(1.0)
+            gl[l] += np.sum(c[sel] * np.asarray(dfac, np.float64))
+    obj = (real - earliest[None, :]).sum(axis=1).mean()
+    return obj, ge / S, gl / S

@@ -9,6 +9,11 @@
 2. Against central finite differences with common random numbers (the same
    seeds), step 1e-3 s, on random coordinates: within 1e-3 absolute + 1e-3 relative.
 3. Through the torch.autograd.Function wrapper.
+4. Every memory plan -- all winners kept, level blocks recomputed from window
+   checkpoints, the window off chip (global rows), several sample chunks --
+   gives the same bits.
+5. At the single-large-DAG size (200,000 events, 1,434 levels): against the
+   oracle's chains, between plans, and against central finite differences.
 """
 from __future__ import annotations
 
@@ -19,57 +24,9 @@ import mc_dagprop_gb300 as m
 import oracle
 from mc_dagprop_gb300 import batching
 from mc_dagprop_gb300 import workloads as W
+from mcd_testlib import chain_gradient, chain_gradient_loop
 
 pytestmark = pytest.mark.gpu
-
-
-def cpu_gradient(flat, gen, real, dur, cause):
-    """Backward pass over the samples' winning chains (vectorised over samples)."""
-    S, E = real.shape
-    earliest = flat["earliest"]
-    ub = earliest + flat["max_delay"]
-    L = dur.shape[1]
-    base = np.zeros(L)
-    kind = np.zeros(L, dtype=object)
-    types = {g[1]: g for g in gen}
-    for i, d, t in zip(flat["act_idx"], flat["act_duration"], flat["act_type"]):
-        base[i] = d
-        kind[i] = types.get(int(t), ("none",))
-    preds = {}
-    off = flat["pred_offsets"]
-    for k, t in enumerate(flat["target"]):
-        preds[int(t)] = list(zip(flat["pred_src"][off[k]:off[k + 1]], flat["pred_act"][off[k]:off[k + 1]]))
-    cnt = np.zeros((S, E), np.int64)
-    ge = np.zeros(E, np.int64)
-    gl = np.zeros(L)
-    delayed = real > earliest[None, :]
-    for e in range(E - 1, -1, -1):  # layered DAGs: index order is topological
-        c = cnt[:, e] + delayed[:, e]
-        ce = cause[:, e]
-        pl = preds.get(e, [])
-        clamped = np.zeros(S, bool)
-        link = np.full(S, -1)
-        for src, l in pl:
-            sel = ce == src
-            link[sel] = l
-            clamped[sel] = real[sel, src] + dur[sel, l] > ub[e]
-        ge[e] = np.sum(np.where((ce < 0) | clamped, c, 0)) - delayed[:, e].sum()
-        flow = (ce >= 0) & ~clamped
-        for src, l in pl:
-            sel = flow & (ce == src)
-            if not sel.any():
-                continue
-            np.add.at(cnt[:, src], np.nonzero(sel)[0], c[sel])
-            spec = kind[l]
-            if spec[0] in ("exponential", "gamma", "empirical_relative"):
-                dfac = (dur[sel, l] / base[l]).astype(np.float32)
-            elif spec[0] == "constant":
-                dfac = np.float32(1.0 + spec[2])
-            else:
-                dfac = np.float32(1.0)
-            gl[l] += np.sum(c[sel] * np.asarray(dfac, np.float64))
-    obj = (real - earliest[None, :]).sum(axis=1).mean()
-    return obj, ge / S, gl / S
 
 
 @pytest.mark.parametrize("max_delay", [1800.0, 150.0])
@@ -81,7 +38,7 @@ def test_gradient_matches_cpu_chain(cuda, max_delay):
     g = prop.gradient(n, seed0)
     _, dur, _ = prop.run_many_arrays(np.arange(seed0, seed0 + n, dtype=np.int64))
     real, cause = oracle.OracleSim(flat, gen).propagate_given(dur)  # the reference's chains
-    obj, ge, gl = cpu_gradient(flat, gen, real, dur, cause)
+    obj, ge, gl = chain_gradient_loop(flat, gen, real, dur, cause)
     assert abs(g["objective"] - obj) <= 1e-9 * max(1.0, abs(obj))
     np.testing.assert_array_equal(g["grad_earliest"], ge)
     np.testing.assert_allclose(g["grad_base"], gl, rtol=1e-5, atol=1e-9)
@@ -135,3 +92,100 @@ def test_torch_autograd_wrapper(cuda):
     assert abs(J.item() - g["objective"]) < 1e-12 * max(1, abs(J.item()))
     np.testing.assert_array_equal(e.grad.numpy(), g["grad_earliest"])
     np.testing.assert_array_equal(b.grad.numpy(), g["grad_base"][flat["act_idx"]])
+
+
+def _same_bits(a, b):
+    assert a["objective"] == b["objective"]
+    np.testing.assert_array_equal(a["grad_earliest"], b["grad_earliest"])
+    np.testing.assert_array_equal(a["grad_base"], b["grad_base"])
+
+
+@pytest.mark.parametrize("mode", ["blocks", "chunks_blocks", "offchip", "offchip_blocks"])
+def test_gradient_plans_agree_bitwise(cuda, mode, monkeypatch):
+    flat, gen = W.config1(seed=33, n_layers=40, width=60)
+    n, seed0 = 2000, 99
+    ref = batching.compile_dag(flat, gen).gradient(n, seed0)
+    assert ref["level_blocks"] == 1 and ref["samples_per_chunk"] == 2016
+    if "blocks" in mode:
+        monkeypatch.setenv("MCD_ADJ_BLOCK_EVENTS", "300")
+    if "chunks" in mode:
+        monkeypatch.setenv("MCD_ADJ_BUDGET_MB", "1")
+    if "offchip" in mode:
+        monkeypatch.setenv("MCD_NO_SMEM_WINDOW", "1")
+    prop = batching.compile_dag(flat, gen)
+    assert prop.info()["window_in_smem"] == ("offchip" not in mode)
+    g = prop.gradient(n, seed0)
+    if "blocks" in mode:
+        assert g["level_blocks"] >= 8
+    if "chunks" in mode:
+        assert g["samples_per_chunk"] < 2000
+    _same_bits(g, ref)
+
+
+@pytest.fixture(scope="module")
+def bench_dag_grad():
+    """The single-large-DAG workload (bench.py's DAG) and its gradient over 256 samples."""
+    flat, gen = W.config1(seed=1, n_layers=2000, width=100)
+    prop = batching.compile_dag(flat, gen)
+    assert prop.info()["n_events"] == 200_000 and prop.info()["window_in_smem"]
+    n, seed0 = 256, 4242
+    return flat, gen, prop, n, seed0, prop.gradient(n, seed0)
+
+
+def test_gradient_200k_events_matches_oracle_chain(cuda, bench_dag_grad):
+    flat, gen, prop, n, seed0, g = bench_dag_grad
+    _, dur, _ = prop.run_many_arrays(np.arange(seed0, seed0 + n, dtype=np.int64))
+    real, cause = oracle.OracleSim(flat, gen).propagate_given(dur)
+    obj, ge, gl = chain_gradient(flat, gen, real, dur, cause)
+    assert abs(g["objective"] - obj) <= 1e-9 * abs(obj)
+    np.testing.assert_array_equal(g["grad_earliest"], ge)
+    np.testing.assert_allclose(g["grad_base"], gl, rtol=1e-5, atol=1e-9)
+    assert (ge != 0).sum() > 1000 and (gl != 0).sum() > 1000
+
+
+@pytest.mark.parametrize("mode", ["blocks", "offchip"])
+def test_gradient_200k_events_plans_agree(cuda, bench_dag_grad, mode, monkeypatch):
+    flat, gen, _, n, seed0, ref = bench_dag_grad
+    if mode == "blocks":
+        monkeypatch.setenv("MCD_ADJ_BUDGET_MB", "128")  # the winners of 256 samples need 307 MB
+    else:
+        monkeypatch.setenv("MCD_NO_SMEM_WINDOW", "1")
+    prop = batching.compile_dag(flat, gen)
+    g = prop.gradient(n, seed0)
+    if mode == "blocks":
+        assert g["level_blocks"] > 1 and g["samples_per_chunk"] == 256
+    else:
+        assert not prop.info()["window_in_smem"]
+    _same_bits(g, ref)
+
+
+def test_gradient_200k_events_finite_differences(cuda, bench_dag_grad):
+    """Central differences with common random numbers (step 1e-3 s) of the
+    statistics path's objective, on three event times and three link bases."""
+    flat, gen, prop, _, _, _ = bench_dag_grad
+    n, seed0, h = 4096, 77, 1e-3
+    g = prop.gradient(n, seed0)
+
+    def J(f):
+        st = batching.compile_dag(f, gen).run_stats(n=n, seed0=seed0)
+        return float(np.sum(st["mean"] - f["earliest"]))
+
+    rng = np.random.default_rng(5)
+    ev = rng.choice(np.flatnonzero(g["grad_earliest"] != 0), 3, replace=False)
+    links = rng.choice(np.flatnonzero(g["grad_base"] != 0), 3, replace=False)
+    pos = {int(l): k for k, l in enumerate(flat["act_idx"])}
+    for e in ev:
+        fp, fm = dict(flat), dict(flat)
+        fp["earliest"], fm["earliest"] = flat["earliest"].copy(), flat["earliest"].copy()
+        fp["earliest"][e] += h
+        fm["earliest"][e] -= h
+        fd = (J(fp) - J(fm)) / (2 * h)
+        assert abs(fd - g["grad_earliest"][e]) <= 1e-3 + 1e-3 * abs(fd), (e, fd, g["grad_earliest"][e])
+    for l in links:
+        k = pos[int(l)]
+        fp, fm = dict(flat), dict(flat)
+        fp["act_duration"], fm["act_duration"] = flat["act_duration"].copy(), flat["act_duration"].copy()
+        fp["act_duration"][k] += h
+        fm["act_duration"][k] -= h
+        fd = (J(fp) - J(fm)) / (2 * h)
+        assert abs(fd - g["grad_base"][l]) <= 1e-3 + 1e-3 * abs(fd), (l, fd, g["grad_base"][l])

@@ -53,3 +53,42 @@ def test_server_rejects_bad_request_and_keeps_serving(cuda):
     with pytest.raises(RuntimeError, match="max_delay"):
         server.wait(t_bad, timeout_ms=30_000)
     assert server.wait(t_ok, timeout_ms=30_000) is not None
+
+
+def test_resident_dags_reused_and_evicted(cuda):
+    """A DAG served before stays compiled on the device: its next requests (other
+    seeds, other sample counts) skip the compile and the record upload, and
+    their statistics equal a fresh run alone.  When the budget needs room, idle
+    resident DAGs are evicted and later requests still succeed."""
+    reqs = W.mixed_dags(seed=19, n_dags=6, ev_lo=200, ev_hi=2000, s_lo=256, s_hi=2048, five_types=True)
+    server = m.Server(memory_budget=8 << 30, n_streams=2, n_warps=0, compile_threads=2)
+    first = [_submit(server, f, g, s0, n) for f, g, n, s0 in reqs]
+    for t in first:
+        assert server.wait(t, timeout_ms=60_000) is not None
+    c0 = server.counters()
+    assert c0["resident_dags"] == len(reqs) and c0["resident_hits"] == 0 and c0["resident_bytes"] > 0
+    again = [(f, g, n + 37, s0 + 10_000) for f, g, n, s0 in reqs]
+    tickets = [_submit(server, f, g, s0, n) for f, g, n, s0 in again]
+    got = [server.wait(t, timeout_ms=60_000) for t in tickets]
+    c1 = server.counters()
+    assert c1["resident_hits"] == len(reqs) and c1["resident_dags"] == len(reqs)
+    assert c1["compile_seconds"] == c0["compile_seconds"]  # nothing compiled the second time
+    for (f, g, n, s0), r in zip(again, got):
+        alone = batching.compile_dag(f, g, 8).run_stats(n=n, seed0=s0)
+        for k in ("mean", "p50", "p90", "p99", "p_on_time"):
+            assert np.array_equal(r[k], alone[k]), k
+    # DAGs of about equal size under a budget that holds about two of them:
+    # residents are evicted to make room
+    same = W.mixed_dags(seed=23, n_dags=6, ev_lo=800, ev_hi=800, s_lo=256, s_hi=512, five_types=True)
+    probe = m.Server(memory_budget=8 << 30, n_streams=1, n_warps=0, compile_threads=1)
+    for f, g, n, s0 in same:
+        assert probe.wait(_submit(probe, f, g, s0, n), timeout_ms=60_000) is not None
+    per_dag = probe.counters()["resident_bytes"] / len(same)
+    del probe
+    # a request's own block: per event 8 B of ticks, 8 of sum, 1,040 of histogram, 40 of statistics
+    rq_block = 1100 * max(len(f["earliest"]) for f, _, _, _ in same) + 4096
+    small = m.Server(memory_budget=int(2.5 * per_dag) + rq_block, n_streams=1, n_warps=0, compile_threads=1)
+    for f, g, n, s0 in same + same:
+        assert small.wait(_submit(small, f, g, s0, n), timeout_ms=60_000) is not None
+    cs = small.counters()
+    assert cs["evicted"] > 0 and cs["completed"] == 2 * len(same) and cs["resident_dags"] <= 3

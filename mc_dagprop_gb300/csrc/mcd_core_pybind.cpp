@@ -132,7 +132,7 @@ struct Generator {
 // The device writes results into page-locked host memory at the link's full
 // rate, but pinning memory is slow (about as slow as the copy it speeds up), so
 // blocks are kept when their arrays die and handed to the next call that fits.
-// The pool holds at most a quarter of the machine's memory
+// The pool holds at most an eighth of the machine's memory and 64 GiB
 // ($MCD_PINNED_POOL_MB overrides; 0 turns it off); past that, results go to
 // ordinary (pageable) memory, copied through the device.  The pool lives until
 // the process exits.
@@ -176,7 +176,7 @@ class PinnedPool {
    private:
     PinnedPool() {
         const long pages = sysconf(_SC_PHYS_PAGES), page = sysconf(_SC_PAGE_SIZE);
-        cap_ = pages > 0 && page > 0 ? (size_t)pages * (size_t)page / 4 : 0;
+        cap_ = pages > 0 && page > 0 ? std::min<size_t>((size_t)pages * (size_t)page / 8, 64ull << 30) : 0;
         if (const char *e = std::getenv("MCD_PINNED_POOL_MB")) cap_ = (size_t)std::max(0ll, std::atoll(e)) << 20;
     }
     std::mutex mu_;

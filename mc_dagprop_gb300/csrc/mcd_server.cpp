@@ -113,6 +113,7 @@ struct Resident {
     std::vector<unsigned char> key;  // empty: not shared (malformed arrays)
     uint64_t hash = 0;
     HostDag h;                       // after the upload: the scalars and the earliest times
+    int32_t n_dist = 0, n_alias = 0, n_aux = 0;  // record counts, kept when the records are dropped
     ImgLayout lay{};
     char *dimg = nullptr;
     size_t bytes = 0;
@@ -220,10 +221,10 @@ void request_args(Request *r) {
     a.stage_meta = reinterpret_cast<const int32_t *>(g + I.meta);
     a.n_stages = h.n_stages;
     a.n_warps = h.n_warps;
-    a.n_aux = (int32_t)h.aux.size();
+    a.n_aux = r->res->n_aux;  // the host records themselves are gone after the upload
     a.window_slots = h.window_slots;
-    a.n_dist = (int32_t)h.dist.size();
-    a.n_alias = (int32_t)h.alias.size();
+    a.n_dist = r->res->n_dist;
+    a.n_alias = r->res->n_alias;
     a.tables_in_smem = h.tables_in_smem ? 1 : 0;
     a.win_smem = h.win_smem ? 1 : 0;
     a.positive = h.positive ? 1 : 0;
@@ -466,7 +467,10 @@ void compile_loop(mcd_server *S) {
                     }
                     const Clock::time_point t1 = Clock::now();
                     upload_image(res, st, stage);
-                    HostDag &h = res->h;  // the scalars and the earliest times stay
+                    HostDag &h = res->h;  // the scalars, the record counts and the earliest times stay
+                    res->n_dist = (int32_t)h.dist.size();
+                    res->n_alias = (int32_t)h.alias.size();
+                    res->n_aux = (int32_t)h.aux.size();
                     drop(h.ev);
                     drop(h.pred);
                     drop(h.aux);
@@ -706,9 +710,13 @@ void schedule_loop(mcd_server *S) {
         try {
             bool progressed = false;
             for (Slot &slot : S->slots) {
-                if (slot.busy && cudaEventQuery(slot.done) == cudaSuccess) {
+                if (!slot.busy) continue;
+                const cudaError_t q = cudaEventQuery(slot.done);
+                if (q == cudaSuccess) {
                     complete_slot(S, slot);
                     progressed = true;
+                } else if (q != cudaErrorNotReady) {  // a failed batch: stop and report, never poll forever
+                    cuda_check(q, "batch completion");
                 }
             }
             for (Slot &slot : S->slots) {

@@ -47,7 +47,7 @@
 extern "C" {
 #endif
 
-#define MCD_ABI_VERSION 2
+#define MCD_ABI_VERSION 3
 
 /* Status codes. */
 #define MCD_OK 0
@@ -133,9 +133,14 @@ typedef struct mcd_dag_options {
     int32_t n_warps; /* warps per CTA, 1..24; 0 = chosen from the DAG's level width;
                         MCD_WARPS_BATCH_CLASS = chosen, then rounded up to 2, 4, 8, 12 or 24 */
     int32_t no_cache; /* 0: share the compiled records of a live handle created from
-                         identical inputs (same arrays, generator, n_warps and device);
+                         identical inputs (same arrays, generator, options and device);
                          1: compile a private copy */
+    int32_t window;   /* where the propagation window lives (the realized times later
+                         levels still read): MCD_WINDOW_AUTO in shared memory when it
+                         fits, else global rows; MCD_WINDOW_GLOBAL always global rows */
 } mcd_dag_options;
+#define MCD_WINDOW_AUTO 0
+#define MCD_WINDOW_GLOBAL 1
 int mcd_dag_create_ex(const mcd_dag_desc *desc, const mcd_generator *gen, const mcd_dag_options *opts,
                       mcd_dag **out);
 void mcd_dag_destroy(mcd_dag *dag);

@@ -3,16 +3,22 @@
 A ``Batch`` compiles every DAG with the same number of warps per CTA (the CTA
 size of its persistent launch) and runs all (DAG, 32-sample tile) work items in
 one CUDA graph.  The warps per CTA trade work per stage against barrier and idle
-time: wide DAGs want many warps, narrow ones few (and more CTAs per SM).
+time: wide DAGs want many warps, narrow ones few (and more CTAs per SM); where
+the propagation window lives trades shared memory (fewer CTAs per SM) against
+global-memory reads of predecessor times.
 ``BatchRunner`` therefore splits a mixed stream into width classes -- by the
 warps the compiler would pick for each DAG alone -- and each width class by the
 CTAs per SM its DAGs' shared-memory layouts allow (a launch runs at the
 occupancy of its largest layout, so one wide window would otherwise throttle
 every narrow DAG of the batch).  It runs one batch per class, all launched
 together on their own streams so their CTAs share the SMs.  For each width
-class ``tune_warps`` times candidate warp counts on a calibration subset and
-keeps the fastest; results are cached per shape class in a JSON file
-(``$MCD_AUTOTUNE_CACHE``, default ``~/.cache/mc_dagprop_gb300/autotune.json``).
+class ``tune_class`` times every (warps per CTA, window place) candidate on a
+calibration subset and keeps the fastest; results are cached per shape class in
+a JSON file (``$MCD_AUTOTUNE_CACHE``, default
+``~/.cache/mc_dagprop_gb300/autotune.json``).  Samples per warp (32, one per
+lane) and the work item ((DAG, 32-sample tile): a tile's levels run in order, so
+cutting it into level blocks would not shorten it) are fixed by the kernel's
+design, not tuned.
 """
 from __future__ import annotations
 
@@ -59,11 +65,15 @@ def _levels(flat: dict) -> int:
     return int(level.max()) + 1
 
 
-def compile_dag(flat: dict, gen: list, n_warps: int = 0):
+def compile_dag(flat: dict, gen: list, n_warps: int = 0, window: str = "auto"):
+    """Propagator of a flat DAG (n_warps: warps per CTA, 0 automatic; window:
+    "auto" keeps the propagation window in shared memory when it fits, "global"
+    in global rows)."""
     g = W.to_generator(_core, gen)
     return _core.MonteCarloPropagator.from_arrays(
         flat["earliest"], flat["act_idx"], flat["act_duration"], flat["act_type"], flat["target"],
-        flat["pred_offsets"], flat["pred_src"], flat["pred_act"], flat["max_delay"], g, n_warps=n_warps)
+        flat["pred_offsets"], flat["pred_src"], flat["pred_act"], flat["max_delay"], g, n_warps=n_warps,
+        window=window)
 
 
 def width_class(auto_warps: int) -> int:
@@ -80,11 +90,17 @@ def _time_batch(props, seed0, ns, reps: int = 2) -> float:
     return (time.perf_counter() - t0) / reps
 
 
-def tune_warps(flats: list, gens: list, ns: list, candidates=CANDIDATE_WARPS, sample_cap: int = 4096,
-               subset: int = 48, use_cache: bool = True, widths: list | None = None) -> int:
-    """Warps per CTA for a batch: the fastest candidate on up to `subset` DAGs of
-    the batch (spread over its sizes) with samples capped at `sample_cap`."""
-    key = "w" + "-".join(str(c) for c in candidates) + ":" + shape_class(flats, ns, widths)
+WINDOW_CANDIDATES = ("auto", "global")
+
+
+def tune_class(flats: list, gens: list, ns: list, candidates=CANDIDATE_WARPS, windows=WINDOW_CANDIDATES,
+               sample_cap: int = 4096, subset: int = 48, use_cache: bool = True,
+               widths: list | None = None) -> tuple:
+    """(warps per CTA, window place) for a batch: the fastest candidate pair on up
+    to `subset` DAGs of the batch (spread over its sizes) with samples capped at
+    `sample_cap`.  Returns (n_warps, window, seconds per candidate)."""
+    key = ("w" + "-".join(str(c) for c in candidates) + ":p" + "-".join(windows) + ":" +
+           shape_class(flats, ns, widths))
     path = _cache_path()
     cache = {}
     if use_cache and os.path.exists(path):
@@ -93,24 +109,32 @@ def tune_warps(flats: list, gens: list, ns: list, candidates=CANDIDATE_WARPS, sa
                 cache = json.load(f)
         except (OSError, ValueError):
             cache = {}
-        if key in cache:
-            return int(cache[key]["n_warps"])
+        if key in cache and "window" in cache[key]:
+            return int(cache[key]["n_warps"]), str(cache[key]["window"]), cache[key]["seconds"]
     idx = np.linspace(0, len(flats) - 1, num=min(subset, len(flats))).astype(int)
     cal_ns = [min(int(ns[i]), sample_cap) for i in idx]
     timings = {}
     for nw in candidates:
-        props = [compile_dag(flats[i], gens[i], nw) for i in idx]
-        timings[nw] = _time_batch(props, [0] * len(idx), cal_ns)
+        for win in windows:
+            props = [compile_dag(flats[i], gens[i], nw, win) for i in idx]
+            timings[f"{nw}/{win}"] = _time_batch(props, [0] * len(idx), cal_ns)
     best = min(timings, key=timings.get)
+    nw, win = best.split("/")
     if use_cache:
-        cache[key] = {"n_warps": int(best), "seconds": {str(k): v for k, v in timings.items()}}
+        cache[key] = {"n_warps": int(nw), "window": win, "seconds": timings}
         try:
             os.makedirs(os.path.dirname(path), exist_ok=True)
             with open(path, "w") as f:
                 json.dump(cache, f, indent=1)
         except OSError:
             pass
-    return int(best)
+    return int(nw), win, timings
+
+
+def tune_warps(flats: list, gens: list, ns: list, candidates=CANDIDATE_WARPS, sample_cap: int = 4096,
+               subset: int = 48, use_cache: bool = True, widths: list | None = None) -> int:
+    """Warps per CTA alone (the window where it fits): tune_class over warps."""
+    return tune_class(flats, gens, ns, candidates, ("auto",), sample_cap, subset, use_cache, widths)[0]
 
 
 class BatchRunner:
@@ -123,6 +147,8 @@ class BatchRunner:
         gens = [it[1] for it in items]
         self.ns = [int(it[2]) for it in items]
         self.seed0 = [int(it[3]) for it in items]
+        window = {}         # width class -> window place chosen by the tuner
+        self.tuning = {}    # width class -> seconds per "warps/window" candidate
         if n_warps:
             classes = {n_warps: list(range(len(items)))}
             warps = {n_warps: n_warps}
@@ -136,9 +162,15 @@ class BatchRunner:
             warps = {}
             for c, idx in classes.items():
                 cand = CLASS_CANDIDATES[c]
-                warps[c] = (tune_warps([flats[i] for i in idx], [gens[i] for i in idx], [self.ns[i] for i in idx],
-                                       candidates=cand, use_cache=use_cache, widths=[widths[i] for i in idx])
-                            if tune else c)
+                if tune:
+                    nw, win, secs = tune_class([flats[i] for i in idx], [gens[i] for i in idx],
+                                               [self.ns[i] for i in idx], candidates=cand, use_cache=use_cache,
+                                               widths=[widths[i] for i in idx])
+                    warps[c] = nw
+                    window[c] = win
+                    self.tuning[c] = secs
+                else:
+                    warps[c] = c
         self.props = [None] * len(items)
         self.where = {}
         self.batches = []
@@ -146,7 +178,7 @@ class BatchRunner:
             nw = warps[c]
             groups = {}
             for i in classes[c]:
-                p = compile_dag(flats[i], gens[i], nw)
+                p = compile_dag(flats[i], gens[i], nw, window.get(c, "auto"))
                 self.props[i] = p
                 groups.setdefault(_core.Batch.occupancy(nw, p.info()["smem_bytes"]), []).append(i)
             for per_sm in sorted(groups, reverse=True):
@@ -156,6 +188,8 @@ class BatchRunner:
                 self.batches.append((nw, per_sm, idx, _core.Batch([self.props[i] for i in idx],
                                                                   [self.seed0[i] for i in idx],
                                                                   [self.ns[i] for i in idx])))
+
+        self.window = window
 
     @property
     def classes(self) -> list:

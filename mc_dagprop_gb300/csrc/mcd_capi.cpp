@@ -259,7 +259,7 @@ void put(std::vector<unsigned char> &k, const T &v) {
 // Serializes what compile_dag reads; false (no caching) where the arrays are not
 // well-formed enough to read safely -- compile_dag then reports the error.
 bool image_key(const mcd_dag_desc &d, const mcd_generator &gen, int32_t n_warps, int device,
-               std::vector<unsigned char> &k) {
+               std::vector<unsigned char> &k, int32_t window) {
     if (d.n_events < 0 || d.n_activities < 0 || d.n_targets < 0) return false;
     if ((d.n_events && !d.earliest) ||
         (d.n_activities && (!d.act_idx || !d.act_duration || !d.act_type)) ||
@@ -280,6 +280,7 @@ bool image_key(const mcd_dag_desc &d, const mcd_generator &gen, int32_t n_warps,
     put(k, (int32_t)0x4D434401);  // key format
     put(k, device);
     put(k, n_warps);
+    put(k, window);
     for (const char *var : {"MCD_NO_SMEM_WINDOW", "MCD_WARPS"}) {  // compile_dag's environment overrides
         const char *v = std::getenv(var);
         put(k, (int64_t)(v ? (int64_t)std::strlen(v) : -1));
@@ -488,6 +489,9 @@ int mcd_dag_create_ex(const mcd_dag_desc *desc, const mcd_generator *gen, const 
         const int32_t nw = opts ? opts->n_warps : 0;
         if (nw < kBatchClassWarps || nw > kMaxWarps)
             throw McdError(MCD_ERR_INVALID, "n_warps must be -1 (batch class), 0 (automatic) or 1..24");
+        const int32_t win = opts ? opts->window : MCD_WINDOW_AUTO;
+        if (win != MCD_WINDOW_AUTO && win != MCD_WINDOW_GLOBAL)
+            throw McdError(MCD_ERR_INVALID, "window must be MCD_WINDOW_AUTO (0) or MCD_WINDOW_GLOBAL (1)");
         const bool use_cache = !(opts && opts->no_cache);
         int dev = -1;
         if (cudaGetDevice(&dev) != cudaSuccess) {  // reported after validation, as before
@@ -498,14 +502,14 @@ int mcd_dag_create_ex(const mcd_dag_desc *desc, const mcd_generator *gen, const 
         uint64_t hash = 0;
         std::shared_ptr<const DagImage> img;
         bool hit = false;
-        if (use_cache && dev >= 0 && image_key(*desc, *gen, nw, dev, key)) {
+        if (use_cache && dev >= 0 && image_key(*desc, *gen, nw, dev, key, win)) {
             hash = hash_bytes(key);
             img = cache_find(hash, key);
             hit = img != nullptr;
         }
         if (!img) {
             auto fresh = std::make_shared<DagImage>();
-            compile_dag(*desc, *gen, fresh->h, nw);
+            compile_dag(*desc, *gen, fresh->h, nw, win);
             cuda_check(cudaGetDevice(&fresh->device), "cudaGetDevice");
             upload_image(*fresh);
             if (!key.empty()) fresh->key = std::move(key);

@@ -230,7 +230,7 @@ static void verify_layout(const HostDag &H) {
     }
 }
 
-void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int32_t n_warps) {
+void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int32_t n_warps, int32_t window) {
     // ---- 1) distributions: the last add_* per type wins (README semantics of dist_map_)
     std::unordered_map<int32_t, size_t> type_spec;
     for (size_t i = 0; i < g.dists.size(); ++i) type_spec[g.dists[i].type] = i;
@@ -530,7 +530,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
     const size_t fixed_bytes = (H.tables_in_smem ? table_bytes : 0) + 3 * 128;
     const size_t win_bytes = (size_t)H.window_slots * kTile * sizeof(double);
     H.win_smem = win_bytes <= kMaxWindowBytes && win_bytes + fixed_bytes + 2 * kMinStageBytes <= kSmemMax &&
-                 std::getenv("MCD_NO_SMEM_WINDOW") == nullptr;
+                 window != MCD_WINDOW_GLOBAL && std::getenv("MCD_NO_SMEM_WINDOW") == nullptr;
     const size_t avail = kSmemMax - fixed_bytes - (H.win_smem ? win_bytes : 0);
     size_t budget = std::min(kMaxStageBytes, avail / 2 > 256 ? avail / 2 - 256 : avail / 2);  // room for padding
 

@@ -258,10 +258,10 @@ struct FlatDag {
 
 class Propagator {
    public:
-    Propagator(const FlatDag &f, const Generator &gen, int n_warps = 0) {
+    Propagator(const FlatDag &f, const Generator &gen, int n_warps = 0, int window = MCD_WINDOW_AUTO) {
         mcd_dag *p = nullptr;
         const mcd_dag_desc d = f.desc();
-        const mcd_dag_options opts{n_warps};
+        const mcd_dag_options opts{n_warps, 0, window};
         int rc;
         {
             py::gil_scoped_release release;
@@ -780,7 +780,7 @@ PYBIND11_MODULE(_core, m) {
             "from_arrays",
             [](py::handle earliest, py::handle act_idx, py::handle act_duration, py::handle act_type,
                py::handle target, py::handle pred_offsets, py::handle pred_src, py::handle pred_act,
-               double max_delay, const Generator &g, int n_warps) {
+               double max_delay, const Generator &g, int n_warps, const std::string &window) {
                 FlatDag f;
                 f.earliest = to_vec<double>(earliest);
                 f.act_idx = to_vec<int32_t>(act_idx);
@@ -796,12 +796,15 @@ PYBIND11_MODULE(_core, m) {
                 if (f.pred_offsets.size() != f.target.size() + 1 || f.pred_offsets.front() != 0 ||
                     f.pred_offsets.back() != (int64_t)f.pred_src.size() || f.pred_src.size() != f.pred_act.size())
                     throw py::value_error("inconsistent precedence arrays");
-                return new Propagator(f, g, n_warps);
+                if (window != "auto" && window != "global")
+                    throw py::value_error("window must be 'auto' or 'global'");
+                return new Propagator(f, g, n_warps, window == "global" ? MCD_WINDOW_GLOBAL : MCD_WINDOW_AUTO);
             },
             py::arg("earliest"), py::arg("act_idx"), py::arg("act_duration"), py::arg("act_type"), py::arg("target"),
             py::arg("pred_offsets"), py::arg("pred_src"), py::arg("pred_act"), py::arg("max_delay"),
-            py::arg("generator"), py::arg("n_warps") = 0,
-            "Construct from a DagContext in flat-array form (n_warps: warps per CTA, 0 = automatic)")
+            py::arg("generator"), py::arg("n_warps") = 0, py::arg("window") = "auto",
+            "Construct from a DagContext in flat-array form (n_warps: warps per CTA, 0 = automatic; window: "
+            "'auto' keeps the propagation window in shared memory when it fits, 'global' in global rows)")
         .def("node_count", &Propagator::node_count, "Number of events")
         .def("activity_count", &Propagator::activity_count, "Number of links")
         .def("run", &Propagator::run, py::arg("seed"), "Run single sim")

@@ -101,15 +101,17 @@ StatsParams stats_params(const HostDag &h, int64_t n);
 size_t tables_bytes(const HostDag &h);
 std::vector<unsigned char> tables_block(const HostDag &h);
 
-// n_warps: warps per CTA the kernels will run with (0: chosen from the DAG's width).
-void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &out, int32_t n_warps);
+// n_warps: warps per CTA the kernels will run with (0: chosen from the DAG's width);
+// window: MCD_WINDOW_AUTO (shared memory when it fits) or MCD_WINDOW_GLOBAL.
+void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &out, int32_t n_warps,
+                 int32_t window = MCD_WINDOW_AUTO);
 
 // The content key of a compiled DAG: everything compile_dag reads, serialized
 // (the arrays, the generator, warps per CTA, device, the compiler's environment
 // overrides); false where the arrays are too malformed to read safely.  Caches
 // of compiled DAGs pick a bucket by hash_bytes and decide by full comparison.
 bool image_key(const mcd_dag_desc &d, const mcd_generator &gen, int32_t n_warps, int device,
-               std::vector<unsigned char> &k);
+               std::vector<unsigned char> &k, int32_t window = MCD_WINDOW_AUTO);
 uint64_t hash_bytes(const std::vector<unsigned char> &k);
 int64_t order_key_host(int64_t bits);
 

@@ -32,7 +32,7 @@ class DagInfo(C.Structure):
 
 
 class DagOptions(C.Structure):
-    _fields_ = [("n_warps", C.c_int32), ("no_cache", C.c_int32)]
+    _fields_ = [("n_warps", C.c_int32), ("no_cache", C.c_int32), ("window", C.c_int32)]
 
 
 def header_functions() -> list[str]:

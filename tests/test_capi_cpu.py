@@ -29,7 +29,7 @@ def test_library_exports_every_header_symbol():
 def test_abi_version_and_last_error():
     L = lib()
     L.mcd_abi_version.restype = C.c_int
-    assert L.mcd_abi_version() == 2
+    assert L.mcd_abi_version() == 3
     assert isinstance(last_error(), str)
 
 

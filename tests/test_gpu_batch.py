@@ -80,3 +80,37 @@ def test_batch_many_layouts_per_cta(cuda, nw):
             ref = p.run_stats(n=ns[i], seed0=seed0[i])
             for k in ("mean", "p50", "p90", "p99", "p_on_time"):
                 assert np.array_equal(got[k], ref[k]), (rep, i, k)
+
+
+def test_window_place_option_and_tuner(cuda, tmp_path, monkeypatch):
+    """The window-place compile option: a DAG whose window fits in shared memory
+    compiled with window="global" keeps it in global rows and gives the same
+    statistics (exact); a batch of such DAGs equals their single runs; the
+    autotuner times every (warps, window) pair of a class and the runner uses its
+    choice."""
+    from mc_dagprop_gb300 import batching
+
+    monkeypatch.setenv("MCD_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    dags = W.mixed_dags(seed=27, n_dags=6, ev_lo=100, ev_hi=2000, s_lo=64, s_hi=2000, five_types=True)
+    props = []
+    for flat, gen, n, s0 in dags:
+        a = batching.compile_dag(flat, gen, 8, "auto")
+        g = batching.compile_dag(flat, gen, 8, "global")
+        assert a.info()["window_in_smem"] and not g.info()["window_in_smem"]
+        sa, sg = a.run_stats(n=n, seed0=s0), g.run_stats(n=n, seed0=s0)
+        for k in ("mean", "p50", "p90", "p99", "p_on_time"):
+            np.testing.assert_array_equal(sa[k], sg[k])
+        props.append(g)
+    b = m.Batch(props, [d[3] for d in dags], [d[2] for d in dags])
+    b.run()
+    for i, (flat, gen, n, s0) in enumerate(dags):
+        alone = props[i].run_stats(n=n, seed0=s0)
+        np.testing.assert_array_equal(b.stats(i)["mean"], alone["mean"])
+    runner = batching.BatchRunner([(f, g, n, s0) for f, g, n, s0 in dags], use_cache=True)
+    for c, secs in runner.tuning.items():
+        assert set(secs) == {f"{w}/{p}" for w in batching.CLASS_CANDIDATES[c] for p in ("auto", "global")}
+        assert runner.window[c] in ("auto", "global")
+    runner.run()
+    for i, (flat, gen, n, s0) in enumerate(dags):
+        alone = batching.compile_dag(flat, gen, 8).run_stats(n=n, seed0=s0)
+        np.testing.assert_array_equal(runner.stats(i)["mean"], alone["mean"])

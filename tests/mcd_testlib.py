@@ -350,3 +350,46 @@ def chain_gradient_loop(flat, gen, real, dur, cause):
             gl[l] += np.sum(c[sel] * np.asarray(dfac, np.float64))
     obj = (real - earliest[None, :]).sum(axis=1).mean()
     return obj, ge / S, gl / S
+
+
+def kitchen_sink(seed: int = 3, n_layers: int = 60, width: int = 120, big_table: bool = False):
+    """A layered DAG drawing on every sampler path: constant, truncated
+    exponential, Erlang shapes 1 (truncated: redraws), 2 and 3, Marsaglia-Tsang
+    shapes 2.5 (truncated) and 0.5, empirical tables with per-link duration
+    tables (16 bins) and without them (40 and 300 bins), a type with no
+    distribution; links referenced by two entries, entries past the last link
+    (duration 0) and links no entry references.  big_table: the 300-bin table
+    becomes 5,000 bins (two random words per draw; the tables block then lives
+    in global memory)."""
+    import numpy as np
+
+    from mc_dagprop_gb300 import workloads as W
+
+    rng = np.random.default_rng(seed)
+    flat = W.layered_dag(seed, n_layers, width, 3, list(range(1, 12)), 600.0)
+    P = len(flat["pred_act"])
+    pa = flat["pred_act"].copy()
+    k = np.arange(100, P)
+    dup = k[rng.random(len(k)) < 0.05]
+    pa[dup] = pa[dup - 50]                    # a link read by two entries
+    extra = 20                                # activities no entry references
+    past = np.arange(200, P, 997)
+    pa[past] = P + extra + 100                # past the last link: duration 0
+    flat["pred_act"] = pa.astype(np.int32)
+    flat["act_idx"] = np.arange(P + extra, dtype=np.int32)
+    flat["act_duration"] = np.concatenate([flat["act_duration"], rng.uniform(30.0, 300.0, extra)])
+    flat["act_type"] = np.concatenate([flat["act_type"], rng.integers(1, 12, extra)]).astype(np.int32)
+    nb = 5000 if big_table else 300
+    gen = [
+        ("constant", 1, 0.3),
+        ("exponential", 2, 0.05, 0.2),
+        ("gamma", 3, 2.0, 0.05, float("inf")),
+        ("gamma", 4, 2.5, 0.04, 0.5),
+        ("gamma", 5, 0.5, 0.1, float("inf")),
+        ("gamma", 6, 1.0, 0.1, 0.15),
+        ("gamma", 7, 3.0, 0.02, float("inf")),
+        ("empirical_absolute", 8, np.linspace(0.0, 300.0, 16), rng.dirichlet(np.ones(16))),
+        ("empirical_relative", 9, np.linspace(0.0, 0.8, 40), rng.dirichlet(np.ones(40))),
+        ("empirical_absolute", 10, np.linspace(0.0, 600.0, nb), rng.dirichlet(np.ones(nb))),
+    ]  # type 11: no distribution (fixed at its base)
+    return flat, gen

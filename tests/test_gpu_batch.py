@@ -114,3 +114,28 @@ def test_window_place_option_and_tuner(cuda, tmp_path, monkeypatch):
     for i, (flat, gen, n, s0) in enumerate(dags):
         alone = batching.compile_dag(flat, gen, 8).run_stats(n=n, seed0=s0)
         np.testing.assert_array_equal(runner.stats(i)["mean"], alone["mean"])
+
+
+def test_tuner_choice_holds_on_held_out_dags(cuda):
+    """The (warps per CTA, window place) the tuner picks on calibration DAGs is
+    within 15 % of the fastest candidate timed on a disjoint held-out set of the
+    same width class (every candidate timed on both sets, nothing cached)."""
+    from mc_dagprop_gb300 import batching as B
+
+    dags = W.mixed_dags(seed=41, n_dags=160, ev_lo=200, ev_hi=8000, s_lo=500, s_hi=4000, five_types=True,
+                        fast=True)
+    by_class = {}
+    for flat, gen, n, _ in dags:
+        c = B.width_class(B.compile_dag(flat, gen).info()["n_warps"])
+        by_class.setdefault(c, []).append((flat, gen, n))
+    c, members = max(by_class.items(), key=lambda kv: len(kv[1]))
+    assert len(members) >= 40
+    cal, held = members[0::2], members[1::2]
+    cand = B.CLASS_CANDIDATES[c]
+    nw, win, cal_t = B.tune_class([x[0] for x in cal], [x[1] for x in cal], [x[2] for x in cal], candidates=cand,
+                                  use_cache=False)
+    assert set(cal_t) == {f"{w}/{p}" for w in cand for p in B.WINDOW_CANDIDATES}
+    _, _, held_t = B.tune_class([x[0] for x in held], [x[1] for x in held], [x[2] for x in held], candidates=cand,
+                                use_cache=False)
+    best = min(held_t.values())
+    assert held_t[f"{nw}/{win}"] <= 1.15 * best, (c, nw, win, cal_t, held_t)

@@ -108,19 +108,24 @@ RqLayout rq_layout_of(int32_t E) {
     return L;
 }
 
-// A compiled DAG on the device, shared by the requests for it.
+// A compiled DAG, shared by the requests for it: host records from its compile
+// on, device records from its upload until it is evicted (the host records stay,
+// so a request that waited while it was evicted uploads them again).
 struct Resident {
     std::vector<unsigned char> key;  // empty: not shared (malformed arrays)
     uint64_t hash = 0;
-    HostDag h;                       // after the upload: the scalars and the earliest times
-    int32_t n_dist = 0, n_alias = 0, n_aux = 0;  // record counts, kept when the records are dropped
+    HostDag h;
+    int32_t n_dist = 0, n_alias = 0, n_aux = 0;  // record counts for the kernel arguments
     ImgLayout lay{};
     char *dimg = nullptr;
     size_t bytes = 0;
     int32_t per_sm = 1;              // batch class: (h.n_warps, per_sm)
     double tile_cost = 0;            // work per 32-sample tile, for longest-first ordering
-    int refs = 0;                    // requests holding it (compiling, waiting, uploaded or running)
-    bool ready = false, failed = false;
+    int refs = 0;                    // admitted requests holding it (until their batch completes)
+    bool compiled = false;           // h, lay, bytes, per_sm valid
+    bool uploading = false;          // an admitted request's thread is uploading the records
+    bool on_device = false;          // dimg holds the records
+    bool failed = false;
     std::string error;
     uint64_t last_use = 0;
 };
@@ -337,9 +342,11 @@ void upload_request(const mcd_server *S, Request *r, cudaStream_t st, Staging &s
 }
 
 // Waits (caller holds the lock) until `bytes` more fit the budget, evicting
-// resident DAGs no request holds, least recently used first.  False when the
-// server stops.
-bool admit(mcd_server *S, std::unique_lock<std::mutex> &lk, size_t bytes, cudaStream_t st) {
+// device records of DAGs no admitted request holds (other than `keep`), least
+// recently used first.  False when the server stops.  Every byte of the budget
+// is held by an admitted request (which runs and returns it) or by evictable
+// records, so a request that fits the budget alone is admitted eventually.
+bool admit(mcd_server *S, std::unique_lock<std::mutex> &lk, size_t bytes, cudaStream_t st, const Resident *keep) {
     for (;;) {
         if (S->stop) return false;
         if (S->bytes_in_use + (int64_t)bytes <= S->opt.memory_budget) {
@@ -347,10 +354,12 @@ bool admit(mcd_server *S, std::unique_lock<std::mutex> &lk, size_t bytes, cudaSt
             return true;
         }
         auto lru = S->residents.end();
-        for (auto it = S->residents.begin(); it != S->residents.end(); ++it)
-            if (it->second->ready && it->second->refs == 0 &&
-                (lru == S->residents.end() || it->second->last_use < lru->second->last_use))
+        for (auto it = S->residents.begin(); it != S->residents.end(); ++it) {
+            const Resident *c = it->second.get();
+            if (c != keep && c->on_device && !c->uploading && c->refs == 0 &&
+                (lru == S->residents.end() || c->last_use < lru->second->last_use))
                 lru = it;
+        }
         if (lru == S->residents.end()) {  // nothing to evict: wait for running requests to finish
             S->cv_budget.wait(lk);
             continue;
@@ -359,10 +368,24 @@ bool admit(mcd_server *S, std::unique_lock<std::mutex> &lk, size_t bytes, cudaSt
         S->residents.erase(lru);
         cudaFreeAsync(victim->dimg, st);  // no batch uses it (refs == 0)
         victim->dimg = nullptr;
+        victim->on_device = false;
         S->bytes_in_use -= (int64_t)victim->bytes;
         S->resident_bytes -= (int64_t)victim->bytes;
         S->evicted += 1;
     }
+}
+
+// A DAG whose compile or upload failed (caller holds the lock): unlisted, and
+// every request waiting for it wakes to the error.
+void fail_resident(mcd_server *S, const std::shared_ptr<Resident> &R) {
+    R->failed = true;
+    auto range = S->residents.equal_range(R->hash);
+    for (auto it = range.first; it != range.second; ++it)
+        if (it->second == R) {
+            S->residents.erase(it);
+            break;
+        }
+    S->cv_resident.notify_all();
 }
 
 // Drops a request's hold on its resident DAG (caller holds the lock).
@@ -413,10 +436,14 @@ void compile_loop(mcd_server *S) {
             d.pred_act = r->pred_act.data();
             d.max_delay = r->max_delay;
             const int32_t warps = S->opt.n_warps > 0 ? S->opt.n_warps : kBatchClassWarps;
-            // the resident DAG of this content, or a new one this thread compiles
+            // The compiled DAG of this content (shared with other requests), or a new
+            // one this thread compiles.  No reference is taken yet: a request that
+            // waits for memory holds neither budget nor a resident DAG, so the
+            // requests holding memory are always ones that will run and return it.
             std::vector<unsigned char> key;
             const bool keyed = image_key(d, r->gen, warps, S->device, key);
             const uint64_t hash = keyed ? hash_bytes(key) : 0;
+            std::shared_ptr<Resident> R;
             bool mine = false;
             {
                 std::unique_lock<std::mutex> lk(S->mu);
@@ -424,95 +451,52 @@ void compile_loop(mcd_server *S) {
                     auto range = S->residents.equal_range(hash);
                     for (auto it = range.first; it != range.second; ++it)
                         if (!it->second->failed && it->second->key == key) {
-                            r->res = it->second;
+                            R = it->second;
                             break;
                         }
                 }
-                if (r->res) {
-                    r->res->refs += 1;
-                    S->resident_hits += 1;
-                } else {
-                    r->res = std::make_shared<Resident>();
-                    r->res->hash = hash;
-                    r->res->refs = 1;
-                    if (keyed) {
-                        r->res->key = std::move(key);
-                        S->residents.emplace(hash, r->res);
-                    }
+                if (!R) {
+                    R = std::make_shared<Resident>();
+                    R->hash = hash;
+                    R->key = std::move(key);
+                    S->residents.emplace(hash, R);  // found by later requests (an empty key matches none)
                     mine = true;
                 }
             }
-            Resident *res = r->res.get();
             if (mine) {
                 try {
-                    compile_dag(d, r->gen, res->h, warps);
-                    if (!res->h.win_smem)  // the served kernel keeps every window on chip
+                    compile_dag(d, r->gen, R->h, warps);
+                    if (!R->h.win_smem)  // the served kernel keeps every window on chip
                         throw McdError(MCD_ERR_INVALID, "request DAG's window does not fit in shared memory");
-                    res->lay = img_layout_of(res->h);
-                    res->bytes = res->lay.total;
-                    if ((int64_t)(res->bytes + rq_layout_of(res->h.E).total) > S->opt.memory_budget)
+                    R->lay = img_layout_of(R->h);
+                    R->bytes = R->lay.total;
+                    if ((int64_t)(R->bytes + rq_layout_of(R->h.E).total) > S->opt.memory_budget)
                         throw McdError(MCD_ERR_INVALID, "request needs more device memory than the server's budget");
                     int per_sm = 0;
-                    cuda_check(batch_blocks_per_sm(true, res->h.positive, res->h.tables_in_smem, res->h.n_warps,
-                                                   (size_t)res->h.smem_total, &per_sm),
+                    cuda_check(batch_blocks_per_sm(true, R->h.positive, R->h.tables_in_smem, R->h.n_warps,
+                                                   (size_t)R->h.smem_total, &per_sm),
                                "occupancy query");
-                    res->per_sm = std::max(1, per_sm);
-                    res->tile_cost = (double)res->h.pred.size() + 2.0 * res->h.E;
-                    const double t_compile = seconds_since(t0);
-                    {
-                        std::unique_lock<std::mutex> lk(S->mu);
-                        S->compile_s += t_compile;
-                        if (!admit(S, lk, res->bytes, st)) throw McdError(MCD_ERR_RUNTIME, "server stopped");
-                        S->resident_bytes += (int64_t)res->bytes;
-                    }
-                    const Clock::time_point t1 = Clock::now();
-                    upload_image(res, st, stage);
-                    HostDag &h = res->h;  // the scalars, the record counts and the earliest times stay
-                    res->n_dist = (int32_t)h.dist.size();
-                    res->n_alias = (int32_t)h.alias.size();
-                    res->n_aux = (int32_t)h.aux.size();
-                    drop(h.ev);
-                    drop(h.pred);
-                    drop(h.aux);
-                    drop(h.dist);
-                    drop(h.alias);
-                    drop(h.picks);
-                    drop(h.vals);
-                    drop(h.wk_off);
-                    drop(h.stage_meta);
-                    drop(h.link_kd);
-                    drop(h.link_v);
-                    drop(h.link_dv);
-                    drop(h.link_block);
-                    drop(h.link_word);
-                    drop(h.ub);
+                    R->per_sm = std::max(1, per_sm);
+                    R->tile_cost = (double)R->h.pred.size() + 2.0 * R->h.E;
+                    R->n_dist = (int32_t)R->h.dist.size();
+                    R->n_alias = (int32_t)R->h.alias.size();
+                    R->n_aux = (int32_t)R->h.aux.size();
                     std::lock_guard<std::mutex> lk(S->mu);
-                    S->upload_s += seconds_since(t1);
-                    res->ready = true;
+                    S->compile_s += seconds_since(t0);
+                    R->compiled = true;
                     S->cv_resident.notify_all();
                 } catch (const std::exception &e) {
                     std::lock_guard<std::mutex> lk(S->mu);
-                    res->failed = true;
-                    res->error = e.what();
-                    for (auto it = S->residents.begin(); it != S->residents.end(); ++it)
-                        if (it->second.get() == res) {
-                            if (res->dimg) {
-                                cudaFreeAsync(res->dimg, st);
-                                res->dimg = nullptr;
-                                S->bytes_in_use -= (int64_t)res->bytes;
-                                S->resident_bytes -= (int64_t)res->bytes;
-                            }
-                            S->residents.erase(it);
-                            break;
-                        }
-                    S->cv_resident.notify_all();
+                    R->error = e.what();
+                    fail_resident(S, R);
                     throw;
                 }
             } else {  // another request's thread compiles or compiled it
                 std::unique_lock<std::mutex> lk(S->mu);
-                S->cv_resident.wait(lk, [&] { return S->stop || res->ready || res->failed; });
-                if (res->failed) throw McdError(MCD_ERR_INVALID, res->error);
-                if (!res->ready) throw McdError(MCD_ERR_RUNTIME, "server stopped");
+                S->cv_resident.wait(lk, [&] { return S->stop || R->compiled || R->failed; });
+                if (R->failed) throw McdError(MCD_ERR_INVALID, R->error);
+                if (!R->compiled) break;  // the server stops
+                S->resident_hits += 1;
             }
             drop(r->earliest);
             drop(r->act_duration);
@@ -522,14 +506,72 @@ void compile_loop(mcd_server *S) {
             drop(r->pred_src);
             drop(r->pred_act);
             drop(r->pred_offsets);
-            // this request's own block
-            r->E = res->h.E;
+            // this request's own block, and the DAG's records when they are not on the
+            // device (never uploaded, or evicted while this request waited): admitted
+            // together, and only then is the DAG referenced
+            r->E = R->h.E;
             r->lay = rq_layout_of(r->E);
             r->bytes = r->lay.total;
-            {  // admission: wait until the block fits the budget
+            bool upload_dag = false;
+            {
                 std::unique_lock<std::mutex> lk(S->mu);
-                if (!admit(S, lk, r->bytes, st)) break;
-                holds_budget = true;
+                for (;;) {
+                    if (R->failed) throw McdError(MCD_ERR_INVALID, R->error);
+                    const size_t need = r->bytes + (R->on_device || R->uploading ? 0 : R->bytes);
+                    if (!admit(S, lk, need, st, R.get())) break;
+                    const bool there = R->on_device || R->uploading;
+                    if (R->failed || (!there && need == r->bytes)) {
+                        // it failed, or was evicted, while this request waited: give the room back
+                        S->bytes_in_use -= (int64_t)need;
+                        S->cv_budget.notify_all();
+                        continue;
+                    }
+                    if (there && need > r->bytes) {  // another request uploaded it meanwhile
+                        S->bytes_in_use -= (int64_t)(need - r->bytes);
+                        S->cv_budget.notify_all();
+                    } else if (!there) {  // this thread uploads the records
+                        R->uploading = true;
+                        upload_dag = true;
+                        S->resident_bytes += (int64_t)R->bytes;
+                        bool listed = false;
+                        auto range = S->residents.equal_range(R->hash);
+                        for (auto it = range.first; it != range.second && !listed; ++it) listed = it->second == R;
+                        if (!listed) S->residents.emplace(R->hash, R);
+                    }
+                    R->refs += 1;
+                    r->res = R;
+                    holds_budget = true;
+                    break;
+                }
+                if (!holds_budget) break;  // the server stops
+            }
+            if (upload_dag) {
+                try {
+                    const Clock::time_point t1 = Clock::now();
+                    upload_image(R.get(), st, stage);
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    S->upload_s += seconds_since(t1);
+                    R->uploading = false;
+                    R->on_device = true;
+                    S->cv_resident.notify_all();
+                } catch (const std::exception &e) {
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    R->uploading = false;
+                    S->resident_bytes -= (int64_t)R->bytes;
+                    S->bytes_in_use -= (int64_t)R->bytes;
+                    if (R->dimg) {
+                        cudaFreeAsync(R->dimg, st);
+                        R->dimg = nullptr;
+                    }
+                    R->error = e.what();
+                    fail_resident(S, R);
+                    throw;
+                }
+            } else {  // another request's thread uploads it, or it is there
+                std::unique_lock<std::mutex> lk(S->mu);
+                S->cv_resident.wait(lk, [&] { return S->stop || R->on_device || R->failed; });
+                if (R->failed) throw McdError(MCD_ERR_INVALID, R->error);
+                if (!R->on_device) throw McdError(MCD_ERR_RUNTIME, "server stopped");
             }
             const Clock::time_point t1 = Clock::now();
             upload_request(S, r, st, stage);
@@ -897,7 +939,9 @@ int mcd_server_counters(mcd_server *S, mcd_server_info *info) {
         info->upload_seconds = S->upload_s;
         info->launch_seconds = S->launch_s;
         info->resident_hits = S->resident_hits;
-        info->resident_dags = (int64_t)S->residents.size();
+        int64_t on_device = 0;
+        for (const auto &kv : S->residents) on_device += kv.second->on_device ? 1 : 0;
+        info->resident_dags = on_device;
         info->resident_bytes = S->resident_bytes;
         info->evicted = S->evicted;
     });

@@ -92,3 +92,29 @@ def test_resident_dags_reused_and_evicted(cuda):
         assert small.wait(_submit(small, f, g, s0, n), timeout_ms=60_000) is not None
     cs = small.counters()
     assert cs["evicted"] > 0 and cs["completed"] == 2 * len(same) and cs["resident_dags"] <= 3
+
+
+def test_tight_budget_with_many_compile_threads_makes_progress(cuda):
+    """A budget that holds one DAG and one request block, but not two DAGs and a
+    block, with four compile threads and six distinct DAGs in flight at once:
+    every request completes.  (A request waiting for memory holds neither budget
+    nor a resident DAG; had each thread kept its compiled DAG on the device while
+    waiting for its own block, the DAGs alone would fill the budget and no block
+    would ever fit.)"""
+    same = W.mixed_dags(seed=29, n_dags=6, ev_lo=800, ev_hi=800, s_lo=256, s_hi=512, five_types=True)
+    probe = m.Server(memory_budget=8 << 30, n_streams=1, n_warps=0, compile_threads=1)
+    for f, g, n, s0 in same:
+        assert probe.wait(_submit(probe, f, g, s0, n), timeout_ms=60_000) is not None
+    per_dag = probe.counters()["resident_bytes"] / len(same)
+    del probe
+    rq_block = 1100 * max(len(f["earliest"]) for f, _, _, _ in same) + 4096
+    budget = int(per_dag + rq_block + 0.5 * min(per_dag, rq_block))
+    tight = m.Server(memory_budget=budget, n_streams=2, n_warps=0, compile_threads=4)
+    tickets = [_submit(tight, f, g, s0, n) for f, g, n, s0 in same + same]
+    got = [tight.wait(t, timeout_ms=120_000) for t in tickets]
+    assert all(r is not None for r in got)
+    c = tight.counters()
+    assert c["completed"] == 2 * len(same) and c["evicted"] > 0
+    for (f, g, n, s0), r in zip(same, got[:len(same)]):
+        alone = batching.compile_dag(f, g, 8).run_stats(n=n, seed0=s0)
+        assert np.array_equal(r["mean"], alone["mean"])

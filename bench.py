@@ -423,14 +423,16 @@ def plain_serving(requests, compile_threads):
 
 
 def serving_measure(rate=400.0, duration=10.0, overload_rate=2000.0, overload_duration=2.0, streams=4,
-                    compile_threads=8, plain_requests=300, seed=4):
+                    compile_threads=8, plain_requests=300, seed=4, near_fraction=0.85, near_duration=6.0):
     """Serving workload: fresh DAG per request (events log-uniform 200-20,000,
     samples log-uniform 4,096-65,536, five delay kinds, own seeds), per-event
     mean and p50/p90/p99, 64 GB device budget.  One run at `rate` (below the
     device's capacity, so latency is service latency), one at `overload_rate`
     (the configuration's rate, above capacity: completed throughput is the
-    device's, latency there is queueing), and the plain per-request path on the
-    first `plain_requests` requests with the same compile parallelism."""
+    device's, latency there is queueing), one at `near_fraction` of the request
+    rate that throughput amounts to (the highest rate the server is expected to
+    sustain: latency near capacity), and the plain per-request path on the first
+    `plain_requests` requests with the same compile parallelism."""
     import mc_dagprop_gb300 as m
 
     t0 = time.perf_counter()
@@ -442,6 +444,13 @@ def serving_measure(rate=400.0, duration=10.0, overload_rate=2000.0, overload_du
     out = {"sustained": serve(server, reqs, rate)}
     if over:
         out["overload"] = serve(server, over, overload_rate, seed=8)
+        if near_fraction and near_duration:
+            per_request = float(np.mean([r[2] * r[4] for r in over]))
+            capacity = out["overload"]["value"] / per_request  # requests per second the device completed
+            near_rate = near_fraction * capacity
+            near = make_requests(max(1, int(near_rate * near_duration)), seed + 3)
+            out["near_capacity"] = dict(serve(server, near, near_rate, seed=9), fraction_of_capacity=near_fraction,
+                                        capacity_requests_per_s=capacity)
     c = server.counters()
     del server
     out["plain"] = plain_serving(reqs[:plain_requests], compile_threads)
@@ -864,6 +873,10 @@ def main():
             "sustained": {"rate_per_s": su["rate_per_s"], "requests": su["requests"],
                           "offered_sample_edges_per_s": su["offered_sample_edges_per_s"], "value": su["value"],
                           "latency_ms": su["latency_ms"], "errors": su["errors"]},
+            "near_capacity": None if "near_capacity" not in sv else {
+                k: sv["near_capacity"][k] for k in ("rate_per_s", "fraction_of_capacity", "capacity_requests_per_s",
+                                                    "requests", "offered_sample_edges_per_s", "value",
+                                                    "latency_ms", "errors")},
             "plain_path": sv["plain"]["path"],
             "server": sv["server"]}
 

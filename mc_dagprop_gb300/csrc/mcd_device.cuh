@@ -502,17 +502,47 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int buf, const EvRe
         uint32_t win_code = kAdjNone;  // ADJ: winner position | clamp flag
         float win_dfac = 0.0f;
         const int pb = ev.pred_begin - pred0, pe = ev.pred_end - pred0;
-        for (int p = pb; p < pe; ++p) {
-            const PredRec pr = load_pred(spred + p);
-            double dur;
-            float dfac = 0.0f;
-            if (GIVEN) {
-                dur = (t.active && pr.link >= 0) ? __ldg(at_row(t.dincol, pr.link, t.ld_in8)) : 0.0;
-            } else {
-                dur = link_duration<STAGED, TS>(a, pr.kd, pr.v, pr.dvo, (uint32_t)pr.block, (uint32_t)pr.link, t.seed,
-                                            grp, smem, buf, dfac);
-                if (!STATS && !ADJ && (pr.kd & KD_WRITE) && t.dcol) *at_row(t.dcol, pr.link, t.ld8) = dur;
+        // Given durations come from global memory, each an uncached DRAM read: the
+        // reads of up to four entries are issued together, then the entries are
+        // relaxed in order (one memory latency per four entries, not per entry).
+        for (int p0 = pb; GIVEN && p0 < pe; p0 += 4) {
+            double dg[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                dg[k] = 0.0;
+                if (p0 + k < pe) {
+                    const int32_t link = reinterpret_cast<const int4 *>(spred + p0 + k)->z;  // PredRec::link
+                    if (t.active && link >= 0) dg[k] = __ldg(at_row(t.dincol, link, t.ld_in8));
+                }
             }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (p0 + k >= pe) continue;
+                const PredRec pr = load_pred(spred + p0 + k);
+                const double src = WIN_SMEM ? win[pr.src_slot * kTile + lane]
+                                            : (t.active ? *at_row(t.rcol, pr.src_user, t.rows_ld8) : 0.0);
+                const double tt = src + dg[k];  // the one FP64 add of the edge (_core.cpp:341)
+                long long tb = __double_as_longlong(tt);
+                long long tk = order_key<POSITIVE>(tb);
+                const bool clamp = ub_key < tk;
+                if (clamp) {  // t = std::min(t, ub)
+                    tk = ub_key;
+                    tb = ev.ub_bits;
+                }
+                if (tk >= lk) {  // if (t >= latest) { latest = t; cause = src; }
+                    lk = tk;
+                    lbits = POSITIVE ? tk : tb;
+                    cause = pr.src_user;
+                    if (ADJ) win_code = (uint32_t)(p0 + k - pb) | (clamp ? kAdjClamped : 0u);
+                }
+            }
+        }
+        for (int p = pb; !GIVEN && p < pe; ++p) {
+            const PredRec pr = load_pred(spred + p);
+            float dfac = 0.0f;
+            const double dur = link_duration<STAGED, TS>(a, pr.kd, pr.v, pr.dvo, (uint32_t)pr.block,
+                                                         (uint32_t)pr.link, t.seed, grp, smem, buf, dfac);
+            if (!STATS && !ADJ && (pr.kd & KD_WRITE) && t.dcol) *at_row(t.dcol, pr.link, t.ld8) = dur;
             // with the window on chip every source has a slot (the compiler checks it)
             const double src = WIN_SMEM ? win[pr.src_slot * kTile + lane]
                                         : (t.active ? *at_row(t.rcol, pr.src_user, t.rows_ld8) : 0.0);
@@ -709,7 +739,7 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
 // One CTA per tile of 32 samples.  TS: the tables block's place (kTablesGlobal or
 // kTablesSmem; the host launches the instantiation that matches the DAG).
 template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, int TS>
-__global__ void __launch_bounds__(768) k_propagate(const KArgs a) {
+__global__ void __launch_bounds__(768, 1) k_propagate(const KArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     double *rows = a.realized ? a.realized : a.scratch;  // global realized rows
     if (STATS && WIN_SMEM) rows = nullptr;

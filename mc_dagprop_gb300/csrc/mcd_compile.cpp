@@ -231,7 +231,7 @@ static void verify_layout(const HostDag &H) {
 }
 
 void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int32_t n_warps, int32_t window) {
-    // ---- 1) distributions: the last add_* per type wins (README semantics of dist_map_)
+    // ---- 1) distributions: the last add_* per type wins (dist_map_[t] = ..., _core.cpp:154-158)
     std::unordered_map<int32_t, size_t> type_spec;
     for (size_t i = 0; i < g.dists.size(); ++i) type_spec[g.dists[i].type] = i;
     if (type_spec.count(-1)) throw McdError(MCD_ERR_RUNTIME, "Activity type -1 is reserved for no delay");

@@ -802,6 +802,7 @@ static void stats_device(mcd_dag *g, const int64_t *seeds, int64_t seed0, int64_
         a.acc = acc;
         a.te = te;
         a.hist = hist;
+        a.hist_lane = (int64_t)h.E * kHistStride * 4 <= kHistLaneBytes ? 1 : 0;
         cuda_check(launch_propagate(a, false, h.win_smem, true, st), "statistics launch");
     }
     FArgs f{};
@@ -926,6 +927,7 @@ int mcd_stats_device_noalloc(mcd_dag *g, const int64_t *seeds, int64_t seed0, in
         a.acc = acc;
         a.te = te;
         a.hist = hist;
+        a.hist_lane = (int64_t)h.E * kHistStride * 4 <= kHistLaneBytes ? 1 : 0;
         cuda_check(launch_propagate(a, false, true, true, st), "statistics launch");
         FArgs f{};
         f.acc = acc;

@@ -392,9 +392,10 @@ __device__ __forceinline__ long long warp_sum_ticks(long long d) {
 
 // One event's realized values of the tile into the per-event accumulators:
 // the tile's sum of (realized - earliest) with one 64-bit atomic, and the
-// histogram with one atomic per distinct bin of the warp.  te: the event's
-// earliest in ticks (KArgs::te), loaded when the event started.
-template <bool POSITIVE>
+// histogram with one atomic per lane (LANE_HIST and KArgs::hist_lane) or per
+// distinct bin of the warp.  te: the event's earliest in ticks (KArgs::te),
+// loaded when the event started.
+template <bool POSITIVE, bool LANE_HIST>
 __device__ __forceinline__ void accumulate_stats(const KArgs &a, const EvRec &ev, long long lbits, long long te,
                                                  bool active, unsigned active_mask) {
     int bin;
@@ -413,7 +414,9 @@ __device__ __forceinline__ void accumulate_stats(const KArgs &a, const EvRec &ev
     }
     if (lbits == ev.init_bits) bin = kBinLo;
     else if (lbits == ev.ub_bits) bin = kBinHi;
-    if (active) {
+    if (LANE_HIST && a.hist_lane) {
+        if (active) atomicAdd(&a.hist[(int64_t)ev.user * kHistStride + bin], 1u);
+    } else if (active) {
         const unsigned same = __match_any_sync(active_mask, bin);
         if ((threadIdx.x & 31) == __ffs(same) - 1)
             atomicAdd(&a.hist[(int64_t)ev.user * kHistStride + bin], (unsigned)__popc(same));
@@ -475,7 +478,7 @@ __device__ __forceinline__ int take_next(uint32_t ctr) {
 // stage's first predecessor record (the records' pred_begin/pred_end are
 // global indices); ev0: its first event's compiled index; buf: the staging
 // buffer (0 or 1) that holds the stage.
-template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ, bool STAGED, int TS>
+template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ, bool STAGED, int TS, bool LANE_HIST>
 __device__ __forceinline__ void stage_events(const KArgs &a, int buf, const EvRec *sev, const PredRec *spred, int pred0,
                                              int ev0, int n_ev, uint32_t ctr, const TileCtx &t, unsigned char *smem,
                                              U4 &grp) {
@@ -569,7 +572,7 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int buf, const EvRe
         if (!POSITIVE && ub_key < lk) lbits = ev.ub_bits;
         const double real = __longlong_as_double(lbits);
         if (WIN_SMEM && ev.slot >= 0) win[ev.slot * kTile + lane] = real;
-        if (STATS) accumulate_stats<POSITIVE>(a, ev, lbits, te, t.active, t.active_mask);
+        if (STATS) accumulate_stats<POSITIVE, LANE_HIST>(a, ev, lbits, te, t.active, t.active_mask);
         if (ADJ) {
             const bool delayed = lk > (POSITIVE ? ev.init_bits : ev.init_key);  // realized > earliest
             if (a.adj_flags & kAdjObjective) accumulate_sum<POSITIVE>(a, ev, lbits, te, t.active);
@@ -612,7 +615,8 @@ __device__ __forceinline__ void stage_events(const KArgs &a, int buf, const EvRe
 // this tile (when not null), and saves the window into a.win_ckpt as each of the
 // a.blk_start stages begins -- the checkpoints a level-block recomputation
 // starts from.
-template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ = false, int TS = kTablesEither>
+template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ = false, int TS = kTablesEither,
+          bool LANE_HIST = true>
 __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, double *rows, int64_t rows_ld,
                                                bool rows_tile_local, unsigned char *smem, uint64_t *bars,
                                                bool reuse) {
@@ -711,11 +715,11 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
         const uint32_t ctr = smem_u32(&stage_ctr[j & 1]);
         if (meta.y >= 0) {  // records in the staging buffer (shared memory)
             const unsigned char *buf = smem + a.smem_stage_off + b * a.stage_bytes;
-            stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, true, TS>(
+            stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, true, TS, LANE_HIST>(
                 a, b, reinterpret_cast<const EvRec *>(buf), reinterpret_cast<const PredRec *>(buf + mv.z), meta.z,
                 meta.x, meta.y, ctr, t, smem, grp);
         } else {  // a stage whose records exceed the buffer is read from global memory
-            stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, false, TS>(a, b, a.ev + meta.x, a.pred + meta.z,
+            stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, false, TS, LANE_HIST>(a, b, a.ev + meta.x, a.pred + meta.z,
                                                                        meta.z, meta.x, -meta.y, ctr, t, smem, grp);
         }
         __syncthreads();

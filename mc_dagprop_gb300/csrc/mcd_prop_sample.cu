@@ -39,7 +39,9 @@ __global__ void __launch_bounds__(768, 1) k_batch_stats(const BatchArgs b) {
             continue;
         }
         double *rows = WIN_SMEM ? nullptr : b.scratch + (int64_t)blockIdx.x * b.scratch_stride;
-        const bool ok = propagate_tile<false, WIN_SMEM, true, POSITIVE, false, TSMEM ? kTablesSmem : kTablesGlobal>(
+        // (many DAGs' histogram counters at once: a warp's equal bins added once)
+        const bool ok = propagate_tile<false, WIN_SMEM, true, POSITIVE, false, TSMEM ? kTablesSmem : kTablesGlobal,
+                                       false>(
             a, it.y, rows, WIN_SMEM ? 0 : kTile, true, smem, s_bars, reuse);
         reuse = true;
         if (!ok) return;

@@ -11,8 +11,9 @@
 // predecessor reads never touch HBM; every output row is written once,
 // coalesced (256 B per warp store).
 //
-// FP64 throughput on this part is ~1.6 ops/clk/SM (measured), against ~108 for
-// 32-bit integer logic, so FP64 is spent only where bit-exactness needs it: the
+// FP64 throughput on this part is about 2 lanes per clock per SM (a warp's FP64
+// instruction holds the pipe ~16 SM clocks), against ~108 for 32-bit integer
+// logic, so FP64 is spent only where bit-exactness needs it: the
 // one IEEE add per edge of the reference's loop (_core.cpp:341).  Comparisons
 // run on 64-bit integer order keys that order doubles like the IEEE operators;
 // a sampled duration base * (1 + X) is one FP64 multiply by the double equal to
@@ -93,7 +94,7 @@ __device__ __forceinline__ long long order_key(long long b) {
 // ---------------------------------------------------------------- duration scaling
 // The double equal to a finite float m >= 1, built with integer operations: a
 // float-to-double conversion would occupy the FP64 pipe, which on this part
-// issues about 1.6 lane-operations per clock per SM.
+// issues about 2 lane-operations per clock per SM.
 __device__ __forceinline__ double widen(float m) {
     const uint32_t b = __float_as_uint(m);
     const uint32_t hi = (((b >> 23) + 896u) << 20) | ((b >> 3) & 0x000FFFFFu);

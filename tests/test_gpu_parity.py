@@ -102,10 +102,16 @@ def _edge_flats():
     yield flat_from_lists([0.0, 1.0, 2.0], {(0, 1): (0, 10.0, 1), (1, 2): (1, 10.0, 1)},
                           [(1, [(0, 0)]), (2, [(1, 1)])], math.nan)
     yield W.layered_dag(5, 30, 7, 4, [1, 2], 50.0)
+    # longer predecessor lists (the given-durations kernel reads them four at a
+    # time): up to 11 per event, and one event with 37
+    yield W.layered_dag(6, 20, 12, 3, [1, 2], 80.0, max_preds=11)
+    yield flat_from_lists([0.0] * 38, {(k, 37): (k, 1.0 + k % 3, 1) for k in range(37)},
+                          [(37, [(k, k) for k in range(37)])], 1e6)
 
 
 def test_given_special_values_bitexact(cuda, window_mode):
-    """NaN / +-inf / -0 / negative durations, ties, zero and NaN max_delay."""
+    """NaN / +-inf / -0 / negative durations, ties, zero and NaN max_delay; long
+    predecessor lists."""
     rng = np.random.default_rng(11)
     specials = np.array([math.nan, math.inf, -math.inf, -0.0, 0.0, -5.0, 1e308, 5e-324, 3.0])
     for flat in _edge_flats():

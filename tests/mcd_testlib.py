@@ -352,7 +352,8 @@ def chain_gradient_loop(flat, gen, real, dur, cause):
     return obj, ge / S, gl / S
 
 
-def kitchen_sink(seed: int = 3, n_layers: int = 60, width: int = 120, big_table: bool = False):
+def kitchen_sink(seed: int = 3, n_layers: int = 60, width: int = 120, big_table: bool = False,
+                 max_preds: int = 4):
     """A layered DAG drawing on every sampler path: constant, truncated
     exponential, Erlang shapes 1 (truncated: redraws), 2 and 3, Marsaglia-Tsang
     shapes 2.5 (truncated) and 0.5, empirical tables with per-link duration
@@ -360,13 +361,13 @@ def kitchen_sink(seed: int = 3, n_layers: int = 60, width: int = 120, big_table:
     distribution; links referenced by two entries, entries past the last link
     (duration 0) and links no entry references.  big_table: the 300-bin table
     becomes 5,000 bins (two random words per draw; the tables block then lives
-    in global memory)."""
+    in global memory).  max_preds: predecessors per event, 1 to max_preds."""
     import numpy as np
 
     from mc_dagprop_gb300 import workloads as W
 
     rng = np.random.default_rng(seed)
-    flat = W.layered_dag(seed, n_layers, width, 3, list(range(1, 12)), 600.0)
+    flat = W.layered_dag(seed, n_layers, width, 3, list(range(1, 12)), 600.0, max_preds=max_preds)
     P = len(flat["pred_act"])
     pa = flat["pred_act"].copy()
     k = np.arange(100, P)

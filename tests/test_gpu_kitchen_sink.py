@@ -1,5 +1,6 @@
 """Every sampler path in one DAG (see mcd_testlib.kitchen_sink) through the
-sampled kernel at several CTA widths, window places and time signs: realized
+sampled kernel at several CTA widths, window places, time signs and predecessor
+list lengths (events of up to 12 draw several Philox blocks each): realized
 and cause_event equal the oracle's propagation of the durations the kernel
 reports, bit for bit, and links no entry references get their durations."""
 from __future__ import annotations
@@ -26,10 +27,11 @@ def _bits(a):
     return np.ascontiguousarray(a, dtype=np.float64).view(np.int64)
 
 
-@pytest.mark.parametrize("warps,window,shift,big", [(24, "auto", 0.0, False), (8, "global", 0.0, False),
-                                                    (24, "auto", -500.0, False), (12, "auto", 0.0, True)])
-def test_kitchen_sink_outputs_are_the_oracle_propagation(cuda, warps, window, shift, big):
-    flat, gen = kitchen_sink(seed=5, n_layers=40, width=150, big_table=big)
+@pytest.mark.parametrize("warps,window,shift,big,preds", [(24, "auto", 0.0, False, 4), (8, "global", 0.0, False, 4),
+                                                          (24, "auto", -500.0, False, 4), (12, "auto", 0.0, True, 4),
+                                                          (16, "auto", 0.0, False, 12)])
+def test_kitchen_sink_outputs_are_the_oracle_propagation(cuda, warps, window, shift, big, preds):
+    flat, gen = kitchen_sink(seed=5, n_layers=40, width=150, big_table=big, max_preds=preds)
     flat = dict(flat, earliest=flat["earliest"] + shift)
     prop = _prop(flat, gen, n_warps=warps, window=window)
     info = prop.info()

@@ -3,7 +3,7 @@
 // Requests are (DAG, generator, seed0, n samples) asking for per-event
 // statistics.  submit() copies the inputs and returns a ticket at once.
 //   - A pool of host threads compiles the DAGs (mcd_compile.cpp) with warps per
-//     CTA from each DAG's width (rounded to 2, 4, 8 or 16), waits until the
+//     CTA from each DAG's width (rounded to 2, 4, 8, 12 or 24), waits until the
 //     request's device blocks fit the memory budget, takes them from the
 //     stream-ordered allocator and uploads on its own stream: uploads run in
 //     parallel, off the scheduler.

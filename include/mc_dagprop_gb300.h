@@ -47,7 +47,7 @@
 extern "C" {
 #endif
 
-#define MCD_ABI_VERSION 3
+#define MCD_ABI_VERSION 4
 
 /* Status codes. */
 #define MCD_OK 0
@@ -117,6 +117,10 @@ typedef struct mcd_dag_info {
     int32_t tables_in_smem;    /* 1: distribution tables held in shared memory */
     int32_t cache_hit;         /* 1: the compiled records are shared with an earlier live
                                   handle of identical inputs (compiled-DAG cache) */
+    int32_t n_event_pairs;     /* pairs of events of one level that one warp runs back to
+                                  back, sharing Philox blocks */
+    int64_t block_draws;       /* Philox blocks one sample's propagation draws (first
+                                  attempts; the rows of unreferenced links not counted) */
 } mcd_dag_info;
 
 /* Simulator::Simulator: validates, compiles to level-ordered CSR and uploads to
@@ -154,7 +158,8 @@ int mcd_dag_get_info(const mcd_dag *dag, mcd_dag_info *info);
  * draws come from Philox4x32-10 block block[l] (counter: sample seed, block,
  * attempt); word[l] in 0..3 is the first 32-bit word the link takes from it --
  * one word for exponential and small empirical links, 1-3 words for gamma of
- * shape 1-3, links first referenced by one event sharing blocks of four words --
+ * shape 1-3, links first referenced by one event (or by a pair of events of one
+ * level, run back to back) sharing blocks of four words --
  * and -1 when the link uses the whole block (other gamma shapes, large empirical
  * tables).  Gamma redraws above max_scale use blocks keyed by the link and the
  * attempt.  block[l] = -1 for links of fixed duration. */

@@ -67,8 +67,8 @@ __global__ void __launch_bounds__(768) k_adjoint(const KArgs a) {
             __syncthreads();
             return;
         }
-        const int4 meta = __ldg(reinterpret_cast<const int4 *>(a.stage_meta) + 2 * l);
-        const int pred_boff = __ldg(a.stage_meta + 8 * l + 6);
+        const int4 meta = __ldg(reinterpret_cast<const int4 *>(a.stage_meta + kStageMetaInts * l));
+        const int pred_boff = __ldg(a.stage_meta + kStageMetaInts * l + 6);
         const EvRec *sev = meta.y >= 0 ? reinterpret_cast<const EvRec *>(buf) : a.ev + meta.x;
         const PredRec *spred = meta.y >= 0 ? reinterpret_cast<const PredRec *>(buf + pred_boff)
                                            : a.pred + meta.z;

@@ -565,6 +565,8 @@ static void fill_info(const HostDag &h, mcd_dag_info *info) {
     info->smem_bytes = h.smem_total;
     info->positive = h.positive ? 1 : 0;
     info->tables_in_smem = h.tables_in_smem ? 1 : 0;
+    info->n_event_pairs = h.n_pairs;
+    info->block_draws = h.block_draws;
 }
 
 int mcd_dag_get_info(const mcd_dag *g, mcd_dag_info *info) {

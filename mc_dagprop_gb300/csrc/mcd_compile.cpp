@@ -105,17 +105,19 @@ static void check_table(const DistSpec &d) {
 
 // The invariants every kernel access relies on, checked on the compiled DAG:
 // shared-memory regions in order, aligned and within the budget; staged
-// records within their buffer; warp chunks covering each stage; every source in
-// an earlier stage; and window slots reused only after the stage of the last
-// read of the previous tenant.  A violation is a compiler defect and fails the
-// compile rather than a launch.
+// records within their buffer; warp chunks covering each stage; work units
+// within their stage; every source in an earlier stage; window slots reused only
+// after the stage of the last read of the previous tenant; and every KD_REUSE
+// reference naming the block its work unit drew last.  A violation is a
+// compiler defect and fails the compile rather than a launch.
 static void verify_layout(const HostDag &H) {
     auto fail = [](const char *what) {
         throw McdError(MCD_ERR_RUNTIME, std::string("internal layout check failed: ") + what);
     };
     const int64_t E = H.E, P = (int64_t)H.pred.size(), NW = H.n_warps, NS = H.n_stages;
     if ((int64_t)H.ev.size() != E) fail("event records");
-    if ((int64_t)H.stage_meta.size() != NS * 8 || (int64_t)H.wk_off.size() != NS * NW + 1) fail("stage tables");
+    if ((int64_t)H.stage_meta.size() != NS * kStageMetaInts || (int64_t)H.wk_off.size() != NS * NW + 1)
+        fail("stage tables");
     if (H.picks.size() != H.alias.size()) fail("alias picks");
     // shared memory: [window][stage buffer 0][stage buffer 1][tables][2 mbarriers, 2 stage counters]
     const int64_t win = H.win_smem ? (int64_t)H.window_slots * kTile * (int64_t)sizeof(double) : 0;
@@ -134,10 +136,11 @@ static void verify_layout(const HostDag &H) {
     std::vector<char> seen((size_t)E, 0);
     int64_t ev_next = 0, pred_next = 0, val_next = 0;
     for (int64_t st = 0; st < NS; ++st) {
-        const int32_t *m = &H.stage_meta[(size_t)st * 8];
+        const int32_t *m = &H.stage_meta[(size_t)st * kStageMetaInts];
         const int64_t first = m[0], nev = m[1] >= 0 ? m[1] : -(int64_t)m[1], pfirst = m[2], npred = m[3];
         const int64_t vfirst = m[4], nval = m[5];
         if (first != ev_next || nev <= 0 || first + nev > E || pfirst != pred_next) fail("stage ranges");
+        if (m[8] < 0 || 2 * (int64_t)m[8] > nev || m[9] || m[10] || m[11]) fail("event pairs");
         if (vfirst != val_next || nval < 0 || nval % 2 || vfirst + nval > (int64_t)H.vals.size())
             fail("value region");
         const int64_t pboff = m[6], vboff = m[7];
@@ -170,8 +173,12 @@ static void verify_layout(const HostDag &H) {
     for (int64_t i = 0; i < E; ++i) slot_of[(size_t)H.ev[(size_t)i].user] = H.ev[(size_t)i].slot;
     for (int64_t st = 0, i = 0; st < NS; ++st) {
         const int64_t end = H.wk_off[(size_t)((st + 1) * NW)];
+        const int32_t *sm = &H.stage_meta[(size_t)st * kStageMetaInts];
+        int64_t drawn = -1;  // the block whose words the unit's registers hold (-1: none yet)
         for (; i < end; ++i) {
             const EvRec &r = H.ev[(size_t)i];
+            const int64_t local = i - sm[0];
+            if (!(local < 2 * (int64_t)sm[8] && (local & 1))) drawn = -1;  // a unit starts
             for (int64_t k = r.pred_begin; k < r.pred_end; ++k) {
                 const PredRec &p = H.pred[(size_t)k];
                 if (p.src_user < 0 || p.src_user >= E || stage_of[(size_t)p.src_user] >= st) fail("source order");
@@ -185,12 +192,18 @@ static void verify_layout(const HostDag &H) {
                     const int64_t di = (int64_t)(p.kd >> 8);
                     if (di < 0 || di >= (int64_t)H.dist.size()) fail("distribution index");
                     const DistParam &dp = H.dist[(size_t)di];
+                    if (!(kind == K_GAMMA && !dp.erlang)) {  // draws into the unit's registers
+                        if ((p.kd & KD_REUSE) && p.block != drawn) fail("Philox block reuse");
+                        drawn = p.block;
+                    } else if (p.kd & (KD_REUSE | KD_TWO_WORD)) {
+                        fail("Philox block reuse");
+                    }
                     const bool emp = kind == K_EMP_ABS || kind == K_EMP_REL;
                     if (emp &&
                         (dp.tab_n <= 0 || dp.tab_off < 0 || (int64_t)dp.tab_off + dp.tab_n > (int64_t)H.alias.size()))
                         fail("alias table range");
                     if (emp && dp.link_tab) {
-                        const int32_t *m = &H.stage_meta[(size_t)st * 8];
+                        const int32_t *m = sm;
                         int64_t first;  // the table's first entry in the stage's value region
                         if (m[1] >= 0) {
                             if (p.dvo < 0 || (p.dvo & kVtGlobal) || (p.dvo - m[7]) % (int32_t)sizeof(double))
@@ -518,9 +531,83 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         const DistParam &dp = H.dist[(size_t)(H.link_kd[l] >> 8)];
         return dp.link_tab ? dp.tab_n : 0;
     };
+    auto one_word = [&](int32_t l) {
+        const int kind = H.link_kd[l] & KD_KIND_MASK;
+        return kind == K_EXP || ((kind == K_EMP_ABS || kind == K_EMP_REL) &&
+                                 H.dist[(size_t)(H.link_kd[l] >> 8)].tab_n <= kOneWordBins);
+    };
+    auto link_words = [&](int32_t l) -> int32_t {  // words of a shared block the link's first draw takes
+        if (one_word(l)) return 1;
+        if ((H.link_kd[l] & KD_KIND_MASK) == K_GAMMA) return H.dist[(size_t)(H.link_kd[l] >> 8)].erlang;
+        return 0;
+    };
+    // Words an event's draws take from shared blocks, when all of them do (-1:
+    // some reference draws a block of its own).  Two events of a level whose words
+    // add up to at most four draw one block between them when one warp runs them
+    // back to back (step 8b pairs such events).
+    std::vector<int32_t> ev_words((size_t)E, 0);
+    for (int32_t e = 0; e < E; ++e)
+        for (int64_t k = 0; k < tlen[e] && ev_words[e] >= 0; ++k) {
+            const int32_t l = d.pred_act[tstart[e] + k];
+            if (l >= L || (H.link_kd[l] & KD_KIND_MASK) == K_FIXED) continue;
+            const int32_t w = link_words(l);
+            ev_words[e] = w > 0 ? ev_words[e] + w : -1;
+        }
     std::vector<int64_t> ev_vals((size_t)E, 0);  // value-region entries of an event's references
     for (int32_t e = 0; e < E; ++e)
         for (int64_t k = 0; k < tlen[e]; ++k) ev_vals[e] += table_bins(d.pred_act[tstart[e] + k]);
+    auto ev_bytes = [&](int32_t e) {  // an event's records and value region in a staging buffer
+        return sizeof(EvRec) + (size_t)tlen[e] * sizeof(PredRec) + (size_t)ev_vals[e] * sizeof(double);
+    };
+
+    // ---- 8b) work units, level by level: pairs of events drawing 1-3 words each,
+    // at most four together (3 + 1, 2 + 2, 2 + 1, 1 + 1; each class costliest
+    // first), then the other events.  A level lists its pairs (costliest first)
+    // before its single events (in cost order).  The units depend on the levels
+    // and the delay kinds only -- not on warps per CTA, the window's place or the
+    // staging budget -- so a sample's draws are the same under every layout.  Only
+    // events of at most kMinStageBytes / 4 of records pair up, so a pair always
+    // fits the smallest staging buffer.
+    std::vector<char> pair_first((size_t)E, 0);
+    {
+        std::vector<int32_t> by_w[4], seq;
+        std::vector<std::pair<int32_t, int32_t>> pairs;
+        std::vector<char> paired((size_t)E, 0);
+        for (int32_t l = 0; l < n_levels; ++l) {
+            for (auto &v : by_w) v.clear();
+            for (int32_t k = lvl_off[l]; k < lvl_off[l + 1]; ++k) {
+                const int32_t e = by_level[k];
+                if (ev_words[e] >= 1 && ev_words[e] <= 3 && ev_bytes(e) <= kMinStageBytes / 4)
+                    by_w[ev_words[e]].push_back(e);
+            }
+            size_t at[4] = {0, 0, 0, 0};
+            pairs.clear();
+            auto pair_up = [&](int wa, int wb) {
+                while (at[wa] < by_w[wa].size() && at[wb] + (wa == wb ? 1 : 0) < by_w[wb].size()) {
+                    const int32_t ea = by_w[wa][at[wa]++];
+                    pairs.emplace_back(ea, by_w[wb][at[wb]++]);
+                }
+            };
+            pair_up(3, 1);
+            pair_up(2, 2);
+            pair_up(2, 1);
+            pair_up(1, 1);
+            if (pairs.empty()) continue;
+            std::stable_sort(pairs.begin(), pairs.end(), [&](const auto &x, const auto &y) {
+                return cost[x.first] + cost[x.second] > cost[y.first] + cost[y.second];
+            });
+            seq.clear();
+            for (const auto &pr : pairs) {
+                seq.push_back(pr.first);
+                seq.push_back(pr.second);
+                paired[(size_t)pr.first] = paired[(size_t)pr.second] = 1;
+                pair_first[(size_t)pr.first] = 1;
+            }
+            for (int32_t k = lvl_off[l]; k < lvl_off[l + 1]; ++k)
+                if (!paired[(size_t)by_level[k]]) seq.push_back(by_level[k]);
+            std::copy(seq.begin(), seq.end(), by_level.begin() + lvl_off[l]);
+        }
+    }
 
     // ---- 9) shared-memory budget: window rows, two record staging buffers
     // (each stage's event and predecessor records and value region), distribution tables
@@ -537,7 +624,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
     // ---- 10) stages (a level, or a slice of a wide level that fits a buffer)
     // and per-(stage, warp) chunks balanced by cost
     std::vector<int32_t> order;
-    std::vector<int32_t> meta;  // ev_first, n_ev (negated: unstaged), n_pred, n_val (even)
+    std::vector<int32_t> meta;  // ev_first, n_ev (negated: unstaged), n_pred, n_val (even), offsets, pairs
     std::vector<int32_t> wk;
     for (;;) {
         order.clear();
@@ -547,18 +634,21 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         for (int32_t l = 0; l < n_levels; ++l) {
             int32_t i = lvl_off[l];
             while (i < lvl_off[l + 1]) {
-                // one stage: events i .. j-1 of this level
+                // one stage: events i .. j-1 of this level (a pair is never split)
                 int32_t j = i;
                 size_t bytes = 0, nev = 0, npred = 0, nval = 0;
                 while (j < lvl_off[l + 1]) {
-                    const size_t add = sizeof(EvRec) + (size_t)tlen[by_level[j]] * sizeof(PredRec) +
-                                       (size_t)ev_vals[by_level[j]] * sizeof(double);
+                    const int32_t cnt = pair_first[by_level[j]] ? 2 : 1;
+                    size_t add = 0;
+                    for (int32_t k = j; k < j + cnt; ++k) add += ev_bytes(by_level[k]);
                     if (j > i && bytes + add > budget) break;
                     bytes += add;
-                    nev += 1;
-                    npred += (size_t)tlen[by_level[j]];
-                    nval += (size_t)ev_vals[by_level[j]];
-                    ++j;
+                    for (int32_t k = j; k < j + cnt; ++k) {
+                        nev += 1;
+                        npred += (size_t)tlen[by_level[k]];
+                        nval += (size_t)ev_vals[by_level[k]];
+                    }
+                    j += cnt;
                 }
                 nval = (nval + 1) / 2 * 2;  // 16-byte copies
                 if (nval > (size_t)std::numeric_limits<int32_t>::max() / 2)
@@ -566,6 +656,8 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
                 const bool staged = bytes <= budget;
                 if (staged) max_bytes = std::max(max_bytes, nev * sizeof(EvRec) + npred * sizeof(PredRec) +
                                                                nval * sizeof(double));
+                int32_t n_pairs = 0;
+                for (int32_t k = i; k < j; ++k) n_pairs += pair_first[by_level[k]];
                 double total = 0.0;
                 for (int32_t k = i; k < j; ++k) total += cost[by_level[k]];
                 const int32_t first = (int32_t)order.size();
@@ -573,12 +665,13 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
                 int32_t w = 0;
                 wk.push_back(first);
                 for (int32_t k = i; k < j; ++k) {
-                    const double c = cost[by_level[k]];
+                    const int32_t e = by_level[k];
+                    const double c = cost[e];
                     while (w + 1 < nw && acc + 0.5 * c > total * (double)(w + 1) / (double)nw) {
                         ++w;
                         wk.push_back((int32_t)order.size());
                     }
-                    order.push_back(by_level[k]);
+                    order.push_back(e);
                     acc += c;
                 }
                 while (w + 1 < nw) {
@@ -591,6 +684,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
                 meta.push_back((int32_t)nval);
                 meta.push_back((int32_t)(nev * sizeof(EvRec)));  // 48-byte records: 16-byte aligned offsets
                 meta.push_back((int32_t)(nev * sizeof(EvRec) + npred * sizeof(PredRec)));
+                meta.push_back(n_pairs);
                 i = j;
             }
         }
@@ -599,16 +693,17 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         if (2 * (size_t)H.stage_bytes <= avail || budget <= kMinStageBytes) break;
         budget = std::max(kMinStageBytes, budget * 3 / 4);
     }
-    H.n_stages = (int32_t)(meta.size() / 6);
+    constexpr size_t kMetaPerStage = 7;
+    H.n_stages = (int32_t)(meta.size() / kMetaPerStage);
     H.wk_off = wk;
     // stage_meta with predecessor and value offsets (records and value regions
     // are laid out in compiled order)
-    H.stage_meta.assign((size_t)H.n_stages * 8, 0);
+    H.stage_meta.assign((size_t)H.n_stages * kStageMetaInts, 0);
     {
         int64_t pos = 0, vpos = 0;
         for (int32_t st = 0; st < H.n_stages; ++st) {
-            int32_t *m = &H.stage_meta[(size_t)st * 8];
-            const int32_t *q = &meta[(size_t)st * 6];
+            int32_t *m = &H.stage_meta[(size_t)st * kStageMetaInts];
+            const int32_t *q = &meta[(size_t)st * kMetaPerStage];
             m[0] = q[0];
             m[1] = q[1];
             m[2] = (int32_t)pos;
@@ -619,6 +714,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
             m[5] = q[3];
             m[6] = q[4];
             m[7] = q[5];
+            m[8] = q[6];
             pos += q[2];
             vpos += q[3];
         }
@@ -645,17 +741,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
     H.pred.reserve((size_t)(d.n_targets > 0 ? d.pred_offsets[d.n_targets] : 0));
     std::vector<char> referenced((size_t)L, 0), written((size_t)L, 0);
     // Philox blocks (see KD_REUSE): links drawing from a shared block group per
-    // event, up to four words a block; the rest own one
-    auto one_word = [&](int32_t l) {
-        const int kind = H.link_kd[l] & KD_KIND_MASK;
-        return kind == K_EXP || ((kind == K_EMP_ABS || kind == K_EMP_REL) &&
-                                 H.dist[(size_t)(H.link_kd[l] >> 8)].tab_n <= kOneWordBins);
-    };
-    auto link_words = [&](int32_t l) -> int32_t {  // words of a shared block the link's first draw takes
-        if (one_word(l)) return 1;
-        if ((H.link_kd[l] & KD_KIND_MASK) == K_GAMMA) return H.dist[(size_t)(H.link_kd[l] >> 8)].erlang;
-        return 0;
-    };
+    // work unit, up to four words a block; the rest own one
     H.link_block.assign((size_t)L, -1);
     H.link_word.assign((size_t)L, -1);
     H.earliest.assign(d.earliest, d.earliest + E);
@@ -675,19 +761,30 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
     int64_t st_end = 0, vbase = 0;
     auto close_stage = [&]() {  // pad the stage's value region to its recorded (even) size
         if (st_cur < 0) return;
-        const int32_t *m = &H.stage_meta[(size_t)st_cur * 8];
+        const int32_t *m = &H.stage_meta[(size_t)st_cur * kStageMetaInts];
         if ((int64_t)H.vals.size() - vbase > m[5]) throw McdError(MCD_ERR_RUNTIME, "value region overflow");
         while ((int64_t)H.vals.size() < vbase + m[5]) H.vals.push_back(0.0);
     };
+    int32_t group = -1, group_n = 0;  // the work unit's open Philox block of one-word links
+    int32_t last_block = -1;          // block its last non-gamma random reference drew (in registers)
     for (int32_t i = 0; i < E; ++i) {
         const int32_t e = order[i];
         while (i >= st_end) {  // the first event of the next stage
             close_stage();
             ++st_cur;
-            const int32_t *m = &H.stage_meta[(size_t)st_cur * 8];
+            const int32_t *m = &H.stage_meta[(size_t)st_cur * kStageMetaInts];
             st_end = (int64_t)m[0] + (m[1] >= 0 ? m[1] : -(int64_t)m[1]);
             vbase = (int64_t)H.vals.size();
             if (vbase != m[4]) throw McdError(MCD_ERR_RUNTIME, "value region offset");
+        }
+        {  // the second event of a pair continues its unit's block; any other event starts a unit
+            const int32_t *m = &H.stage_meta[(size_t)st_cur * kStageMetaInts];
+            const int64_t local = (int64_t)i - m[0];
+            if (!(local < 2 * (int64_t)m[8] && (local & 1))) {
+                group = -1;
+                group_n = 0;
+                last_block = -1;
+            }
         }
         EvRec r{};
         r.user = e;
@@ -699,8 +796,6 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         r.init_key = std::isnan(earliest) ? std::numeric_limits<int64_t>::max() : order_key_host(r.init_bits);
         r.ub_bits = bits_of(ub);
         r.ub_key = std::isnan(ub) ? std::numeric_limits<int64_t>::max() : order_key_host(r.ub_bits);
-        int32_t group = -1, group_n = 0;  // this event's open Philox block of one-word links
-        int32_t last_block = -1;          // block its last non-gamma random reference drew (in registers)
         for (int64_t k = 0; k < tlen[e]; ++k) {
             const int32_t src = d.pred_src[tstart[e] + k];
             const int32_t l = d.pred_act[tstart[e] + k];
@@ -751,7 +846,7 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
                     const int32_t di = H.link_kd[l] >> 8;
                     const bool rel = (H.link_kd[l] & KD_KIND_MASK) == K_EMP_REL;
                     const double base = H.link_v[l];
-                    const int32_t *sm = &H.stage_meta[(size_t)st_cur * 8];
+                    const int32_t *sm = &H.stage_meta[(size_t)st_cur * kStageMetaInts];
                     const int64_t local = (int64_t)H.vals.size() - vbase;
                     if (sm[1] >= 0) p.dvo = (int32_t)(sm[7] + local * (int64_t)sizeof(double));  // staged: byte offset
                     else p.dvo = kVtGlobal | (int32_t)(vbase + local);                           // index in vals
@@ -797,6 +892,12 @@ void compile_dag(const mcd_dag_desc &d, const mcd_generator &g, HostDag &H, int3
         }
         H.aux.push_back(LinkRec{l, kd, H.link_v[l]});
     }
+    // what the work units save: Philox blocks a sample's propagation draws
+    H.n_pairs = 0;
+    for (int32_t st = 0; st < H.n_stages; ++st) H.n_pairs += H.stage_meta[(size_t)st * kStageMetaInts + 8];
+    H.block_draws = 0;
+    for (const PredRec &p : H.pred)
+        if ((p.kd & KD_KIND_MASK) != K_FIXED && !(p.kd & KD_REUSE)) ++H.block_draws;
     verify_layout(H);
 }
 

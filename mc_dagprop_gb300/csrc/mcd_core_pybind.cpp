@@ -450,6 +450,8 @@ class Propagator {
         d["positive"] = (bool)i.positive;
         d["tables_in_smem"] = (bool)i.tables_in_smem;
         d["cache_hit"] = (bool)i.cache_hit;
+        d["n_event_pairs"] = i.n_event_pairs;
+        d["block_draws"] = i.block_draws;
         return d;
     }
     mcd_dag *handle() const { return dag_.get(); }

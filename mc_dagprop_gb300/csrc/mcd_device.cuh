@@ -343,7 +343,7 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 // stay in step.  A value region holds an even number of doubles (16-byte sizes
 // and offsets).
 __device__ __forceinline__ void stage_issue(const KArgs &a, int stage, char *buf, uint64_t *bar) {
-    const int4 *meta = reinterpret_cast<const int4 *>(a.stage_meta) + 2 * stage;
+    const int4 *meta = reinterpret_cast<const int4 *>(a.stage_meta + kStageMetaInts * stage);
     const int4 m = __ldg(meta);       // ev_first, n_ev, pred_first, n_pred
     const int4 mv = __ldg(meta + 1);  // val_first, n_val, byte offsets of predecessor records and values
     const bool staged = m.y >= 0;
@@ -473,26 +473,39 @@ __device__ __forceinline__ int take_next(uint32_t ctr) {
     return v;
 }
 
-// One stage's events, taken one at a time from the stage's counter (the
-// compiler orders them costliest first).  STAGED: sev/spred point into the
-// staging buffer in shared memory; otherwise into global memory.  pred0: the
-// stage's first predecessor record (the records' pred_begin/pred_end are
-// global indices); ev0: its first event's compiled index; buf: the staging
-// buffer (0 or 1) that holds the stage.
+// One stage's work units, taken one at a time from the stage's counter: unit
+// u < n_pair is the pair of events 2u and 2u + 1, run back to back so that the
+// second continues the first's Philox block (grp); unit u >= n_pair is event
+// u + n_pair alone (the compiler orders the pairs, then the single events,
+// costliest first).  STAGED:
+// sev/spred point into the staging buffer in shared memory; otherwise into
+// global memory.  pred0: the stage's first predecessor record (the records'
+// pred_begin/pred_end are global indices); ev0: its first event's compiled
+// index; buf: the staging buffer (0 or 1) that holds the stage.
 template <bool GIVEN, bool WIN_SMEM, bool STATS, bool POSITIVE, bool ADJ, bool STAGED, int TS, bool LANE_HIST>
 __device__ __forceinline__ void stage_events(const KArgs &a, int buf, const EvRec *sev, const PredRec *spred, int pred0,
-                                             int ev0, int n_ev, uint32_t ctr, const TileCtx &t, unsigned char *smem,
-                                             U4 &grp) {
+                                             int ev0, int n_ev, int n_pair, uint32_t ctr, const TileCtx &t,
+                                             unsigned char *smem, U4 &grp) {
     double *win = reinterpret_cast<double *>(smem);
     const int lane = t.lane;
-    // the next index is taken before this event's work, hiding the atomic's
-    // latency (a warp holds at most one extra event: the cheapest, by order)
+    // The warp's next event: the second of the current pair, or the first event of
+    // the next unit, which lane 0 takes before this event's work, hiding the
+    // atomic's latency (a warp holds at most one extra unit: the cheapest, by
+    // order).  Units past the last map to events past n_ev.
     int i_next = 0;
-    if (lane == 0) i_next = take_next(ctr);
+    if (lane == 0) {
+        const int u = take_next(ctr);
+        i_next = u < n_pair ? 2 * u : u + n_pair;
+    }
     i_next = __shfl_sync(0xFFFFFFFFu, i_next, 0);
     while (i_next < n_ev) {
         const int i = i_next;
-        if (lane == 0) i_next = take_next(ctr);
+        if (i < 2 * n_pair && !(i & 1)) {
+            i_next = i + 1;
+        } else if (lane == 0) {
+            const int u = take_next(ctr);
+            i_next = u < n_pair ? 2 * u : u + n_pair;
+        }
         const EvRec ev = load_ev(sev + i);
         // the event's earliest in ticks, needed after its predecessors (the load's
         // latency hides behind them)
@@ -684,16 +697,21 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
     // a stage's metadata is loaded one stage ahead: its latency then hides behind
     // the previous stage's events instead of stalling every warp at the stage start
     const int4 *smeta = reinterpret_cast<const int4 *>(a.stage_meta);
+    constexpr int kMetaVecs = kStageMetaInts / 4;
     int4 meta_next = make_int4(0, 0, 0, 0), mv_next = make_int4(0, 0, 0, 0);
+    int pairs_next = 0;
     if (s_begin < s_end) {
-        meta_next = __ldg(smeta + 2 * s_begin);
-        mv_next = __ldg(smeta + 2 * s_begin + 1);
+        meta_next = __ldg(smeta + kMetaVecs * s_begin);
+        mv_next = __ldg(smeta + kMetaVecs * s_begin + 1);
+        pairs_next = __ldg(a.stage_meta + kStageMetaInts * s_begin + 8);
     }
     for (int l = s_begin; l < s_end; ++l) {
         const int4 meta = meta_next, mv = mv_next;
+        const int n_pair = pairs_next;
         if (l + 1 < s_end) {
-            meta_next = __ldg(smeta + 2 * (l + 1));
-            mv_next = __ldg(smeta + 2 * (l + 1) + 1);
+            meta_next = __ldg(smeta + kMetaVecs * (l + 1));
+            mv_next = __ldg(smeta + kMetaVecs * (l + 1) + 1);
+            pairs_next = __ldg(a.stage_meta + kStageMetaInts * (l + 1) + 8);
         }
         const int j = l - s_begin;  // stages run so far: buffer, barrier phase and counter
         const int b = j & 1;
@@ -718,10 +736,10 @@ __device__ __forceinline__ bool propagate_tile(const KArgs &a, int64_t tile, dou
             const unsigned char *buf = smem + a.smem_stage_off + b * a.stage_bytes;
             stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, true, TS, LANE_HIST>(
                 a, b, reinterpret_cast<const EvRec *>(buf), reinterpret_cast<const PredRec *>(buf + mv.z), meta.z,
-                meta.x, meta.y, ctr, t, smem, grp);
+                meta.x, meta.y, n_pair, ctr, t, smem, grp);
         } else {  // a stage whose records exceed the buffer is read from global memory
-            stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, false, TS, LANE_HIST>(a, b, a.ev + meta.x, a.pred + meta.z,
-                                                                       meta.z, meta.x, -meta.y, ctr, t, smem, grp);
+            stage_events<GIVEN, WIN_SMEM, STATS, POSITIVE, ADJ, false, TS, LANE_HIST>(
+                a, b, a.ev + meta.x, a.pred + meta.z, meta.z, meta.x, -meta.y, n_pair, ctr, t, smem, grp);
         }
         __syncthreads();
         if (threadIdx.x == 0 && l + 2 < s_end)

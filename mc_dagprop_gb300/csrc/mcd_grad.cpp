@@ -46,7 +46,7 @@ struct AdjPlan {
 
 // Events of stage st (a stage read from global memory stores its count negated).
 int64_t stage_events(const HostDag &h, int32_t st) {
-    const int32_t n = h.stage_meta[(size_t)st * 8 + 1];
+    const int32_t n = h.stage_meta[(size_t)st * kStageMetaInts + 1];
     return n >= 0 ? n : -(int64_t)n;
 }
 
@@ -219,7 +219,7 @@ extern "C" int mcd_gradient_host(mcd_dag *g, int64_t seed0, int64_t n, double *o
                 KArgs r = a;
                 r.stage_begin = plan.blk[k];
                 r.stage_end = plan.blk[k + 1];
-                r.code_base = h.stage_meta[(size_t)plan.blk[k] * 8];  // compiled index of the block's first event
+                r.code_base = h.stage_meta[(size_t)plan.blk[k] * kStageMetaInts];  // compiled index of the block's first event
                 r.adj_code = code;
                 r.adj_flags = 0;
                 r.win_in = (h.win_smem && k > 0) ? wck + (k - 1) * tiles * win_n : nullptr;

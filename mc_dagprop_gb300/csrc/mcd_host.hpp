@@ -62,11 +62,13 @@ struct HostDag {
     bool tables_in_smem = true;
     int32_t n_stages = 0, stage_bytes = 0;
     int32_t smem_stage_off = 0, smem_tables_off = 0, smem_bar_off = 0, smem_total = 0;
-    std::vector<int32_t> stage_meta;  // 8 ints per stage (KArgs::stage_meta)
+    std::vector<int32_t> stage_meta;  // kStageMetaInts ints per stage (KArgs::stage_meta)
     std::vector<EvRec> ev;
     std::vector<PredRec> pred;
     std::vector<LinkRec> aux;  // links stored by the aux pass
     int32_t n_orphan = 0;      // sampled links no precedence entry references
+    int32_t n_pairs = 0;       // event pairs over all stages (KArgs::stage_meta)
+    int64_t block_draws = 0;   // Philox blocks a sample draws on first attempts
     std::vector<DistParam> dist;
     std::vector<AliasEntry> alias;
     std::vector<AliasPick> picks;  // parallel to alias

@@ -38,14 +38,16 @@ enum Kind : int32_t { K_FIXED = 0, K_EXP = 1, K_GAMMA = 2, K_EMP_ABS = 3, K_EMP_
 // Packed kind word of a link reference:
 //   kind | word << KD_WORD_SHIFT | KD_REUSE | KD_TWO_WORD | KD_WRITE | dist << 8.
 // Random words: a link draws from the Philox block `block` of its PredRec.
-// Links first referenced by the same event share blocks of four words: one-word
-// links (exponential; empirical tables of at most kOneWordBins bins) take one
-// word, gamma links of shape 1, 2 or 3 (sum of exponentials) take that many
-// words for their first attempt; `word` is the first of them.  KD_REUSE marks a
-// reference whose block the event's previous reference of these kinds already
-// drew (the words are still in registers).  Other gamma links and larger
-// empirical tables (KD_TWO_WORD) own their block.  KD_WRITE marks the one reference of a link that stores its duration
-// row; links no precedence entry references are stored by the aux-link pass.
+// Links first referenced by the same work unit (one event, or a pair of events
+// of one stage that one warp runs back to back) share blocks of four words:
+// one-word links (exponential; empirical tables of at most kOneWordBins bins)
+// take one word, gamma links of shape 1, 2 or 3 (sum of exponentials) take that
+// many words for their first attempt; `word` is the first of them.  KD_REUSE
+// marks a reference whose block the unit's previous reference of these kinds
+// already drew (the words are still in registers).  Other gamma links and
+// larger empirical tables (KD_TWO_WORD) own their block.  KD_WRITE marks the one
+// reference of a link that stores its duration row; links no precedence entry
+// references are stored by the aux-link pass.
 constexpr int32_t KD_KIND_MASK = 0x07;
 constexpr int KD_WORD_SHIFT = 3;  // bits 3-4
 constexpr int32_t KD_REUSE = 0x20;
@@ -160,6 +162,12 @@ constexpr int kHistStride = 260;
 // bins are added once.
 constexpr int64_t kHistLaneBytes = 48ll << 20;
 
+// Ints of stage metadata per stage (three int4 loads).  A stage's first
+// 2 * pairs events form pairs (events 2u and 2u + 1 are one work unit: one warp
+// runs them back to back and they share Philox blocks); each later event is a
+// unit of its own.
+constexpr int kStageMetaInts = 12;
+
 // Arguments of the propagation kernels.
 struct KArgs {
     const EvRec *ev;
@@ -167,9 +175,9 @@ struct KArgs {
     const LinkRec *aux;
     const DistParam *dist;    // tables block: DistParam[n_dist], AliasEntry[n_alias], AliasPick[n_alias]
     const int32_t *wk_off;    // [n_stages * n_warps + 1] event chunk per (stage, warp), compiled indices
-    const int32_t *stage_meta;  // [n_stages][8] {first event, events (negated: read from global), first pred, preds,
-                                //  first value, values, byte offsets of the predecessor records and of the
-                                //  value region inside a staging buffer}
+    const int32_t *stage_meta;  // [n_stages][kStageMetaInts] {first event, events (negated: read from global),
+                                //  first pred, preds, first value, values, byte offsets of the predecessor
+                                //  records and of the value region inside a staging buffer, event pairs, 0, 0, 0}
     const double *vals;         // per-link duration tables, stage by stage (value regions)
     int32_t n_stages;
     int32_t n_warps;

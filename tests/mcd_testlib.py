@@ -28,7 +28,8 @@ class DagInfo(C.Structure):
                 ("n_preds", C.c_int64), ("window_slots", C.c_int32), ("window_in_smem", C.c_int32),
                 ("n_orphan_links", C.c_int32), ("device", C.c_int32), ("device_bytes", C.c_int64),
                 ("n_stages", C.c_int32), ("smem_bytes", C.c_int32), ("positive", C.c_int32),
-                ("tables_in_smem", C.c_int32), ("cache_hit", C.c_int32)]
+                ("tables_in_smem", C.c_int32), ("cache_hit", C.c_int32), ("n_event_pairs", C.c_int32),
+                ("block_draws", C.c_int64)]
 
 
 class DagOptions(C.Structure):

@@ -29,7 +29,7 @@ def test_library_exports_every_header_symbol():
 def test_abi_version_and_last_error():
     L = lib()
     L.mcd_abi_version.restype = C.c_int
-    assert L.mcd_abi_version() == 3
+    assert L.mcd_abi_version() == 4
     assert isinstance(last_error(), str)
 
 
@@ -188,3 +188,60 @@ def test_compiler_layout_decisions():
     assert rc == MCD_OK and info.tables_in_smem == 0
     rc, info, msg = describe(W.config0()[0], [("empirical_absolute", 1, vals[:100], np.ones(100)), ("constant", 2, 0.5)])
     assert rc == MCD_OK and info.tables_in_smem == 1
+
+
+def _block_draws_per_event(flat: dict, gen: list) -> float:
+    """Philox blocks per event when every event is its own work unit: the links an
+    event references first share blocks of four words in predecessor order (one
+    word for exponential and small tables, shape-k Erlang gamma k words), other
+    random links draw blocks of their own.  A restatement of the compiler's rule
+    without event pairs, for the five-kind layered DAGs (each link referenced once)."""
+    words = {"exponential": 1, "empirical_absolute": 1, "empirical_relative": 1}
+    per_type = {}
+    for g in gen:
+        if g[0] == "gamma":
+            per_type[g[1]] = int(g[2]) if float(g[2]) in (1.0, 2.0, 3.0) else -1
+        else:
+            per_type[g[1]] = words.get(g[0], 0)
+    draws = 0
+    off, act, typ = flat["pred_offsets"], flat["pred_act"], flat["act_type"]
+    for k in range(len(flat["target"])):
+        used = None
+        for a in act[off[k]:off[k + 1]]:
+            w = per_type.get(int(typ[a]), 0)
+            if w < 0:
+                draws += 1
+            elif w > 0:
+                if used is None or used + w > 4:
+                    draws += 1
+                    used = 0
+                used += w
+    return draws / len(flat["earliest"])
+
+
+def test_event_pairs_share_philox_blocks():
+    """The compiler runs pairs of events of one level whose draws fit one block of
+    four words back to back on one warp, so they draw one block between them: on
+    the five-kind benchmark shape the blocks a sample draws fall by about 30 %
+    against one unit per event, and the fixed-duration DAG draws none."""
+    from mc_dagprop_gb300 import workloads as W
+    from mcd_testlib import describe
+
+    flat, gen = W.config1(n_layers=200)
+    rc, info, msg = describe(flat, gen)
+    assert rc == MCD_OK, msg
+    E = info.n_events
+    single = _block_draws_per_event(flat, gen)
+    assert 1.0 < single < 1.1
+    assert info.n_event_pairs > 0.3 * E
+    assert info.block_draws / E < 0.75 * single
+    # the units depend on the levels alone: the same under other warps per CTA and
+    # with the window in global rows (other stage splits)
+    for env in ({"MCD_WARPS": "3"}, {"MCD_NO_SMEM_WINDOW": "1"}):
+        rc, other, msg = describe(flat, gen, env=env)
+        assert rc == MCD_OK, msg
+        assert (other.n_warps, other.window_in_smem, other.n_stages) != (info.n_warps, info.window_in_smem,
+                                                                         info.n_stages)
+        assert (other.n_event_pairs, other.block_draws) == (info.n_event_pairs, info.block_draws)
+    rc, info, msg = describe(flat, [("constant", t, 1.0) for t in range(1, 6)])
+    assert rc == MCD_OK and info.block_draws == 0 and info.n_event_pairs == 0

@@ -285,3 +285,67 @@ def test_unstaged_stage_tables_and_draws(cuda):
         elif g[0] == "exponential":
             ref = PM.exponential_durations(seeds, l, base, g[2], g[3], block=block[l], word=word[l])
             np.testing.assert_allclose(dur[:, l], ref, rtol=2e-6)
+
+
+def _erlang_durations(seeds, base, shape, scale, block, word):
+    """Shape-k Erlang gamma without truncation, the kernel's float32 formula:
+    X = -scale * log(U_w * ... * U_{w+k-1}) from words w.. of the block,
+    duration base * (1 + X)."""
+    r = PM.words(seeds, block)
+    prod = PM.u01_open0(r[word]).astype(np.float32)
+    for j in range(1, shape):
+        prod = (prod * PM.u01_open0(r[word + j])).astype(np.float32)
+    X = np.maximum(-np.float32(scale) * np.log(prod), np.float32(0.0)).astype(np.float32)
+    return np.array([PM.scale_by(base, np.float32(1.0) + x) for x in X])
+
+
+def test_event_pairs_share_blocks_draw_for_draw(cuda):
+    """Events of one level run in pairs whose draws share Philox blocks: on a
+    layered five-kind DAG every sampled link's durations match the model at the
+    (block, word) the compiled DAG reports, blocks are shared between links of
+    two different events, and the draws are the same under other warps per CTA
+    and with the window in global rows."""
+    from mc_dagprop_gb300 import batching
+
+    flat = W.layered_dag(41, 30, 40, 3, [1, 2, 3, 4, 5], 3600.0)
+    gen = SHARED_GEN[:5]
+    prop = propagator_from_flat(m, flat, gen)
+    info = prop.info()
+    assert info["n_event_pairs"] > 0.2 * info["n_events"]
+    block, word = prop.link_streams()
+    L = len(flat["act_duration"])
+    event_of = np.full(L, -1, np.int64)
+    off, tgt, act = flat["pred_offsets"], flat["target"], flat["pred_act"]
+    for k in range(len(tgt)):
+        event_of[act[off[k]:off[k + 1]]] = tgt[k]
+    by_block = {}
+    for l in range(L):
+        if block[l] >= 0 and word[l] >= 0:
+            by_block.setdefault(int(block[l]), set()).add(int(event_of[l]))
+    assert sum(len(evs) > 1 for evs in by_block.values()) > 0.2 * info["n_event_pairs"]
+    seeds = SEEDS[:2000]
+    _, dur, _ = prop.run_many_arrays(seeds)
+    kinds = flat["act_type"]
+    gmap = {g[1]: g for g in gen}
+    checked = 0
+    for l in range(L):
+        g, base = gmap[int(kinds[l])], float(flat["act_duration"][l])
+        if g[0].startswith("empirical"):
+            ref = PM.empirical_durations(seeds, l, base, g[2], g[3], g[0] == "empirical_relative",
+                                         block=block[l], word=word[l])
+            assert np.array_equal(dur[:, l], ref), l
+        elif g[0] == "exponential":
+            ref = PM.exponential_durations(seeds, l, base, g[2], g[3], block=block[l], word=word[l])
+            np.testing.assert_allclose(dur[:, l], ref, rtol=2e-6)
+        elif g[0] == "gamma":
+            ref = _erlang_durations(seeds, base, int(g[2]), g[3], block[l], word[l])
+            np.testing.assert_allclose(dur[:, l], ref, rtol=2e-6)
+        else:
+            continue
+        checked += 1
+    assert checked > 0.7 * L
+    for n_warps, window in ((4, "auto"), (12, "global")):
+        other = batching.compile_dag(flat, gen, n_warps, window)
+        assert other.info()["n_event_pairs"] == info["n_event_pairs"]
+        _, d2, _ = other.run_many_arrays(seeds[:256])
+        assert np.array_equal(d2.view(np.int64), dur[:256].view(np.int64))

@@ -136,7 +136,9 @@ int mcd_batch_create(mcd_dag *const *dags, int32_t n_dags, const int64_t *seed0,
         B->n_items = (int64_t)items.size() / 2;
         if (B->n_items > (int64_t)INT32_MAX) throw McdError(MCD_ERR_INVALID, "too many work items");
         const size_t E = (size_t)B->total_E;
-        const size_t s_acc = align_up(E * 8, 256), s_hist = align_up(E * kHistStride * 4, 256), s_ctr = 256,
+        // one queue head per launch, 64 bytes apart (up to eight kernel variants)
+        const size_t s_acc = align_up(E * 8, 256), s_hist = align_up(E * kHistStride * 4, 256),
+                     s_ctr = align_up(B->launches.size() * 64, 256),
                      s_out = align_up(5 * E * 8, 256), s_te = align_up(E * 8, 256),
                      s_args = align_up((size_t)n_dags * sizeof(KArgs), 256),
                      s_fargs = align_up((size_t)n_dags * sizeof(FArgs), 256),

@@ -140,3 +140,40 @@ def test_tuner_choice_holds_on_held_out_dags(cuda):
                                 use_cache=False)
     best = min(held_t.values())
     assert held_t[f"{nw}/{win}"] <= 1.25 * best, (c, nw, win, cal_t, held_t)
+
+
+def test_batch_all_eight_kernel_variants(cuda):
+    """A batch whose DAGs need all eight kernel variants (window on chip or in
+    global rows, positive times or not, distribution tables in shared or global
+    memory): eight persistent launches, each with its own queue head; over two
+    runs every DAG gets exactly its single-DAG statistics."""
+    from mc_dagprop_gb300 import batching
+
+    rng = np.random.default_rng(8)
+    small = W.gen_five_types(rng)
+    big = [g if g[1] != 4 else ("empirical_absolute", 4, np.arange(1000) * 0.3, rng.random(1000) + 0.01)
+           for g in small]
+    props, seed0, ns, variants = [], [], [], set()
+    k = 0
+    for window in ("auto", "global"):
+        for positive in (True, False):
+            for gen in (small, big):
+                flat = W.layered_dag(60 + k, 8, 24, 2, [1, 2, 3, 4, 5], 1800.0)
+                if not positive:
+                    flat = dict(flat, earliest=flat["earliest"] - 400.0)
+                p = batching.compile_dag(flat, gen, 8, window)
+                info = p.info()
+                variants.add((info["window_in_smem"], info["positive"], info["tables_in_smem"]))
+                props.append(p)
+                seed0.append(1000 * k)
+                ns.append(96 + 40 * k)
+                k += 1
+    assert len(variants) == 8
+    batch = m.Batch(props, seed0, ns)
+    for rep in range(2):
+        batch.run()
+        for i, p in enumerate(props):
+            got = batch.stats(i)
+            ref = p.run_stats(n=ns[i], seed0=seed0[i])
+            for key in ("mean", "p50", "p90", "p99", "p_on_time"):
+                assert np.array_equal(got[key], ref[key]), (rep, i, key)

@@ -393,7 +393,8 @@ def serve(server, requests, rate, seed=7):
             "completed_seconds": wall, "submit_seconds": submit_s, "max_submit_lag_s": late,
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "max": float(lat.max())},
-            "errors": len(errors)}
+            "errors": len(errors),
+            "error_messages": {msg: errors.count(msg) for msg in sorted(set(errors))[:5]}}
 
 
 def plain_serving(requests, compile_threads):

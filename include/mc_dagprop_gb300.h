@@ -292,7 +292,9 @@ int mcd_gradient_plan(const mcd_dag *dag, int64_t *samples_per_chunk, int64_t *l
  * per CTA and CTAs per SM, the class of the oldest waiting request -- as one
  * persistent batch.  A request's statistics equal those of the same request run
  * alone with mcd_stats_*.  Requests whose window does not fit in shared memory
- * are rejected.  wait() returns done = 1 and the statistics (and the latency
+ * run in batches of their own with per-CTA realized rows in global memory
+ * (outside memory_budget: events x 32 samples x 8 B per CTA of such a batch, at
+ * most one CTA per 32-sample tile).  wait() returns done = 1 and the statistics (and the latency
  * from submit to completion) when the request has finished, done = 0 when it is
  * still pending after wait_ms, or the request's error. */
 typedef struct mcd_server mcd_server;

@@ -16,8 +16,8 @@
 //     Philox is keyed by the sample's seed, the link and the attempt.)
 //   - Requests are batched by class: equal warps per CTA, equal CTAs per SM for
 //     their shared-memory layout (so no request lowers another's occupancy) and
-//     the same kernel variant (positive times or not, tables in shared memory or
-//     not).
+//     the same kernel variant (window in shared memory or in per-CTA scratch
+//     rows, positive times or not, tables in shared memory or not).
 //   - One scheduler thread, whenever one of its stream slots is free, launches
 //     the uploaded requests of the class of the oldest waiting request as one
 //     batch (the persistent k_batch_stats over (request, tile) items, then the
@@ -167,6 +167,8 @@ struct Slot {
     char *meta_dev = nullptr;   // KArgs[], FArgs[], items, queue head
     char *meta_pinned = nullptr;
     size_t meta_bytes = 0;
+    double *scratch = nullptr;  // per-CTA realized rows of a batch whose windows are off chip
+    size_t scratch_bytes = 0;
     double *pinned = nullptr;   // statistics of the batch, host side
     size_t pinned_elems = 0;
     std::vector<void *> retired;  // outgrown pinned buffers
@@ -466,15 +468,13 @@ void compile_loop(mcd_server *S) {
             if (mine) {
                 try {
                     compile_dag(d, r->gen, R->h, warps);
-                    if (!R->h.win_smem)  // the served kernel keeps every window on chip
-                        throw McdError(MCD_ERR_INVALID, "request DAG's window does not fit in shared memory");
                     R->lay = img_layout_of(R->h);
                     R->bytes = R->lay.total;
                     if ((int64_t)(R->bytes + rq_layout_of(R->h.E).total) > S->opt.memory_budget)
                         throw McdError(MCD_ERR_INVALID, "request needs more device memory than the server's budget");
                     int per_sm = 0;
-                    cuda_check(batch_blocks_per_sm(true, R->h.positive, R->h.tables_in_smem, R->h.n_warps,
-                                                   (size_t)R->h.smem_total, &per_sm),
+                    cuda_check(batch_blocks_per_sm(R->h.win_smem, R->h.positive, R->h.tables_in_smem,
+                                                   R->h.n_warps, (size_t)R->h.smem_total, &per_sm),
                                "occupancy query");
                     R->per_sm = std::max(1, per_sm);
                     R->tile_cost = (double)R->h.pred.size() + 2.0 * R->h.E;
@@ -670,13 +670,26 @@ void launch_batch(mcd_server *S, Slot &slot, std::vector<Request *> &batch) {
     ba.items = reinterpret_cast<const int32_t *>(slot.meta_dev + s_ka + s_fa);
     ba.n_items = (int32_t)n_items;
     ba.counter = reinterpret_cast<unsigned int *>(slot.meta_dev + s_ka + s_fa + s_items);
-    ba.scratch = nullptr;  // requests keep their window in shared memory (checked at compile)
-    ba.scratch_stride = 0;
     ba.smem_bytes = (int32_t)smem;
     const HostDag &h0 = batch[0]->res->h;
     const int32_t nw = h0.n_warps;
-    const int grid = batch[0]->res->per_sm * S->sms;  // the class's CTAs per SM, on every SM
-    cuda_check(launch_batch_stats(ba, true, h0.positive, h0.tables_in_smem, nw, smem, grid, st),
+    int grid = batch[0]->res->per_sm * S->sms;  // the class's CTAs per SM, on every SM
+    ba.scratch = nullptr;
+    ba.scratch_stride = 0;
+    if (!h0.win_smem) {  // windows off chip: realized rows of 32 samples per CTA, at most one CTA per item
+        grid = (int)std::min<size_t>((size_t)grid, n_items);
+        ba.scratch_stride = (int64_t)max_E * kTile;
+        const size_t bytes = (size_t)grid * (size_t)ba.scratch_stride * sizeof(double);
+        if (bytes > slot.scratch_bytes) {  // the slot is idle: nothing in flight uses the old rows
+            if (slot.scratch) cuda_check(cudaFreeAsync(slot.scratch, st), "slot scratch free");
+            slot.scratch = nullptr;
+            slot.scratch_bytes = 0;
+            cuda_check(cudaMallocAsync(reinterpret_cast<void **>(&slot.scratch), bytes, st), "slot scratch");
+            slot.scratch_bytes = bytes;
+        }
+        ba.scratch = slot.scratch;
+    }
+    cuda_check(launch_batch_stats(ba, h0.win_smem, h0.positive, h0.tables_in_smem, nw, smem, grid, st),
                "batch launch");
     cuda_check(launch_batch_finish(reinterpret_cast<const FArgs *>(slot.meta_dev + s_ka), (int32_t)nb, max_E, st),
                "batch finish");
@@ -727,11 +740,12 @@ std::vector<Request *> take_class(mcd_server *S) {
     const Request *first = S->ready.front();
     const HostDag &h0 = first->res->h;
     const int32_t nw = h0.n_warps, per_sm = first->res->per_sm;
-    const bool positive = h0.positive, tsmem = h0.tables_in_smem;
+    const bool positive = h0.positive, tsmem = h0.tables_in_smem, win_smem = h0.win_smem;
     std::deque<Request *> rest;
     for (Request *r : S->ready) {
         const HostDag &h = r->res->h;
         if (h.n_warps == nw && r->res->per_sm == per_sm && h.positive == positive && h.tables_in_smem == tsmem &&
+            h.win_smem == win_smem &&
             (S->opt.max_batch <= 0 || (int32_t)batch.size() < S->opt.max_batch))
             batch.push_back(r);
         else
@@ -842,6 +856,7 @@ void mcd_server_destroy(mcd_server *S) {
     for (Slot &s : S->slots) {
         if (s.stream) cudaStreamSynchronize(s.stream);
         if (s.meta_dev) cudaFree(s.meta_dev);
+        if (s.scratch) cudaFree(s.scratch);
         if (s.meta_pinned) cudaFreeHost(s.meta_pinned);
         if (s.pinned) cudaFreeHost(s.pinned);
         for (void *p : s.retired) cudaFreeHost(p);

@@ -118,3 +118,23 @@ def test_tight_budget_with_many_compile_threads_makes_progress(cuda):
     for (f, g, n, s0), r in zip(same, got[:len(same)]):
         alone = batching.compile_dag(f, g, 8).run_stats(n=n, seed0=s0)
         assert np.array_equal(r["mean"], alone["mean"])
+
+
+def test_server_serves_dags_whose_window_is_off_chip(cuda):
+    """A DAG whose live events exceed the shared-memory window is served from
+    per-CTA realized rows in global memory, in batches of its own class, beside
+    DAGs whose window is on chip: every request equals its single run."""
+    wide = W.layered_dag(3, 6, 1500, 1, [1, 2], 10.0)
+    small, gsmall = W.config0()
+    two = list(W.GEN_TWO_TYPES)
+    assert not batching.compile_dag(wide, two, 8).info()["window_in_smem"]
+    server = m.Server(memory_budget=8 << 30, n_streams=2, n_warps=0, compile_threads=2)
+    reqs = [(wide, two, 300, 5), (small, gsmall, 500, 7), (wide, two, 100, 11), (small, gsmall, 64, 13)]
+    tickets = [_submit(server, f, g, s0, n) for f, g, n, s0 in reqs]
+    for (f, g, n, s0), t in zip(reqs, tickets):
+        got = server.wait(t, timeout_ms=60_000)
+        assert got is not None
+        alone = batching.compile_dag(f, g, 8).run_stats(n=n, seed0=s0)
+        for k in ("mean", "p50", "p90", "p99", "p_on_time"):
+            assert np.array_equal(got[k], alone[k]), k
+    assert server.counters()["completed"] == len(reqs)

@@ -245,3 +245,21 @@ def test_event_pairs_share_philox_blocks():
         assert (other.n_event_pairs, other.block_draws) == (info.n_event_pairs, info.block_draws)
     rc, info, msg = describe(flat, [("constant", t, 1.0) for t in range(1, 6)])
     assert rc == MCD_OK and info.block_draws == 0 and info.n_event_pairs == 0
+
+
+def test_serving_stream_compiles():
+    """500 requests of the serving stream (fresh layered DAGs of 200-20,000 events,
+    five delay kinds) compile on the host -- event pairs, stages and the layout
+    check of every compile included -- and most of them pair events."""
+    from mc_dagprop_gb300 import workloads as W
+    from mcd_testlib import describe
+
+    rng = np.random.default_rng(4)
+    paired = 0
+    for _ in range(500):
+        flat, gen, _, _ = W.fresh_request(rng)
+        rc, info, msg = describe(flat, gen)
+        assert rc == MCD_OK, msg
+        assert 2 * info.n_event_pairs <= info.n_events and info.block_draws <= info.n_preds
+        paired += info.n_event_pairs > 0
+    assert paired > 400
